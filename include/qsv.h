@@ -1,0 +1,150 @@
+/*
+ * qsv.h — C ABI of the GB300 state-vector library (libqsv.so).
+ *
+ * The library holds one dense 2^n state vector per handle in HBM (complex64 or
+ * complex128, interleaved re/im, amplitude index bit (n-1-q) holds qubit q, so qubit 0
+ * is the most significant bit — the reference's convention, qip/ext/kronprod.pyx:168).
+ * Every call is asynchronous on the handle's CUDA stream unless it returns a host
+ * value.  Every entry point returns an int status (QSV_OK == 0); qsv_last_error()
+ * gives the message of the last failure on a handle.  No entry point traps, asserts on
+ * the device or spins without a bound: device-side waits give up with QSV_ERR_TIMEOUT.
+ *
+ * Qubit indices in every call use the reference's global qubit index (0 = MSB).
+ * A matrix acting on targets (t_0, ..., t_{k-1}) is 2^k x 2^k complex128, row-major,
+ * interleaved, with t_0 the most significant bit of the row/column index
+ * (qip/ext/kronprod.pyx:184-189).
+ *
+ * Each declaration names the reference interface it replaces (path within the
+ * Renmusxd/QIP project).
+ */
+#ifndef QSV_H
+#define QSV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct qsv_state qsv_state;
+
+enum qsv_dtype { QSV_C64 = 0, QSV_C128 = 1 };
+
+enum qsv_status {
+  QSV_OK = 0,
+  QSV_ERR_INVALID = 1,     /* bad argument: maps to ValueError / Exception          */
+  QSV_ERR_OOM = 2,         /* device allocation failed: maps to MemoryError         */
+  QSV_ERR_CUDA = 3,        /* a CUDA runtime call failed                             */
+  QSV_ERR_TIMEOUT = 4,     /* a bounded device wait gave up                          */
+  QSV_ERR_UNSUPPORTED = 5  /* valid request outside what the library implements      */
+};
+
+/* ---- lifetime --------------------------------------------------------------------
+ * Replaces the numpy state/arena pair that CythonBackend owns
+ * (qip/backend.py:68-71, 88, 103).  One device buffer; updates are in place, so there
+ * is no arena.  The state starts as |0...0>. */
+int qsv_create(int n, int dtype, qsv_state** out);
+int qsv_destroy(qsv_state* s);
+/* Use an external CUDA stream (cudaStream_t passed as void*; NULL = the handle's own). */
+int qsv_set_stream(qsv_state* s, void* stream);
+int qsv_synchronize(qsv_state* s);
+int qsv_num_qubits(const qsv_state* s);
+int qsv_dtype(const qsv_state* s);
+/* Device pointer of the amplitude buffer (for zero-copy interop). */
+void* qsv_device_ptr(qsv_state* s);
+const char* qsv_last_error(const qsv_state* s);
+const char* qsv_status_string(int status);
+/* Number of kernels this library launched in the calling process so far. */
+unsigned long long qsv_launch_count(void);
+
+/* ---- state preparation / readout -------------------------------------------------- */
+/* Product state from fed registers.  Replaces CythonBackend.make_state and
+ * qip.util.gen_edit_indices (qip/backend.py:73-104, qip/util.py:108-124):
+ * amp[i] = prod_g feed_g[bits of i at group g's qubits, first qubit = MSB] when every
+ * unfed qubit of i is 0, else 0; no feeds -> |0...0>.  Feeds are complex128,
+ * concatenated in group order (group g holds 2^group_sizes[g] values); not normalised. */
+int qsv_set_product_state(qsv_state* s, int ngroups, const int* group_sizes,
+                          const int* qubits_flat, const double* feeds_c128);
+/* Overwrite amplitudes [start, start+count) from host data of the handle's dtype.
+ * Replaces StateType.overwrite_relative_range (qip/backend.py:171-172). */
+int qsv_write_range(qsv_state* s, const void* host, uint64_t start, uint64_t count);
+/* Add host data to amplitudes [start, start+count).
+ * Replaces StateType.addto_relative_range (qip/backend.py:174-175). */
+int qsv_add_range(qsv_state* s, const void* host, uint64_t start, uint64_t count);
+/* Copy amplitudes [start, start+count) to host memory of the handle's dtype.  Blocks.
+ * Replaces CythonBackend.get_state / get_relative_range (qip/backend.py:106-107,168-169). */
+int qsv_read_range(qsv_state* s, void* host, uint64_t start, uint64_t count);
+
+/* ---- gates (kronselect_dot) ---------------------------------------------------------
+ * The reference applies every gate through cdot_loop (qip/ext/kronprod.pyx:41-200) via
+ * StateType.kronselect_dot (qip/backend.py:112-116).  The host layer splits a
+ * kronselect_dot dict into the calls below; each is in place.  Controls must all be 1
+ * (the CMat structure, qip/operators.py:233-268, kronprod.pyx:215-225). */
+
+/* Dense 2^k x 2^k matrix on k targets (1 <= k <= 5), optional controls. */
+int qsv_apply_matrix(qsv_state* s, int k, const int* targets, int ncontrols,
+                     const int* controls, const double* mat_c128);
+/* Diagonal matrix diag(d_0..d_{2^k-1}) on k targets (k <= 10), optional controls.
+ * Only amplitudes whose diagonal entry differs from 1 are read or written. */
+int qsv_apply_diagonal(qsv_state* s, int k, const int* targets, int ncontrols,
+                       const int* controls, const double* diag_c128);
+/* Monomial matrix (exactly one non-zero per row): out[r] = phase[r] * in[perm[r]].
+ * Entries whose phase is exactly 1 move data without arithmetic (bit-exact). */
+int qsv_apply_monomial(qsv_state* s, int k, const int* targets, int ncontrols,
+                       const int* controls, const int* perm, const double* phase_c128);
+/* Exchange the m-qubit register a with register b (SwapMat, qip/operators.py:157-179,
+ * kronprod.pyx:227-231), optional controls.  Pure data movement, bit-exact. */
+int qsv_apply_swap(qsv_state* s, int m, const int* a, const int* b, int ncontrols,
+                   const int* controls);
+/* Fused dense blocks on the tensor cores (complex64 handles only): for each block b,
+ * a 2^k_b x 2^k_b matrix (4 <= k_b <= 6) applied to all 2^(n-k_b) groups as a
+ * split-bf16 GEMM with FP32 accumulation (tcgen05).  No reference counterpart: the
+ * reference applies one kronselect_dot dict per pass (kronprod.pyx:157). */
+int qsv_apply_blocks(qsv_state* s, int nblocks, const int* ks, const int* targets_flat,
+                     const double* mats_c128);
+
+/* Device-resident fused-block plan: the block images are built and uploaded once, so
+ * qsv_plan_launch issues kernels only (no host work, no copies) and can be captured in
+ * a CUDA graph.  Same semantics as qsv_apply_blocks.  No reference counterpart. */
+typedef struct qsv_plan qsv_plan;
+int qsv_plan_create(qsv_state* s, int nblocks, const int* ks, const int* targets_flat,
+                    const double* mats_c128, qsv_plan** out);
+int qsv_plan_launch(qsv_state* s, const qsv_plan* p, int first, int count);
+int qsv_plan_destroy(qsv_plan* p);
+
+/* ---- measurement ---------------------------------------------------------------------
+ * Marginal probabilities over m qubits, FP64 compensated sums, out[2^m].
+ * Outcome bit j <-> qubits[j] (LSB first), as measure_probabilities
+ * (qip/ext/kronprod.pyx:238-261).  m = 0 gives the squared norm (prob_magnitude,
+ * kronprod.pyx:318-326). */
+int qsv_probabilities(qsv_state* s, int m, const int* qubits, double* out);
+/* Squared norm sum |amp|^2 (FP64).  Replaces prob_magnitude / StateType.total_prob
+ * (kronprod.pyx:318-326, qip/backend.py:123-124). */
+int qsv_norm2(qsv_state* s, double* out);
+/* Single-qubit marginals P(q = 1) of every qubit in one pass, out[n], plus the squared
+ * norm in *norm2.  No reference counterpart (one StochasticMeasure per qubit there). */
+int qsv_qubit_marginals(qsv_state* s, double* out, double* norm2);
+/* Collapse onto the outcome where the m measured qubits equal `value` (bit j of value
+ * <-> qubits[j], LSB first) and scale the kept amplitudes by `scale` (FP64).
+ * Replaces the collapse loop of measure (kronprod.pyx:430-444). */
+int qsv_collapse(qsv_state* s, int m, const int* qubits, uint64_t value, double scale);
+/* Collapse and remove the measured qubits: the state shrinks to 2^(n-m) amplitudes,
+ * remaining qubits keep their order.  Replaces reduce_measure (kronprod.pyx:449-490). */
+int qsv_reduce(qsv_state* s, int m, const int* qubits, uint64_t value, double scale);
+
+/* <a|b> = sum conj(a_i) b_i in FP64 (compensated), states of equal n, any dtypes.
+ * Used for infidelity 1 - |<a|b>|^2 / (<a|a><b|b>).  No reference counterpart. */
+int qsv_inner_product(qsv_state* a, qsv_state* b, double* re, double* im);
+
+/* ---- function oracle -----------------------------------------------------------------
+ * |x>|q>|r> -> |x>|f(x) xor q>|r> with f given as a table of 2^n1 values.
+ * Replaces func_apply (qip/ext/func_apply.pyx:9-112). */
+int qsv_func_apply(qsv_state* s, int n1, const int* reg1, int n2, const int* reg2,
+                   const int64_t* table);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QSV_H */

@@ -1,0 +1,467 @@
+"""State backends: the ``StateType`` interface and the GB300 implementation.
+
+``StateType`` restates the reference's backend interface (``qip/backend.py:14-65``):
+the graph executor only ever talks to a state through these methods, so a backend
+whose ``make_state`` is passed as ``run(..., backend_constructor=...)`` runs any
+circuit unchanged (``qip/pipeline.py:95-96,133``).
+
+``GpuBackend`` keeps the state resident in HBM in one buffer (no arena: every kernel is
+in place) and drives it through libqsv's C ABI.  Calls are queued on a CUDA stream; the
+host waits only where a value comes back (state readout, probabilities, norms,
+measurement outcomes).  For complex64 states, gates are queued and fused into dense
+blocks on the tensor cores when the state is next observed.
+"""
+from __future__ import annotations
+
+import ctypes
+import random
+from typing import Callable, List, Mapping, Optional, Sequence, Tuple, Union
+
+import numpy
+
+from . import _native as nat
+from .fusion import Block, plan
+from .gates import GateOp, classify_matrix, decompose
+from .util import InitialState, IndexType, MatrixType
+
+
+class StateType(object):
+    """Backend interface of the graph executor (``qip/backend.py:14-65``)."""
+
+    def __init__(self, n: int, state: object):
+        self.n = n
+        self.state = state
+
+    def get_state(self) -> object:
+        return self.state
+
+    def kronselect_dot(self, mats: Mapping[IndexType, MatrixType],
+                       input_offset: int = 0, output_offset: int = 0) -> None:
+        raise NotImplementedError("kronselect_dot not implemented by base class")
+
+    def func_apply(self, reg1_indices: Sequence[int], reg2_indices: Sequence[int],
+                   func: Callable[[int], int], input_offset: int = 0, output_offset: int = 0) -> None:
+        raise NotImplementedError("func_apply not implemented by base class")
+
+    def total_prob(self) -> float:
+        raise NotImplementedError("total_prob not implemented by base class")
+
+    def measure(self, indices: Sequence[int], measured: Optional[int] = None,
+                measured_prob: Optional[float] = None,
+                input_offset: int = 0, output_offset: int = 0) -> Tuple[int, float]:
+        raise NotImplementedError("measure not implemented by base class")
+
+    def reduce_measure(self, indices: Sequence[int], measured: Optional[int] = None,
+                       measured_prob: Optional[float] = None,
+                       input_offset: int = 0, output_offset: int = 0) -> Tuple[int, float]:
+        raise NotImplementedError("reduce_measure not implemented by base class")
+
+    def soft_measure(self, indices: Sequence[int], measured: Optional[int] = None,
+                     input_offset: int = 0) -> Tuple[int, float]:
+        raise NotImplementedError("soft_measure not implemented by base class")
+
+    def measure_probabilities(self, indices: Sequence[int], top_k: int = 0
+                              ) -> Union[Sequence[float], Tuple[Sequence[int], Sequence[float]]]:
+        """If top_k is 0, all outcome probabilities; else (indices, probs) of the top k."""
+        raise NotImplementedError("measure_probabilities not implemented by base class")
+
+    def get_state_size(self) -> int:
+        raise NotImplementedError("get_state_size not implemented by base class")
+
+    def get_relative_range(self, start: int, end: int) -> Sequence[complex]:
+        raise NotImplementedError("get_relative_range not implemented by base class")
+
+    def overwrite_relative_range(self, start: int, end: int, data: Sequence[complex]):
+        raise NotImplementedError("overwrite_relative_range not implemented by base class")
+
+    def addto_relative_range(self, start: int, end: int, data: Sequence[complex]):
+        raise NotImplementedError("addto_relative_range not implemented by base class")
+
+    def close(self):
+        pass
+
+
+# ---- helpers shared with the measurement semantics ------------------------------------
+
+def check_measured(nindices: int, measured: Optional[int], measured_prob: Optional[float]) -> None:
+    """Argument checks of ``measure``/``reduce_measure`` (``qip/ext/kronprod.pyx:402-407``)."""
+    if measured is not None:
+        if not (0 <= measured < 2 ** nindices):
+            raise ValueError("Measured value must be less than 2**len(indices)")
+    if measured_prob is not None:
+        if not 0.0 < measured_prob <= 1.0:
+            raise ValueError("measured_prob must be 0 < p <= 1")
+
+
+def sample_outcome(probs_msb: numpy.ndarray, measured: Optional[int], r: float) -> Tuple[int, float]:
+    """Walk outcomes in order subtracting their probability from r until r <= 0
+    (``qip/ext/kronprod.pyx:371-383``).  ``probs_msb[m]`` is the probability of outcome
+    m, whose most significant bit is the smallest measured qubit index.  When
+    ``measured`` is given only that outcome is visited.  If the walk runs off the end
+    the last outcome is returned, as the reference does."""
+    lo, hi = (0, len(probs_msb)) if measured is None else (int(measured), int(measured) + 1)
+    p = 0.0
+    m = lo
+    for m in range(lo, hi):
+        p = float(probs_msb[m])
+        r -= p
+        if r <= 0:
+            break
+    return m, p
+
+
+def top_k_outcomes(probs_msb: numpy.ndarray, top_k: int) -> Tuple[List[int], List[float]]:
+    """The ``top_k`` most probable outcomes, descending; ties keep the lower outcome
+    first.  (The reference's bounded heap, ``kronprod.pyx:287-315``, writes one slot
+    past its end once more than top_k outcomes exist; this is the well-defined intent.)"""
+    top_k = min(int(top_k), len(probs_msb))
+    order = numpy.lexsort((numpy.arange(len(probs_msb)), -probs_msb))[:top_k]
+    return [numpy.int64(i) for i in order], [numpy.float64(probs_msb[i]) for i in order]
+
+
+def _feed_vector(feed, size: int) -> numpy.ndarray:
+    if isinstance(feed, (int, numpy.integer)) and not isinstance(feed, bool):
+        if not 0 <= int(feed) < size:
+            raise ValueError("basis-state feed {} outside [0, {})".format(feed, size))
+        v = numpy.zeros(size, dtype=numpy.complex128)
+        v[int(feed)] = 1.0
+        return v
+    v = numpy.asarray(feed, dtype=numpy.complex128).reshape(-1)
+    if v.shape[0] != size:
+        raise ValueError("Feed of length {} for a register of {} states".format(v.shape[0], size))
+    return v
+
+
+_DTYPES = {numpy.dtype(numpy.complex64): nat.QSV_C64, numpy.dtype(numpy.complex128): nat.QSV_C128}
+
+
+class GpuBackend(StateType):
+    """GB300 state vector behind the ``StateType`` interface.
+
+    Register it as ``run(..., backend_constructor=GpuBackend.make_state)``.  ``statetype``
+    picks the precision: ``numpy.complex128`` runs every gate on FP64 per-gate kernels;
+    ``numpy.complex64`` queues gates and applies them as fused tensor-core blocks
+    (``fusion=False`` keeps the per-gate FP32 kernels).
+    """
+
+    FLUSH_LIMIT = 8192
+
+    def __init__(self, n: int, handle: ctypes.c_void_p, statetype, fusion: bool, max_block: int = 6):
+        super().__init__(n, None)
+        self._h = handle
+        self._lib = nat.load()
+        self.statetype = numpy.dtype(statetype)
+        self.fusion = bool(fusion)
+        self.max_block = int(max_block)
+        self._pending: List[GateOp] = []
+        self.stats = {"ops": 0, "blocks": 0, "block_gates": 0, "launch_calls": 0}
+
+    # ---- construction ---------------------------------------------------------------
+    @staticmethod
+    def make_state(n: int, index_groups: Sequence[Sequence[int]], feed_list: Sequence[InitialState],
+                   inputstartindex: Optional[int] = None, inputendindex: Optional[int] = None,
+                   outputstartindex: Optional[int] = None, outputendindex: Optional[int] = None,
+                   statetype: type = numpy.complex128, fusion: Optional[bool] = None,
+                   max_block: int = 6) -> "GpuBackend":
+        """Same contract as ``CythonBackend.make_state`` (``qip/backend.py:73-104``): the
+        product of the fed register vectors at their global indices, unfed qubits |0>,
+        |0...0> without feeds, no normalisation."""
+        full = 2 ** n
+        for lo, hi in ((inputstartindex, inputendindex), (outputstartindex, outputendindex)):
+            if (lo not in (None, 0)) or (hi not in (None, full)):
+                raise ValueError("GpuBackend holds the whole state: index windows are not supported")
+        dt = numpy.dtype(statetype)
+        if dt not in _DTYPES:
+            raise ValueError("statetype must be numpy.complex64 or numpy.complex128, not {}".format(statetype))
+        lib = nat.load()
+        h = ctypes.c_void_p()
+        nat.check(lib.qsv_create(int(n), _DTYPES[dt], ctypes.byref(h)), None, "qsv_create")
+        if fusion is None:
+            fusion = dt == numpy.dtype(numpy.complex64)
+        st = GpuBackend(n, h, dt, fusion, max_block)
+        if len(feed_list) > 0:
+            st._set_product(index_groups, feed_list)
+        return st
+
+    def _set_product(self, index_groups, feed_list) -> None:
+        sizes, qubits, vecs = [], [], []
+        for group, feed in zip(index_groups, feed_list):
+            g = [int(q) for q in group]
+            sizes.append(len(g))
+            qubits.extend(g)
+            vecs.append(_feed_vector(feed, 2 ** len(g)))
+        sz = nat.int_array(sizes)
+        qb = nat.int_array(qubits)
+        feeds = numpy.ascontiguousarray(numpy.concatenate(vecs)).view(numpy.float64)
+        self._check(self._lib.qsv_set_product_state(self._h, len(sizes), nat.ip(sz), nat.ip(qb), nat.dp(feeds)),
+                    "make_state")
+
+    # ---- plumbing ---------------------------------------------------------------------
+    def _check(self, status: int, what: str) -> None:
+        nat.check(status, self._h, what)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def device_ptr(self) -> int:
+        return int(self._lib.qsv_device_ptr(self._h))
+
+    def set_stream(self, stream_ptr: int) -> None:
+        self.flush()
+        self._check(self._lib.qsv_set_stream(self._h, ctypes.c_void_p(stream_ptr)), "set_stream")
+
+    def synchronize(self) -> None:
+        self.flush()
+        self._check(self._lib.qsv_synchronize(self._h), "synchronize")
+
+    # ---- gates --------------------------------------------------------------------------
+    def kronselect_dot(self, mats: Mapping[IndexType, MatrixType],
+                       input_offset: int = 0, output_offset: int = 0) -> None:
+        """Apply a ``{indices: matrix}`` Kronecker dictionary in place (replaces
+        ``CythonBackend.kronselect_dot``, ``qip/backend.py:112-116``)."""
+        if input_offset or output_offset:
+            raise ValueError("GpuBackend holds the whole state: offsets must be 0")
+        ops = decompose(mats)
+        for op in ops:
+            for q in op.qubits:
+                if not 0 <= q < self.n:
+                    raise ValueError("qubit index {} out of range for n={}".format(q, self.n))
+        if self.fusion:
+            self._pending.extend(ops)
+            if len(self._pending) >= self.FLUSH_LIMIT:
+                self.flush()
+        else:
+            for op in ops:
+                self.apply_op(op)
+
+    def apply_ops(self, ops: Sequence[GateOp]) -> None:
+        """Queue (fusion) or launch (per-gate) pre-decomposed operations."""
+        if self.fusion:
+            self._pending.extend(ops)
+            if len(self._pending) >= self.FLUSH_LIMIT:
+                self.flush()
+        else:
+            for op in ops:
+                self.apply_op(op)
+
+    def apply_op(self, op: GateOp) -> None:
+        lib, h = self._lib, self._h
+        t = nat.int_array(op.targets)
+        c = nat.int_array(op.controls)
+        self.stats["ops"] += 1
+        self.stats["launch_calls"] += 1
+        if op.kind == "dense":
+            m = nat.c128(op.mat)
+            self._check(lib.qsv_apply_matrix(h, len(t), nat.ip(t), len(c), nat.ip(c), nat.dp(m)), "apply_matrix")
+        elif op.kind == "diag":
+            d = nat.c128(op.mat)
+            self._check(lib.qsv_apply_diagonal(h, len(t), nat.ip(t), len(c), nat.ip(c), nat.dp(d)), "apply_diagonal")
+        elif op.kind == "mono":
+            p = nat.int_array(op.perm)
+            ph = nat.c128(op.mat)
+            self._check(lib.qsv_apply_monomial(h, len(t), nat.ip(t), len(c), nat.ip(c), nat.ip(p), nat.dp(ph)),
+                        "apply_monomial")
+        elif op.kind == "swap":
+            b = nat.int_array(op.swap_b)
+            self._check(lib.qsv_apply_swap(h, len(t), nat.ip(t), nat.ip(b), len(c), nat.ip(c)), "apply_swap")
+        else:
+            raise ValueError(op.kind)
+
+    def apply_blocks(self, blocks: Sequence[Block]) -> None:
+        """Apply fused blocks of 4..6 qubits on the tensor cores (complex64 only)."""
+        if not blocks:
+            return
+        ks = nat.int_array([len(b.qubits) for b in blocks])
+        tg = nat.int_array([q for b in blocks for q in b.qubits])
+        mats = numpy.ascontiguousarray(numpy.concatenate([numpy.asarray(b.matrix, numpy.complex128).reshape(-1)
+                                                          for b in blocks])).view(numpy.float64)
+        self.stats["blocks"] += len(blocks)
+        self.stats["block_gates"] += sum(b.ngates for b in blocks)
+        self.stats["launch_calls"] += 1
+        self._check(self._lib.qsv_apply_blocks(self._h, len(blocks), nat.ip(ks), nat.ip(tg), nat.dp(mats)),
+                    "apply_blocks")
+
+    def run_plan(self, steps) -> None:
+        """Execute a fusion plan: runs of tensor-core blocks go in one call."""
+        batch: List[Block] = []
+        for st in steps:
+            if isinstance(st, Block) and len(st.qubits) >= 4 and self.n - len(st.qubits) >= 7:
+                batch.append(st)
+                continue
+            self.apply_blocks(batch)
+            batch = []
+            if isinstance(st, Block):
+                # Narrow block: one structured per-gate pass (diagonal / monomial / dense).
+                for op in classify_matrix(st.qubits, (), st.matrix):
+                    self.apply_op(op)
+            else:
+                self.apply_op(st)
+        self.apply_blocks(batch)
+
+    def flush(self) -> None:
+        """Fuse and launch every queued gate."""
+        if not self._pending:
+            return
+        pending, self._pending = self._pending, []
+        kmax = min(self.max_block, max(1, self.n - 7)) if self.n >= 11 else 3
+        self.run_plan(plan(pending, kmax=kmax))
+
+    # ---- readout -------------------------------------------------------------------------
+    def get_state(self) -> numpy.ndarray:
+        self.flush()
+        out = numpy.empty(2 ** self.n, dtype=self.statetype)
+        self._check(self._lib.qsv_read_range(self._h, out.ctypes.data_as(ctypes.c_void_p), 0, out.shape[0]),
+                    "get_state")
+        return out
+
+    def get_state_size(self) -> int:
+        return 2 ** self.n
+
+    def get_relative_range(self, start: int, end: int) -> numpy.ndarray:
+        self.flush()
+        start, end = int(start), int(end)
+        out = numpy.empty(max(0, end - start), dtype=self.statetype)
+        self._check(self._lib.qsv_read_range(self._h, out.ctypes.data_as(ctypes.c_void_p), start, out.shape[0]),
+                    "get_relative_range")
+        return out
+
+    def overwrite_relative_range(self, start: int, end: int, data: Sequence[complex]):
+        self.flush()
+        d = numpy.ascontiguousarray(numpy.asarray(data, dtype=self.statetype).reshape(-1))
+        if d.shape[0] != int(end) - int(start):
+            raise ValueError("data length does not match the range")
+        self._check(self._lib.qsv_write_range(self._h, d.ctypes.data_as(ctypes.c_void_p), int(start), d.shape[0]),
+                    "overwrite_relative_range")
+        self._lib.qsv_synchronize(self._h)
+
+    def addto_relative_range(self, start: int, end: int, data: Sequence[complex]):
+        self.flush()
+        d = numpy.ascontiguousarray(numpy.asarray(data, dtype=self.statetype).reshape(-1))
+        if d.shape[0] != int(end) - int(start):
+            raise ValueError("data length does not match the range")
+        self._check(self._lib.qsv_add_range(self._h, d.ctypes.data_as(ctypes.c_void_p), int(start), d.shape[0]),
+                    "addto_relative_range")
+        self._lib.qsv_synchronize(self._h)
+
+    # ---- probabilities and measurement ----------------------------------------------------
+    def _probs(self, qubits: Sequence[int]) -> numpy.ndarray:
+        """out[v], bit j of v <-> qubits[j] (LSB first)."""
+        self.flush()
+        q = nat.int_array(qubits)
+        out = numpy.zeros(2 ** len(q), dtype=numpy.float64)
+        self._check(self._lib.qsv_probabilities(self._h, len(q), nat.ip(q), nat.dp(out)), "probabilities")
+        return out
+
+    def _probs_msb(self, indices: Sequence[int]) -> numpy.ndarray:
+        """Outcome order of soft_measure / top-k: MSB = smallest measured qubit index
+        (``entwine_bit``, ``qip/ext/util.pyx:2-23``)."""
+        return self._probs(sorted((int(i) for i in indices), reverse=True))
+
+    def total_prob(self) -> float:
+        self.flush()
+        out = numpy.zeros(1, dtype=numpy.float64)
+        self._check(self._lib.qsv_norm2(self._h, nat.dp(out)), "total_prob")
+        return float(out[0])
+
+    def qubit_marginals(self) -> Tuple[numpy.ndarray, float]:
+        """P(qubit q = 1) for every qubit in one pass, plus the squared norm."""
+        self.flush()
+        out = numpy.zeros(self.n, dtype=numpy.float64)
+        nrm = numpy.zeros(1, dtype=numpy.float64)
+        self._check(self._lib.qsv_qubit_marginals(self._h, nat.dp(out), nat.dp(nrm)), "qubit_marginals")
+        return out, float(nrm[0])
+
+    def measure_probabilities(self, indices: Sequence[int], top_k: int = 0):
+        """Replaces ``CythonBackend.measure_probabilities`` (``qip/backend.py:158-163``):
+        all outcome probabilities with bit j <-> indices[j] (``kronprod.pyx:259``), or the
+        top_k outcomes in the MSB-first outcome order of ``kronprod.pyx:294``."""
+        if top_k:
+            return top_k_outcomes(self._probs_msb(indices), top_k)
+        return self._probs([int(i) for i in indices])
+
+    def soft_measure(self, indices: Sequence[int], measured: Optional[int] = None,
+                     input_offset: int = 0) -> Tuple[int, float]:
+        """Sample an outcome without changing the state (``kronprod.pyx:329-383``).  The
+        draw is ``random.random()`` scaled by the state's squared norm."""
+        if input_offset:
+            raise ValueError("GpuBackend holds the whole state: offsets must be 0")
+        probs = self._probs_msb(indices)
+        r = random.random() * float(probs.sum())
+        return sample_outcome(probs, measured, r)
+
+    def _outcome_pattern(self, indices: Sequence[int], m: int) -> Tuple[List[int], int]:
+        """Qubits listed LSB first and the outcome value in that order, for outcome m in
+        the MSB-first encoding."""
+        qs = sorted((int(i) for i in indices), reverse=True)
+        return qs, int(m)
+
+    def measure(self, indices: Sequence[int], measured: Optional[int] = None,
+                measured_prob: Optional[float] = None,
+                input_offset: int = 0, output_offset: int = 0) -> Tuple[int, float]:
+        """Measure and collapse (``kronprod.pyx:386-446``): amplitudes disagreeing with
+        the outcome become 0, the rest are scaled by sqrt(1/p) in FP64."""
+        if input_offset or output_offset:
+            raise ValueError("GpuBackend holds the whole state: offsets must be 0")
+        indices = [int(i) for i in indices]
+        check_measured(len(indices), measured, measured_prob)
+        if measured is None or measured_prob is None:
+            m, p = self.soft_measure(indices, measured=measured)
+        else:
+            m, p = int(measured), float(measured_prob)
+        self.flush()
+        qs, v = self._outcome_pattern(indices, m)
+        q = nat.int_array(qs)
+        scale = float(numpy.sqrt(1.0 / p))
+        self._check(self._lib.qsv_collapse(self._h, len(q), nat.ip(q), v, scale), "measure")
+        return m, p
+
+    def reduce_measure(self, indices: Sequence[int], measured: Optional[int] = None,
+                       measured_prob: Optional[float] = None,
+                       input_offset: int = 0, output_offset: int = 0) -> Tuple[int, float]:
+        """Measure and remove the measured qubits; the state shrinks to 2^(n-len) and
+        the remaining qubits keep their order (intent of ``kronprod.pyx:449-490``)."""
+        if input_offset or output_offset:
+            raise ValueError("GpuBackend holds the whole state: offsets must be 0")
+        indices = [int(i) for i in indices]
+        check_measured(len(indices), measured, measured_prob)
+        if measured is None or measured_prob is None:
+            m, p = self.soft_measure(indices, measured=measured)
+        else:
+            m, p = int(measured), float(measured_prob)
+        self.flush()
+        qs, v = self._outcome_pattern(indices, m)
+        q = nat.int_array(qs)
+        scale = float(numpy.sqrt(1.0 / p))
+        self._check(self._lib.qsv_reduce(self._h, len(q), nat.ip(q), v, scale), "reduce_measure")
+        self.n -= len(indices)
+        return m, p
+
+    # ---- function oracle ------------------------------------------------------------------
+    def func_apply(self, reg1_indices: Sequence[int], reg2_indices: Sequence[int],
+                   func: Callable[[int], int], input_offset: int = 0, output_offset: int = 0) -> None:
+        """|x>|q>|r> -> |x>|f(x) xor q>|r> (``qip/ext/func_apply.pyx:9-112``).  f is
+        tabulated on the host over all 2^len(reg1) inputs, as the reference's
+        ``pregen`` path does, keeping the low len(reg2) bits of each value."""
+        self.flush()
+        r1 = [int(i) for i in reg1_indices]
+        r2 = [int(i) for i in reg2_indices]
+        mask = (1 << len(r2)) - 1
+        table = numpy.array([int(func(x)) & mask for x in range(2 ** len(r1))], dtype=numpy.int64)
+        a1, a2 = nat.int_array(r1), nat.int_array(r2)
+        self._check(self._lib.qsv_func_apply(self._h, len(a1), nat.ip(a1), len(a2), nat.ip(a2),
+                                             table.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))),
+                    "func_apply")
+
+    # ---- lifetime -------------------------------------------------------------------------
+    def close(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h:
+            self._pending = []
+            self._lib.qsv_destroy(h)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,1251 @@
+// libqsv core: handle lifetime, state preparation and readout, the per-gate HBM
+// kernels (dense / diagonal / monomial / register swap), measurement reductions and
+// the function-oracle permutation.  The tensor-core fused-block path lives in
+// qsv_fused.cu.
+//
+// Layout: one dense vector of 2^n amplitudes (float2 or double2) in HBM; amplitude
+// index bit (n-1-q) is qubit q (qubit 0 = most significant bit), the reference's
+// convention (qip/ext/kronprod.pyx:168, 187-189).  Updates are in place.
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "qsv_internal.cuh"
+
+namespace qsv {
+
+std::atomic<unsigned long long> g_launches{0};
+static char g_global_err[512] = {0};
+static std::mutex g_global_err_mu;
+
+int set_error(qsv_state* s, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (s) {
+    memcpy(s->err, buf, sizeof(buf));
+  } else {
+    std::lock_guard<std::mutex> lk(g_global_err_mu);
+    memcpy(g_global_err, buf, sizeof(buf));
+  }
+  return code;
+}
+
+int ensure_scratch(qsv_state* s, size_t bytes) {
+  if (bytes <= s->scratch_bytes) return QSV_OK;
+  size_t want = std::max(bytes, s->scratch_bytes * 2);
+  want = (want + 255) & ~size_t(255);
+  if (s->d_scratch) {
+    // The old scratch may still be read by queued kernels.
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return set_error(s, QSV_ERR_CUDA, "sync: %s", cudaGetErrorString(e));
+    cudaFree(s->d_scratch);
+    s->d_scratch = nullptr;
+    s->scratch_bytes = 0;
+  }
+  if (cudaMalloc(&s->d_scratch, want) != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(s, QSV_ERR_OOM, "scratch allocation of %zu bytes failed", want);
+  }
+  s->scratch_bytes = want;
+  return QSV_OK;
+}
+
+int check_launch(qsv_state* s, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(s, QSV_ERR_CUDA, "%s launch: %s", what, cudaGetErrorString(e));
+  count_launch();
+  return QSV_OK;
+}
+
+unsigned grid_for(const qsv_state* s, uint64_t work, unsigned per_block, unsigned waves) {
+  uint64_t blocks = (work + per_block - 1) / per_block;
+  uint64_t cap = (uint64_t)std::max(1, s->sm_count) * waves;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return (unsigned)blocks;
+}
+
+int to_positions(qsv_state* s, int count, const int* qubits, int* pos_out, uint64_t* seen_mask) {
+  if (count < 0 || count > QSV_MAXQ) return set_error(s, QSV_ERR_INVALID, "too many qubits (%d)", count);
+  if (count > 0 && qubits == nullptr) return set_error(s, QSV_ERR_INVALID, "null qubit list");
+  for (int i = 0; i < count; ++i) {
+    const int q = qubits[i];
+    if (q < 0 || q >= s->n)
+      return set_error(s, QSV_ERR_INVALID, "qubit index %d out of range for n=%d", q, s->n);
+    const int p = s->n - 1 - q;
+    if (*seen_mask & (1ull << p)) return set_error(s, QSV_ERR_INVALID, "qubit %d repeated", q);
+    *seen_mask |= 1ull << p;
+    pos_out[i] = p;
+  }
+  return QSV_OK;
+}
+
+}  // namespace qsv
+
+using namespace qsv;
+
+// ======================================================================================
+// Kernels
+// ======================================================================================
+namespace {
+
+template <typename R>
+using CT = typename C2T<R>::type;
+
+template <typename R>
+__global__ void k_set_basis(CT<R>* psi, uint64_t index) {
+  CT<R> one;
+  one.x = R(1);
+  one.y = R(0);
+  psi[index] = one;
+}
+
+// ---- product state: amp[i] = prod_g feed_g[sub_g(i)] (qip/backend.py:94-101) ---------
+struct ProductArgs {
+  uint64_t total;
+  uint64_t unfed_mask;
+  int ngroups;
+  int nq;                       // total fed qubits
+  int size[QSV_MAXQ];           // qubits per group
+  int pos[QSV_MAXQ];            // bit positions, group by group, first = MSB of the group
+  uint64_t feed_off[QSV_MAXQ];  // offset of group g's vector in the feed buffer
+};
+
+template <typename R>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_product(CT<R>* __restrict__ psi, const double2* __restrict__ feeds,
+              const __grid_constant__ ProductArgs a) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < a.total; i += stride) {
+    CT<R> out;
+    if (i & a.unfed_mask) {
+      out.x = R(0);
+      out.y = R(0);
+    } else {
+      double2 acc = make_double2(1.0, 0.0);
+      int q = 0;
+      for (int g = 0; g < a.ngroups; ++g) {
+        uint64_t sub = 0;
+        for (int j = 0; j < a.size[g]; ++j, ++q) sub = (sub << 1) | ((i >> a.pos[q]) & 1ull);
+        const double2 f = feeds[a.feed_off[g] + sub];
+        acc = make_double2(acc.x * f.x - acc.y * f.y, acc.x * f.y + acc.y * f.x);
+      }
+      out.x = R(acc.x);
+      out.y = R(acc.y);
+    }
+    psi[i] = out;
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_add_range(CT<R>* __restrict__ psi, const CT<R>* __restrict__ src, uint64_t count) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count; i += stride) {
+    CT<R> a = psi[i];
+    const CT<R> b = src[i];
+    a.x += b.x;
+    a.y += b.y;
+    psi[i] = a;
+  }
+}
+
+// ---- dense k-qubit gate with controls -------------------------------------------------
+template <typename R, int K>
+struct DenseArgs {
+  uint64_t ngroups;
+  uint64_t ctrl;               // OR-ed into every group base (controls == 1)
+  uint64_t off[1 << K];        // state offset of matrix index j (targets[0] = MSB)
+  int npos;
+  int pos[QSV_MAXQ];           // target+control bit positions, ascending
+  CT<R> m[(1 << K) * (1 << K)];  // row-major
+};
+
+template <typename R, int K>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_dense(CT<R>* __restrict__ psi, const __grid_constant__ DenseArgs<R, K> a) {
+  constexpr int D = 1 << K;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < a.ngroups; g += stride) {
+    const uint64_t base = qsv_insert_zeros(g, a.pos, a.npos) | a.ctrl;
+    CT<R> v[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) v[j] = psi[base + a.off[j]];
+    if constexpr (K <= 3) {
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        CT<R> acc;
+        acc.x = R(0);
+        acc.y = R(0);
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc = qsv_cfma(a.m[r * D + c], v[c], acc);
+        psi[base + a.off[r]] = acc;
+      }
+    } else {
+#pragma unroll 1
+      for (int r = 0; r < D; ++r) {
+        CT<R> acc;
+        acc.x = R(0);
+        acc.y = R(0);
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc = qsv_cfma(a.m[r * D + c], v[c], acc);
+        psi[base + a.off[r]] = acc;
+      }
+    }
+  }
+}
+
+// Specialised single-qubit dense gate without controls: the most common plain pass.
+template <typename R>
+struct Dense1Args {
+  uint64_t ngroups;
+  int p;  // target bit position
+  CT<R> m00, m01, m10, m11;
+};
+
+template <typename R>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_dense1(CT<R>* __restrict__ psi, const __grid_constant__ Dense1Args<R> a) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t lowmask = (1ull << a.p) - 1ull;
+  const uint64_t hi = 1ull << a.p;
+  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < a.ngroups; g += stride) {
+    const uint64_t i0 = ((g >> a.p) << (a.p + 1)) | (g & lowmask);
+    const CT<R> x = psi[i0];
+    const CT<R> y = psi[i0 + hi];
+    CT<R> o0, o1;
+    o0.x = R(0); o0.y = R(0); o1 = o0;
+    o0 = qsv_cfma(a.m00, x, o0);
+    o0 = qsv_cfma(a.m01, y, o0);
+    o1 = qsv_cfma(a.m10, x, o1);
+    o1 = qsv_cfma(a.m11, y, o1);
+    psi[i0] = o0;
+    psi[i0 + hi] = o1;
+  }
+}
+
+// ---- diagonal: only entries != 1 are touched ------------------------------------------
+constexpr int QSV_MAXDIAG = 256;
+template <typename R>
+struct DiagArgs {
+  uint64_t ngroups;
+  uint64_t ctrl;
+  int npos;
+  int pos[QSV_MAXQ];
+  int nent;
+  uint64_t off[QSV_MAXDIAG];
+  CT<R> ph[QSV_MAXDIAG];
+};
+
+template <typename R>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_diag(CT<R>* __restrict__ psi, const __grid_constant__ DiagArgs<R> a) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < a.ngroups; g += stride) {
+    const uint64_t base = qsv_insert_zeros(g, a.pos, a.npos) | a.ctrl;
+    for (int e = 0; e < a.nent; ++e) {
+      const uint64_t idx = base + a.off[e];
+      psi[idx] = qsv_cmul(a.ph[e], psi[idx]);
+    }
+  }
+}
+
+// ---- monomial: out[r] = phase[r] * in[perm[r]] ----------------------------------------
+template <typename R, int K>
+struct MonoArgs {
+  uint64_t ngroups;
+  uint64_t ctrl;
+  int npos;
+  int pos[QSV_MAXQ];
+  uint64_t off[1 << K];
+  int perm[1 << K];
+  unsigned exact;  // bit r set: phase[r] == 1, move without arithmetic
+  CT<R> ph[1 << K];
+};
+
+template <typename R, int K>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_mono(CT<R>* __restrict__ psi, const __grid_constant__ MonoArgs<R, K> a) {
+  constexpr int D = 1 << K;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < a.ngroups; g += stride) {
+    const uint64_t base = qsv_insert_zeros(g, a.pos, a.npos) | a.ctrl;
+    CT<R> v[D];
+#pragma unroll
+    for (int j = 0; j < D; ++j) v[j] = psi[base + a.off[j]];
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      CT<R> x = v[0];
+#pragma unroll
+      for (int c = 1; c < D; ++c)
+        if (a.perm[r] == c) x = v[c];
+      if (!((a.exact >> r) & 1u)) x = qsv_cmul(a.ph[r], x);
+      psi[base + a.off[r]] = x;
+    }
+  }
+}
+
+// ---- register swap (SwapMat) -----------------------------------------------------------
+struct SwapArgs {
+  uint64_t nitems;  // 2^(n - ncontrols)
+  uint64_t ctrl;
+  int ncp;
+  int cpos[QSV_MAXQ];  // control positions ascending
+  int m;
+  int apos[QSV_MAXQ / 2];  // register a, first = MSB
+  int bpos[QSV_MAXQ / 2];
+};
+
+template <typename R>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_swap(CT<R>* __restrict__ psi, const __grid_constant__ SwapArgs a) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < a.nitems; t += stride) {
+    const uint64_t idx = qsv_insert_zeros(t, a.cpos, a.ncp) | a.ctrl;
+    unsigned x = 0, y = 0;
+    uint64_t flip = 0;
+    for (int j = 0; j < a.m; ++j) {
+      const unsigned xb = (idx >> a.apos[j]) & 1u;
+      const unsigned yb = (idx >> a.bpos[j]) & 1u;
+      x = (x << 1) | xb;
+      y = (y << 1) | yb;
+      if (xb != yb) flip |= (1ull << a.apos[j]) | (1ull << a.bpos[j]);
+    }
+    if (x < y) {
+      const uint64_t partner = idx ^ flip;
+      const CT<R> u = psi[idx];
+      const CT<R> w = psi[partner];
+      psi[idx] = w;
+      psi[partner] = u;
+    }
+  }
+}
+
+// ---- measurement reductions ---------------------------------------------------------------
+// Neumaier-compensated FP64 accumulation.
+struct Acc {
+  double s = 0.0, c = 0.0;
+  __device__ __forceinline__ void add(double x) {
+    const double t = s + x;
+    if (fabs(s) >= fabs(x))
+      c += (s - t) + x;
+    else
+      c += (x - t) + s;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return s + c; }
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of one double per thread (result valid in thread 0).
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  return r;
+}
+
+struct ProbArgs {
+  uint64_t nrest;   // 2^(n-m) amplitudes per outcome
+  uint64_t chunk;   // amplitudes per block along the rest index
+  uint64_t nchunks;
+  uint64_t nbins;
+  int m;
+  int npos;
+  int pos[QSV_MAXQ];          // measured positions ascending (zero insertion)
+  uint64_t binbit[QSV_MAXQ];  // outcome bit j -> state mask of qubits[j]
+};
+
+// partial[bin * nchunks + chunk] = sum over one chunk of the rest index.
+template <typename R>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_probs_partial(const CT<R>* __restrict__ psi, const __grid_constant__ ProbArgs a,
+                    double* __restrict__ partial) {
+  __shared__ double sh[32];
+  const uint64_t blk = blockIdx.x + (uint64_t)blockIdx.y * gridDim.x;
+  if (blk >= a.nbins * a.nchunks) return;
+  const uint64_t bin = blk / a.nchunks;
+  const uint64_t chunk = blk - bin * a.nchunks;
+  uint64_t binbase = 0;
+  for (int j = 0; j < a.m; ++j)
+    if ((bin >> j) & 1ull) binbase |= a.binbit[j];
+  const uint64_t r0 = chunk * a.chunk;
+  const uint64_t r1 = min(r0 + a.chunk, a.nrest);
+  Acc acc;
+  for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    const uint64_t idx = qsv_insert_zeros(r, a.pos, a.npos) | binbase;
+    const CT<R> v = psi[idx];
+    const double x = (double)v.x, y = (double)v.y;
+    acc.add(fma(x, x, y * y));
+  }
+  const double tot = block_sum(acc.value(), sh);
+  if (threadIdx.x == 0) partial[blk] = tot;
+}
+
+// One thread per outcome, looping over the rest index (used when outcomes are many).
+template <typename R>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_probs_perbin(const CT<R>* __restrict__ psi, const __grid_constant__ ProbArgs a,
+                   double* __restrict__ out) {
+  const uint64_t bin = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (bin >= a.nbins) return;
+  uint64_t binbase = 0;
+  for (int j = 0; j < a.m; ++j)
+    if ((bin >> j) & 1ull) binbase |= a.binbit[j];
+  Acc acc;
+  for (uint64_t r = 0; r < a.nrest; ++r) {
+    const uint64_t idx = qsv_insert_zeros(r, a.pos, a.npos) | binbase;
+    const CT<R> v = psi[idx];
+    const double x = (double)v.x, y = (double)v.y;
+    acc.add(fma(x, x, y * y));
+  }
+  out[bin] = acc.value();
+}
+
+// out[b] = compensated sum of partial[b*nchunks .. +nchunks), one warp per outcome.
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_probs_finish(const double* __restrict__ partial, uint64_t nchunks, uint64_t nbins,
+                   double* __restrict__ out) {
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= nbins) return;
+  Acc acc;
+  for (uint64_t c = lane; c < nchunks; c += 32) acc.add(partial[warp * nchunks + c]);
+  // Combine lanes: exchange (s, c) pairs and keep compensating.
+  double s = acc.s, cc = acc.c;
+  for (int o = 16; o > 0; o >>= 1) {
+    const double os = __shfl_xor_sync(0xffffffffu, s, o);
+    const double oc = __shfl_xor_sync(0xffffffffu, cc, o);
+    const double t = s + os;
+    double e;
+    if (fabs(s) >= fabs(os))
+      e = (s - t) + os;
+    else
+      e = (os - t) + s;
+    s = t;
+    cc = cc + oc + e;
+  }
+  if (lane == 0) out[warp] = s + cc;
+}
+
+// All single-qubit marginals in one pass.  Block b owns amplitudes
+// [b*chunk, (b+1)*chunk) with chunk = 2^cbits >= 2^13; thread t visits t + 256*j.
+// Positions 0..7 are fixed per thread, 8..cbits-1 vary with j, >= cbits fixed per block.
+// partial[b*(n+1) + p] = sum |a|^2 over the chunk with bit p set; [.. + n] = chunk total.
+template <typename R>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_marginals_partial(const CT<R>* __restrict__ psi, int n, int cbits,
+                        double* __restrict__ partial) {
+  __shared__ double sh[32];
+  const uint64_t base = (uint64_t)blockIdx.x << cbits;
+  const uint64_t per_thread = 1ull << (cbits - 8);
+  double tot = 0.0;
+  double vb[QSV_MAXN];  // varying bits 8..cbits-1 (indexed by p-8)
+#pragma unroll
+  for (int p = 0; p < QSV_MAXN; ++p) vb[p] = 0.0;
+  for (uint64_t j = 0; j < per_thread; ++j) {
+    const uint64_t idx = base + threadIdx.x + (j << 8);
+    const CT<R> v = psi[idx];
+    const double x = (double)v.x, y = (double)v.y;
+    const double pr = fma(x, x, y * y);
+    tot += pr;
+#pragma unroll
+    for (int p = 0; p < QSV_MAXN - 8; ++p)
+      if (p < cbits - 8 && ((j >> p) & 1ull)) vb[p] += pr;
+  }
+  const double blocktot = block_sum(tot, sh);
+  if (threadIdx.x == 0) partial[(uint64_t)blockIdx.x * (n + 1) + n] = blocktot;
+  for (int p = 0; p < 8 && p < n; ++p) {
+    const double s = block_sum(((threadIdx.x >> p) & 1u) ? tot : 0.0, sh);
+    if (threadIdx.x == 0) partial[(uint64_t)blockIdx.x * (n + 1) + p] = s;
+  }
+#pragma unroll
+  for (int p = 0; p < QSV_MAXN - 8; ++p) {
+    if (p < cbits - 8) {
+      const double s = block_sum(vb[p], sh);
+      if (threadIdx.x == 0) partial[(uint64_t)blockIdx.x * (n + 1) + 8 + p] = s;
+    }
+  }
+  for (int p = cbits; p < n; ++p) {
+    if (threadIdx.x == 0)
+      partial[(uint64_t)blockIdx.x * (n + 1) + p] = ((blockIdx.x >> (p - cbits)) & 1u) ? blocktot : 0.0;
+  }
+}
+
+// Column sums of partial[nblocks][n+1], one warp per column.
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_columns_finish(const double* __restrict__ partial, uint64_t nrows, int ncols,
+                     double* __restrict__ out) {
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= (uint64_t)ncols) return;
+  Acc acc;
+  for (uint64_t r = lane; r < nrows; r += 32) acc.add(partial[r * ncols + warp]);
+  double s = acc.s, cc = acc.c;
+  for (int o = 16; o > 0; o >>= 1) {
+    const double os = __shfl_xor_sync(0xffffffffu, s, o);
+    const double oc = __shfl_xor_sync(0xffffffffu, cc, o);
+    const double t = s + os;
+    double e;
+    if (fabs(s) >= fabs(os))
+      e = (s - t) + os;
+    else
+      e = (os - t) + s;
+    s = t;
+    cc = cc + oc + e;
+  }
+  if (lane == 0) out[warp] = s + cc;
+}
+
+// ---- collapse / reduce --------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_collapse(CT<R>* __restrict__ psi, uint64_t total, uint64_t mask, uint64_t pattern,
+               double scale) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += stride) {
+    CT<R> v;
+    if ((i & mask) == pattern) {
+      v = psi[i];
+      v.x = R((double)v.x * scale);
+      v.y = R((double)v.y * scale);
+    } else {
+      v.x = R(0);
+      v.y = R(0);
+    }
+    psi[i] = v;
+  }
+}
+
+struct ReduceArgs {
+  uint64_t total_out;
+  uint64_t pattern;
+  int npos;
+  int pos[QSV_MAXQ];
+  double scale;
+};
+
+template <typename R>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_reduce(const CT<R>* __restrict__ src, CT<R>* __restrict__ dst,
+             const __grid_constant__ ReduceArgs a) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < a.total_out; j += stride) {
+    CT<R> v = src[qsv_insert_zeros(j, a.pos, a.npos) | a.pattern];
+    v.x = R((double)v.x * a.scale);
+    v.y = R((double)v.y * a.scale);
+    dst[j] = v;
+  }
+}
+
+// ---- function oracle: out[x, y, r] = in[x, y ^ f(x), r] ----------------------------------
+struct FuncArgs {
+  uint64_t total;
+  int n1, n2;
+  int p1[QSV_MAXQ];  // reg1 positions, first = MSB of x
+  int p2[QSV_MAXQ];  // reg2 positions, first = MSB of y
+};
+
+template <typename R>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_func(const CT<R>* __restrict__ src, CT<R>* __restrict__ dst,
+           const long long* __restrict__ table, const __grid_constant__ FuncArgs a) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < a.total; i += stride) {
+    uint64_t x = 0;
+    for (int j = 0; j < a.n1; ++j) x = (x << 1) | ((i >> a.p1[j]) & 1ull);
+    const uint64_t f = (uint64_t)table[x];
+    uint64_t flip = 0;
+    for (int j = 0; j < a.n2; ++j)
+      if ((f >> (a.n2 - 1 - j)) & 1ull) flip |= 1ull << a.p2[j];
+    dst[i] = src[i ^ flip];
+  }
+}
+
+// ---- inner product <a|b> over two states (any dtype pair) --------------------------------
+template <typename RA, typename RB>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_inner_partial(const CT<RA>* __restrict__ a, const CT<RB>* __restrict__ b, uint64_t total,
+                    double* __restrict__ partial) {
+  __shared__ double sh[32];
+  Acc re, im;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += stride) {
+    const CT<RA> x = a[i];
+    const CT<RB> y = b[i];
+    const double xr = x.x, xi = x.y, yr = y.x, yi = y.y;
+    re.add(fma(xr, yr, xi * yi));
+    im.add(fma(xr, yi, -xi * yr));
+  }
+  const double r = block_sum(re.value(), sh);
+  const double q = block_sum(im.value(), sh);
+  if (threadIdx.x == 0) {
+    partial[2 * blockIdx.x] = r;
+    partial[2 * blockIdx.x + 1] = q;
+  }
+}
+
+}  // namespace
+
+// ======================================================================================
+// Host side
+// ======================================================================================
+namespace {
+
+inline bool is_c64(const qsv_state* s) { return s->dtype == QSV_C64; }
+
+template <typename R>
+CT<R> to_ct(const double* c) {
+  CT<R> v;
+  v.x = R(c[0]);
+  v.y = R(c[1]);
+  return v;
+}
+
+int launch_basis(qsv_state* s, uint64_t index) {
+  if (is_c64(s))
+    k_set_basis<float><<<1, 1, 0, s->stream>>>((float2*)s->d_amp, index);
+  else
+    k_set_basis<double><<<1, 1, 0, s->stream>>>((double2*)s->d_amp, index);
+  return check_launch(s, "set_basis");
+}
+
+// Collects target/control positions and checks they are disjoint.
+struct GateGeom {
+  int k = 0, nc = 0;
+  int tpos[QSV_MAXQ];
+  int cpos[QSV_MAXQ];
+  int sorted[QSV_MAXQ];
+  int npos = 0;
+  uint64_t ctrl = 0;
+};
+
+int gate_geometry(qsv_state* s, int k, const int* targets, int nc, const int* controls, GateGeom& g) {
+  if (k < 0 || nc < 0 || k + nc > QSV_MAXQ || k + nc > s->n)
+    return set_error(s, QSV_ERR_INVALID, "bad gate width k=%d controls=%d for n=%d", k, nc, s->n);
+  uint64_t seen = 0;
+  int rc = to_positions(s, k, targets, g.tpos, &seen);
+  if (rc) return rc;
+  rc = to_positions(s, nc, controls, g.cpos, &seen);
+  if (rc) return rc;
+  g.k = k;
+  g.nc = nc;
+  g.npos = k + nc;
+  for (int i = 0; i < k; ++i) g.sorted[i] = g.tpos[i];
+  for (int i = 0; i < nc; ++i) {
+    g.sorted[k + i] = g.cpos[i];
+    g.ctrl |= 1ull << g.cpos[i];
+  }
+  std::sort(g.sorted, g.sorted + g.npos);
+  return QSV_OK;
+}
+
+uint64_t target_offset(const GateGeom& g, unsigned j) {
+  uint64_t off = 0;
+  for (int b = 0; b < g.k; ++b)
+    if ((j >> (g.k - 1 - b)) & 1u) off |= 1ull << g.tpos[b];
+  return off;
+}
+
+template <typename R, int K>
+int launch_dense(qsv_state* s, const GateGeom& g, const double* mat) {
+  constexpr int D = 1 << K;
+  const uint64_t ngroups = 1ull << (s->n - g.k - g.nc);
+  if (K == 1 && g.nc == 0) {
+    Dense1Args<R> a;
+    a.ngroups = ngroups;
+    a.p = g.tpos[0];
+    a.m00 = to_ct<R>(mat + 0);
+    a.m01 = to_ct<R>(mat + 2);
+    a.m10 = to_ct<R>(mat + 4);
+    a.m11 = to_ct<R>(mat + 6);
+    k_dense1<R><<<grid_for(s, ngroups), QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, a);
+    return check_launch(s, "dense1");
+  }
+  auto* a = new (std::nothrow) DenseArgs<R, K>();
+  if (!a) return set_error(s, QSV_ERR_OOM, "host allocation failed");
+  a->ngroups = ngroups;
+  a->ctrl = g.ctrl;
+  a->npos = g.npos;
+  for (int i = 0; i < g.npos; ++i) a->pos[i] = g.sorted[i];
+  for (int j = 0; j < D; ++j) a->off[j] = target_offset(g, j);
+  for (int j = 0; j < D * D; ++j) a->m[j] = to_ct<R>(mat + 2 * j);
+  k_dense<R, K><<<grid_for(s, ngroups), QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, *a);
+  delete a;
+  return check_launch(s, "dense");
+}
+
+template <typename R>
+int dispatch_dense(qsv_state* s, const GateGeom& g, const double* mat) {
+  switch (g.k) {
+    case 1: return launch_dense<R, 1>(s, g, mat);
+    case 2: return launch_dense<R, 2>(s, g, mat);
+    case 3: return launch_dense<R, 3>(s, g, mat);
+    case 4: return launch_dense<R, 4>(s, g, mat);
+    case 5: return launch_dense<R, 5>(s, g, mat);
+    default: return set_error(s, QSV_ERR_UNSUPPORTED, "dense gate on %d targets (max 5)", g.k);
+  }
+}
+
+template <typename R>
+int launch_diag(qsv_state* s, const GateGeom& g, const double* diag) {
+  auto* a = new (std::nothrow) DiagArgs<R>();
+  if (!a) return set_error(s, QSV_ERR_OOM, "host allocation failed");
+  a->ngroups = 1ull << (s->n - g.k - g.nc);
+  a->ctrl = g.ctrl;
+  a->npos = g.npos;
+  for (int i = 0; i < g.npos; ++i) a->pos[i] = g.sorted[i];
+  int ne = 0;
+  for (unsigned j = 0; j < (1u << g.k); ++j) {
+    if (diag[2 * j] == 1.0 && diag[2 * j + 1] == 0.0) continue;
+    if (ne >= QSV_MAXDIAG) {
+      delete a;
+      return set_error(s, QSV_ERR_UNSUPPORTED, "diagonal with more than %d non-unit entries", QSV_MAXDIAG);
+    }
+    a->off[ne] = target_offset(g, j);
+    a->ph[ne] = to_ct<R>(diag + 2 * j);
+    ++ne;
+  }
+  a->nent = ne;
+  int rc = QSV_OK;
+  if (ne > 0) {
+    k_diag<R><<<grid_for(s, a->ngroups), QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, *a);
+    rc = check_launch(s, "diag");
+  }
+  delete a;
+  return rc;
+}
+
+template <typename R, int K>
+int launch_mono(qsv_state* s, const GateGeom& g, const int* perm, const double* phase) {
+  constexpr int D = 1 << K;
+  MonoArgs<R, K> a;
+  a.ngroups = 1ull << (s->n - g.k - g.nc);
+  a.ctrl = g.ctrl;
+  a.npos = g.npos;
+  for (int i = 0; i < g.npos; ++i) a.pos[i] = g.sorted[i];
+  a.exact = 0;
+  for (int r = 0; r < D; ++r) {
+    if (perm[r] < 0 || perm[r] >= D) return set_error(s, QSV_ERR_INVALID, "permutation entry out of range");
+    a.off[r] = target_offset(g, r);
+    a.perm[r] = perm[r];
+    a.ph[r] = to_ct<R>(phase + 2 * r);
+    if (phase[2 * r] == 1.0 && phase[2 * r + 1] == 0.0) a.exact |= 1u << r;
+  }
+  k_mono<R, K><<<grid_for(s, a.ngroups), QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, a);
+  return check_launch(s, "monomial");
+}
+
+template <typename R>
+int dispatch_mono(qsv_state* s, const GateGeom& g, const int* perm, const double* phase) {
+  switch (g.k) {
+    case 1: return launch_mono<R, 1>(s, g, perm, phase);
+    case 2: return launch_mono<R, 2>(s, g, perm, phase);
+    case 3: return launch_mono<R, 3>(s, g, perm, phase);
+    default: return set_error(s, QSV_ERR_UNSUPPORTED, "monomial gate on %d targets (max 3)", g.k);
+  }
+}
+
+template <typename R>
+int launch_probs(qsv_state* s, int m, const int* pos_in_order, double* d_out_or_null,
+                 double* host_out) {
+  // pos_in_order[j] = bit position of outcome bit j.
+  ProbArgs a;
+  a.m = m;
+  a.npos = m;
+  uint64_t nbins = 1ull << m;
+  a.nbins = nbins;
+  a.nrest = 1ull << (s->n - m);
+  for (int j = 0; j < m; ++j) {
+    a.binbit[j] = 1ull << pos_in_order[j];
+    a.pos[j] = pos_in_order[j];
+  }
+  std::sort(a.pos, a.pos + m);
+  const uint64_t target_blocks = (uint64_t)std::max(1, s->sm_count) * 32;
+  int rc;
+  if (nbins > 65535ull * 8 || (a.nrest < 4096 && nbins >= 4096)) {
+    // Many outcomes, short sums: one thread per outcome.
+    rc = ensure_scratch(s, nbins * sizeof(double));
+    if (rc) return rc;
+    double* out = (double*)s->d_scratch;
+    a.chunk = a.nrest;
+    a.nchunks = 1;
+    const unsigned blocks = (unsigned)((nbins + QSV_THREADS - 1) / QSV_THREADS);
+    k_probs_perbin<R><<<blocks, QSV_THREADS, 0, s->stream>>>((const CT<R>*)s->d_amp, a, out);
+    rc = check_launch(s, "probs_perbin");
+    if (rc) return rc;
+    QSV_CUDA(s, cudaMemcpyAsync(host_out, out, nbins * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    QSV_CUDA(s, cudaStreamSynchronize(s->stream));
+    return QSV_OK;
+  }
+  uint64_t chunk = 4096;
+  while (chunk < a.nrest && nbins * ((a.nrest + chunk - 1) / chunk) > target_blocks) chunk <<= 1;
+  if (chunk > a.nrest) chunk = a.nrest;
+  a.chunk = chunk;
+  a.nchunks = (a.nrest + chunk - 1) / chunk;
+  const uint64_t nblk = nbins * a.nchunks;
+  rc = ensure_scratch(s, (nblk + nbins) * sizeof(double));
+  if (rc) return rc;
+  double* partial = (double*)s->d_scratch;
+  double* out = partial + nblk;
+  dim3 grid;
+  grid.x = (unsigned)std::min<uint64_t>(nblk, 65535ull * 1024);
+  grid.y = (unsigned)((nblk + grid.x - 1) / grid.x);
+  k_probs_partial<R><<<grid, QSV_THREADS, 0, s->stream>>>((const CT<R>*)s->d_amp, a, partial);
+  rc = check_launch(s, "probs_partial");
+  if (rc) return rc;
+  const unsigned fblocks = (unsigned)((nbins * 32 + QSV_THREADS - 1) / QSV_THREADS);
+  k_probs_finish<<<fblocks, QSV_THREADS, 0, s->stream>>>(partial, a.nchunks, nbins, out);
+  rc = check_launch(s, "probs_finish");
+  if (rc) return rc;
+  (void)d_out_or_null;
+  QSV_CUDA(s, cudaMemcpyAsync(host_out, out, nbins * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  QSV_CUDA(s, cudaStreamSynchronize(s->stream));
+  return QSV_OK;
+}
+
+}  // namespace
+
+// ======================================================================================
+// C ABI
+// ======================================================================================
+extern "C" {
+
+const char* qsv_status_string(int status) {
+  switch (status) {
+    case QSV_OK: return "ok";
+    case QSV_ERR_INVALID: return "invalid argument";
+    case QSV_ERR_OOM: return "out of device memory";
+    case QSV_ERR_CUDA: return "CUDA error";
+    case QSV_ERR_TIMEOUT: return "device wait timed out";
+    case QSV_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+const char* qsv_last_error(const qsv_state* s) { return s ? s->err : g_global_err; }
+
+unsigned long long qsv_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int qsv_create(int n, int dtype, qsv_state** out) {
+  if (!out) return set_error(nullptr, QSV_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (n < 1 || n > QSV_MAXN) return set_error(nullptr, QSV_ERR_INVALID, "n=%d outside [1, %d]", n, QSV_MAXN);
+  if (dtype != QSV_C64 && dtype != QSV_C128) return set_error(nullptr, QSV_ERR_INVALID, "unknown dtype %d", dtype);
+  auto* s = new (std::nothrow) qsv_state();
+  if (!s) return set_error(nullptr, QSV_ERR_OOM, "host allocation failed");
+  s->n = n;
+  s->dtype = dtype;
+  s->amp_bytes = dtype == QSV_C64 ? 8 : 16;
+  cudaError_t e = cudaGetDevice(&s->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete s;
+    return set_error(nullptr, QSV_ERR_CUDA, "device setup: %s", cudaGetErrorString(e));
+  }
+  s->stream = s->own_stream;
+  const size_t bytes = (size_t(1) << n) * s->amp_bytes;
+  if (cudaMalloc(&s->d_amp, bytes) != cudaSuccess || cudaMalloc(&s->d_flag, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    if (s->d_amp) cudaFree(s->d_amp);
+    cudaStreamDestroy(s->own_stream);
+    delete s;
+    return set_error(nullptr, QSV_ERR_OOM, "device allocation of %zu bytes failed", bytes);
+  }
+  int rc = QSV_OK;
+  if (cudaMemsetAsync(s->d_amp, 0, bytes, s->stream) != cudaSuccess ||
+      cudaMemsetAsync(s->d_flag, 0, sizeof(int), s->stream) != cudaSuccess)
+    rc = set_error(nullptr, QSV_ERR_CUDA, "memset failed");
+  if (!rc) rc = launch_basis(s, 0);
+  if (rc) {
+    if (!s->err[0]) set_error(nullptr, rc, "initialisation failed");
+    else set_error(nullptr, rc, "%s", s->err);
+    qsv_destroy(s);
+    return rc;
+  }
+  *out = s;
+  return QSV_OK;
+}
+
+int qsv_destroy(qsv_state* s) {
+  if (!s) return QSV_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->d_amp) cudaFree(s->d_amp);
+  if (s->d_flag) cudaFree(s->d_flag);
+  if (s->d_scratch) cudaFree(s->d_scratch);
+  if (s->d_images) cudaFree(s->d_images);
+  if (s->h_images) cudaFreeHost(s->h_images);
+  if (s->h_stage) cudaFreeHost(s->h_stage);
+  if (s->images_done) cudaEventDestroy(s->images_done);
+  if (s->own_stream) cudaStreamDestroy(s->own_stream);
+  delete s;
+  return QSV_OK;
+}
+
+int qsv_set_stream(qsv_state* s, void* stream) {
+  QSV_CHECK_HANDLE(s);
+  QSV_CUDA(s, cudaStreamSynchronize(s->stream));
+  s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+  return QSV_OK;
+}
+
+int qsv_synchronize(qsv_state* s) {
+  QSV_CHECK_HANDLE(s);
+  QSV_CUDA(s, cudaStreamSynchronize(s->stream));
+  int flag = 0;
+  QSV_CUDA(s, cudaMemcpy(&flag, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag) {
+    cudaMemset(s->d_flag, 0, sizeof(int));
+    return set_error(s, QSV_ERR_TIMEOUT, "a bounded device wait gave up (code %d)", flag);
+  }
+  return QSV_OK;
+}
+
+int qsv_num_qubits(const qsv_state* s) { return s ? s->n : -1; }
+int qsv_dtype(const qsv_state* s) { return s ? s->dtype : -1; }
+void* qsv_device_ptr(qsv_state* s) { return s ? s->d_amp : nullptr; }
+
+int qsv_set_product_state(qsv_state* s, int ngroups, const int* group_sizes, const int* qubits_flat,
+                          const double* feeds_c128) {
+  QSV_CHECK_HANDLE(s);
+  const uint64_t total = 1ull << s->n;
+  if (ngroups == 0) {
+    QSV_CUDA(s, cudaMemsetAsync(s->d_amp, 0, total * s->amp_bytes, s->stream));
+    return launch_basis(s, 0);
+  }
+  if (ngroups < 0 || ngroups > QSV_MAXQ || !group_sizes || !qubits_flat || !feeds_c128)
+    return set_error(s, QSV_ERR_INVALID, "bad feed description");
+  ProductArgs a;
+  a.total = total;
+  a.ngroups = ngroups;
+  uint64_t seen = 0;
+  int q = 0;
+  uint64_t nfeed = 0;
+  for (int g = 0; g < ngroups; ++g) {
+    const int sz = group_sizes[g];
+    if (sz < 1 || q + sz > s->n) return set_error(s, QSV_ERR_INVALID, "feed group %d has bad size %d", g, sz);
+    int rc = to_positions(s, sz, qubits_flat + q, a.pos + q, &seen);
+    if (rc) return rc;
+    a.size[g] = sz;
+    a.feed_off[g] = nfeed;
+    nfeed += 1ull << sz;
+    q += sz;
+  }
+  a.nq = q;
+  a.unfed_mask = ((s->n == 64) ? ~0ull : ((1ull << s->n) - 1ull)) & ~seen;
+  int rc = ensure_scratch(s, nfeed * sizeof(double2));
+  if (rc) return rc;
+  QSV_CUDA(s, cudaMemcpyAsync(s->d_scratch, feeds_c128, nfeed * sizeof(double2), cudaMemcpyHostToDevice, s->stream));
+  const unsigned grid = grid_for(s, total);
+  if (is_c64(s))
+    k_product<float><<<grid, QSV_THREADS, 0, s->stream>>>((float2*)s->d_amp, (const double2*)s->d_scratch, a);
+  else
+    k_product<double><<<grid, QSV_THREADS, 0, s->stream>>>((double2*)s->d_amp, (const double2*)s->d_scratch, a);
+  return check_launch(s, "product_state");
+}
+
+int qsv_write_range(qsv_state* s, const void* host, uint64_t start, uint64_t count) {
+  QSV_CHECK_HANDLE(s);
+  if (start + count > (1ull << s->n) || (count && !host))
+    return set_error(s, QSV_ERR_INVALID, "range [%llu, +%llu) outside the state", (unsigned long long)start,
+                     (unsigned long long)count);
+  if (!count) return QSV_OK;
+  QSV_CUDA(s, cudaMemcpyAsync((char*)s->d_amp + start * s->amp_bytes, host, count * s->amp_bytes,
+                              cudaMemcpyHostToDevice, s->stream));
+  return QSV_OK;
+}
+
+int qsv_add_range(qsv_state* s, const void* host, uint64_t start, uint64_t count) {
+  QSV_CHECK_HANDLE(s);
+  if (start + count > (1ull << s->n) || (count && !host))
+    return set_error(s, QSV_ERR_INVALID, "range outside the state");
+  if (!count) return QSV_OK;
+  int rc = ensure_scratch(s, count * s->amp_bytes);
+  if (rc) return rc;
+  QSV_CUDA(s, cudaMemcpyAsync(s->d_scratch, host, count * s->amp_bytes, cudaMemcpyHostToDevice, s->stream));
+  const unsigned grid = grid_for(s, count);
+  if (is_c64(s))
+    k_add_range<float><<<grid, QSV_THREADS, 0, s->stream>>>((float2*)s->d_amp + start, (const float2*)s->d_scratch, count);
+  else
+    k_add_range<double><<<grid, QSV_THREADS, 0, s->stream>>>((double2*)s->d_amp + start, (const double2*)s->d_scratch, count);
+  return check_launch(s, "add_range");
+}
+
+int qsv_read_range(qsv_state* s, void* host, uint64_t start, uint64_t count) {
+  QSV_CHECK_HANDLE(s);
+  if (start + count > (1ull << s->n) || (count && !host))
+    return set_error(s, QSV_ERR_INVALID, "range outside the state");
+  if (!count) return QSV_OK;
+  QSV_CUDA(s, cudaMemcpyAsync(host, (const char*)s->d_amp + start * s->amp_bytes, count * s->amp_bytes,
+                              cudaMemcpyDeviceToHost, s->stream));
+  QSV_CUDA(s, cudaStreamSynchronize(s->stream));
+  return QSV_OK;
+}
+
+int qsv_apply_matrix(qsv_state* s, int k, const int* targets, int ncontrols, const int* controls,
+                     const double* mat_c128) {
+  QSV_CHECK_HANDLE(s);
+  if (!mat_c128) return set_error(s, QSV_ERR_INVALID, "null matrix");
+  if (k < 1) return set_error(s, QSV_ERR_INVALID, "matrix gate needs at least one target");
+  GateGeom g;
+  int rc = gate_geometry(s, k, targets, ncontrols, controls, g);
+  if (rc) return rc;
+  return is_c64(s) ? dispatch_dense<float>(s, g, mat_c128) : dispatch_dense<double>(s, g, mat_c128);
+}
+
+int qsv_apply_diagonal(qsv_state* s, int k, const int* targets, int ncontrols, const int* controls,
+                       const double* diag_c128) {
+  QSV_CHECK_HANDLE(s);
+  if (!diag_c128) return set_error(s, QSV_ERR_INVALID, "null diagonal");
+  if (k > 10) return set_error(s, QSV_ERR_UNSUPPORTED, "diagonal on %d targets (max 10)", k);
+  GateGeom g;
+  int rc = gate_geometry(s, k, targets, ncontrols, controls, g);
+  if (rc) return rc;
+  return is_c64(s) ? launch_diag<float>(s, g, diag_c128) : launch_diag<double>(s, g, diag_c128);
+}
+
+int qsv_apply_monomial(qsv_state* s, int k, const int* targets, int ncontrols, const int* controls,
+                       const int* perm, const double* phase_c128) {
+  QSV_CHECK_HANDLE(s);
+  if (!perm || !phase_c128) return set_error(s, QSV_ERR_INVALID, "null permutation");
+  GateGeom g;
+  int rc = gate_geometry(s, k, targets, ncontrols, controls, g);
+  if (rc) return rc;
+  return is_c64(s) ? dispatch_mono<float>(s, g, perm, phase_c128) : dispatch_mono<double>(s, g, perm, phase_c128);
+}
+
+int qsv_apply_swap(qsv_state* s, int m, const int* a, const int* b, int ncontrols, const int* controls) {
+  QSV_CHECK_HANDLE(s);
+  if (m < 1 || 2 * m + ncontrols > QSV_MAXQ || 2 * m + ncontrols > s->n)
+    return set_error(s, QSV_ERR_INVALID, "bad swap width %d", m);
+  SwapArgs args;
+  uint64_t seen = 0;
+  int rc = to_positions(s, m, a, args.apos, &seen);
+  if (!rc) rc = to_positions(s, m, b, args.bpos, &seen);
+  if (!rc) rc = to_positions(s, ncontrols, controls, args.cpos, &seen);
+  if (rc) return rc;
+  args.m = m;
+  args.ncp = ncontrols;
+  args.ctrl = 0;
+  for (int i = 0; i < ncontrols; ++i) args.ctrl |= 1ull << args.cpos[i];
+  std::sort(args.cpos, args.cpos + ncontrols);
+  args.nitems = 1ull << (s->n - ncontrols);
+  const unsigned grid = grid_for(s, args.nitems);
+  if (is_c64(s))
+    k_swap<float><<<grid, QSV_THREADS, 0, s->stream>>>((float2*)s->d_amp, args);
+  else
+    k_swap<double><<<grid, QSV_THREADS, 0, s->stream>>>((double2*)s->d_amp, args);
+  return check_launch(s, "swap");
+}
+
+int qsv_probabilities(qsv_state* s, int m, const int* qubits, double* out) {
+  QSV_CHECK_HANDLE(s);
+  if (!out) return set_error(s, QSV_ERR_INVALID, "null output");
+  if (m < 0 || m > s->n || m > 30) return set_error(s, QSV_ERR_INVALID, "bad measured count %d", m);
+  int pos[QSV_MAXQ];
+  uint64_t seen = 0;
+  int rc = to_positions(s, m, qubits, pos, &seen);
+  if (rc) return rc;
+  return is_c64(s) ? launch_probs<float>(s, m, pos, nullptr, out) : launch_probs<double>(s, m, pos, nullptr, out);
+}
+
+int qsv_norm2(qsv_state* s, double* out) { return qsv_probabilities(s, 0, nullptr, out); }
+
+int qsv_qubit_marginals(qsv_state* s, double* out, double* norm2) {
+  QSV_CHECK_HANDLE(s);
+  if (!out) return set_error(s, QSV_ERR_INVALID, "null output");
+  const int n = s->n;
+  if (n < 14) {
+    // Small states: per-qubit marginal calls.
+    double p[2];
+    double tot = 0.0;
+    for (int q = 0; q < n; ++q) {
+      int rc = qsv_probabilities(s, 1, &q, p);
+      if (rc) return rc;
+      out[q] = p[1];
+      tot = p[0] + p[1];
+    }
+    if (norm2) *norm2 = tot;
+    return QSV_OK;
+  }
+  int cbits = 13;
+  while (cbits < n && ((1ull << (n - cbits)) > (uint64_t)std::max(1, s->sm_count) * 64)) ++cbits;
+  if (cbits > n) cbits = n;
+  const uint64_t nblocks = 1ull << (n - cbits);
+  const size_t bytes = (nblocks * (n + 1) + (n + 1)) * sizeof(double);
+  int rc = ensure_scratch(s, bytes);
+  if (rc) return rc;
+  double* partial = (double*)s->d_scratch;
+  double* col = partial + nblocks * (n + 1);
+  if (is_c64(s))
+    k_marginals_partial<float><<<(unsigned)nblocks, QSV_THREADS, 0, s->stream>>>((const float2*)s->d_amp, n, cbits, partial);
+  else
+    k_marginals_partial<double><<<(unsigned)nblocks, QSV_THREADS, 0, s->stream>>>((const double2*)s->d_amp, n, cbits, partial);
+  rc = check_launch(s, "marginals_partial");
+  if (rc) return rc;
+  const unsigned fblocks = (unsigned)(((n + 1) * 32 + QSV_THREADS - 1) / QSV_THREADS);
+  k_columns_finish<<<fblocks, QSV_THREADS, 0, s->stream>>>(partial, nblocks, n + 1, col);
+  rc = check_launch(s, "marginals_finish");
+  if (rc) return rc;
+  double hostcol[QSV_MAXN + 1];
+  QSV_CUDA(s, cudaMemcpyAsync(hostcol, col, (n + 1) * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  QSV_CUDA(s, cudaStreamSynchronize(s->stream));
+  // Column p holds the mass with state bit p set; qubit q sits at bit n-1-q.
+  for (int q = 0; q < n; ++q) out[q] = hostcol[n - 1 - q];
+  if (norm2) *norm2 = hostcol[n];
+  return QSV_OK;
+}
+
+int qsv_collapse(qsv_state* s, int m, const int* qubits, uint64_t value, double scale) {
+  QSV_CHECK_HANDLE(s);
+  if (m < 0 || m > s->n) return set_error(s, QSV_ERR_INVALID, "bad measured count %d", m);
+  if (m < 64 && value >= (1ull << m)) return set_error(s, QSV_ERR_INVALID, "outcome %llu out of range", (unsigned long long)value);
+  int pos[QSV_MAXQ];
+  uint64_t seen = 0;
+  int rc = to_positions(s, m, qubits, pos, &seen);
+  if (rc) return rc;
+  uint64_t pattern = 0;
+  for (int j = 0; j < m; ++j)
+    if ((value >> j) & 1ull) pattern |= 1ull << pos[j];
+  const uint64_t total = 1ull << s->n;
+  const unsigned grid = grid_for(s, total);
+  if (is_c64(s))
+    k_collapse<float><<<grid, QSV_THREADS, 0, s->stream>>>((float2*)s->d_amp, total, seen, pattern, scale);
+  else
+    k_collapse<double><<<grid, QSV_THREADS, 0, s->stream>>>((double2*)s->d_amp, total, seen, pattern, scale);
+  return check_launch(s, "collapse");
+}
+
+int qsv_reduce(qsv_state* s, int m, const int* qubits, uint64_t value, double scale) {
+  QSV_CHECK_HANDLE(s);
+  if (m < 1 || m >= s->n) return set_error(s, QSV_ERR_INVALID, "reduce needs 1 <= m < n (m=%d)", m);
+  if (value >= (1ull << m)) return set_error(s, QSV_ERR_INVALID, "outcome out of range");
+  ReduceArgs a;
+  uint64_t seen = 0;
+  int pos[QSV_MAXQ];
+  int rc = to_positions(s, m, qubits, pos, &seen);
+  if (rc) return rc;
+  a.pattern = 0;
+  for (int j = 0; j < m; ++j) {
+    if ((value >> j) & 1ull) a.pattern |= 1ull << pos[j];
+    a.pos[j] = pos[j];
+  }
+  std::sort(a.pos, a.pos + m);
+  a.npos = m;
+  a.scale = scale;
+  a.total_out = 1ull << (s->n - m);
+  void* dst = nullptr;
+  if (cudaMalloc(&dst, a.total_out * s->amp_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(s, QSV_ERR_OOM, "reduce: allocation failed");
+  }
+  const unsigned grid = grid_for(s, a.total_out);
+  if (is_c64(s))
+    k_reduce<float><<<grid, QSV_THREADS, 0, s->stream>>>((const float2*)s->d_amp, (float2*)dst, a);
+  else
+    k_reduce<double><<<grid, QSV_THREADS, 0, s->stream>>>((const double2*)s->d_amp, (double2*)dst, a);
+  rc = check_launch(s, "reduce");
+  if (rc) {
+    cudaFree(dst);
+    return rc;
+  }
+  QSV_CUDA(s, cudaStreamSynchronize(s->stream));
+  cudaFree(s->d_amp);
+  s->d_amp = dst;
+  s->n -= m;
+  return QSV_OK;
+}
+
+int qsv_func_apply(qsv_state* s, int n1, const int* reg1, int n2, const int* reg2, const int64_t* table) {
+  QSV_CHECK_HANDLE(s);
+  if (n1 < 1 || n2 < 1 || n1 + n2 > s->n || n1 > 30 || !table)
+    return set_error(s, QSV_ERR_INVALID, "bad register sizes %d, %d", n1, n2);
+  FuncArgs a;
+  uint64_t seen = 0;
+  int rc = to_positions(s, n1, reg1, a.p1, &seen);
+  if (!rc) rc = to_positions(s, n2, reg2, a.p2, &seen);
+  if (rc) return rc;
+  a.n1 = n1;
+  a.n2 = n2;
+  a.total = 1ull << s->n;
+  const size_t tbytes = (size_t(1) << n1) * sizeof(int64_t);
+  rc = ensure_scratch(s, tbytes);
+  if (rc) return rc;
+  QSV_CUDA(s, cudaMemcpyAsync(s->d_scratch, table, tbytes, cudaMemcpyHostToDevice, s->stream));
+  void* dst = nullptr;
+  if (cudaMalloc(&dst, a.total * s->amp_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(s, QSV_ERR_OOM, "func_apply: allocation failed");
+  }
+  const unsigned grid = grid_for(s, a.total);
+  if (is_c64(s))
+    k_func<float><<<grid, QSV_THREADS, 0, s->stream>>>((const float2*)s->d_amp, (float2*)dst,
+                                                       (const long long*)s->d_scratch, a);
+  else
+    k_func<double><<<grid, QSV_THREADS, 0, s->stream>>>((const double2*)s->d_amp, (double2*)dst,
+                                                        (const long long*)s->d_scratch, a);
+  rc = check_launch(s, "func_apply");
+  if (rc) {
+    cudaFree(dst);
+    return rc;
+  }
+  QSV_CUDA(s, cudaStreamSynchronize(s->stream));
+  cudaFree(s->d_amp);
+  s->d_amp = dst;
+  return QSV_OK;
+}
+
+int qsv_inner_product(qsv_state* a, qsv_state* b, double* re, double* im) {
+  QSV_CHECK_HANDLE(a);
+  QSV_CHECK_HANDLE(b);
+  if (!re || !im) return set_error(a, QSV_ERR_INVALID, "null output");
+  if (a->n != b->n) return set_error(a, QSV_ERR_INVALID, "states of %d and %d qubits", a->n, b->n);
+  QSV_CUDA(a, cudaStreamSynchronize(b->stream));
+  const uint64_t total = 1ull << a->n;
+  const unsigned grid = grid_for(a, total, QSV_THREADS, 8);
+  int rc = ensure_scratch(a, (size_t)grid * 2 * sizeof(double) + 2 * sizeof(double));
+  if (rc) return rc;
+  double* partial = (double*)a->d_scratch;
+  double* col = partial + 2 * (size_t)grid;
+  const bool a64 = is_c64(a), b64 = is_c64(b);
+  if (a64 && b64)
+    k_inner_partial<float, float><<<grid, QSV_THREADS, 0, a->stream>>>((const float2*)a->d_amp, (const float2*)b->d_amp, total, partial);
+  else if (a64)
+    k_inner_partial<float, double><<<grid, QSV_THREADS, 0, a->stream>>>((const float2*)a->d_amp, (const double2*)b->d_amp, total, partial);
+  else if (b64)
+    k_inner_partial<double, float><<<grid, QSV_THREADS, 0, a->stream>>>((const double2*)a->d_amp, (const float2*)b->d_amp, total, partial);
+  else
+    k_inner_partial<double, double><<<grid, QSV_THREADS, 0, a->stream>>>((const double2*)a->d_amp, (const double2*)b->d_amp, total, partial);
+  rc = check_launch(a, "inner_partial");
+  if (rc) return rc;
+  k_columns_finish<<<1, 64, 0, a->stream>>>(partial, grid, 2, col);
+  rc = check_launch(a, "inner_finish");
+  if (rc) return rc;
+  double h[2];
+  QSV_CUDA(a, cudaMemcpyAsync(h, col, sizeof(h), cudaMemcpyDeviceToHost, a->stream));
+  QSV_CUDA(a, cudaStreamSynchronize(a->stream));
+  *re = h[0];
+  *im = h[1];
+  return QSV_OK;
+}
+
+}  // extern "C"

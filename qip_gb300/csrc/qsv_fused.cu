@@ -1,0 +1,600 @@
+// Fused dense blocks on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// A fused block is a 2^k x 2^k complex matrix U (4 <= k <= 6) on k target qubits, the
+// product of a run of gates that only touch those qubits.  It is applied to every one
+// of the 2^(n-k) amplitude groups of a complex64 state in one HBM pass.
+//
+// GEMM shape.  A CTA tile holds 128 groups ("batch" b, the 7 lowest non-target bits)
+// x 2^k target combinations.  Writing v_b in R^(2^(k+1)) as [Re; Im], the block is the
+// real matrix W = [[Ur, -Ui], [Ui, Ur]] (KD x KD, KD = 2^(k+1)) and the tile update is
+//     D[b][n] = sum_kk A[b][kk] * W[n][kk]      (M = 128, N = K = KD)
+// with A the tile (row b = v_b).  D row b then holds [Re w_b; Im w_b] in one TMEM
+// lane, so each epilogue thread writes whole output amplitudes and a warp writes 32
+// consecutive groups: coalesced stores without a shuffle.
+//
+// Precision.  Operands are split into bf16 pairs x = hi + lo (hi = bf16(x),
+// lo = bf16(x - hi)) and D accumulates hi*hi + hi*lo + lo*hi in FP32 (three
+// tcgen05.mma kind::f16 passes), about 2^-16 relative error per pass.
+//
+// Shared-memory operands use the canonical K-major layout without swizzle: core
+// matrices of 8 rows x 16 bytes; the leading byte offset (LBO) steps along K between
+// core matrices and the stride byte offset (SBO = 128 B) steps between 8-row groups.
+// A row r, element kk lives at (kk/8)*(rows*16) + r*16 + (kk%8)*2.
+//
+// Every wait is bounded: a stuck mbarrier sets the handle's status word and the kernel
+// still frees its tensor memory before returning.
+
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "qsv_internal.cuh"
+
+using namespace qsv;
+
+namespace {
+
+constexpr int FB_M = 128;         // groups per tile (MMA M)
+constexpr int FB_THREADS = 256;   // 8 warps
+constexpr int FB_BATCH_BITS = 7;  // log2(FB_M)
+constexpr unsigned long long FB_WAIT_NS = 2000000000ull;  // 2 s per wait
+
+template <int KQ>
+struct FB {
+  static constexpr int T = 1 << KQ;            // target combinations
+  static constexpr int KD = 2 * T;             // GEMM K = N
+  static constexpr int A_BYTES = FB_M * KD * 2;  // one bf16 copy of the tile
+  static constexpr int W_BYTES = KD * KD * 2;    // one bf16 copy of W
+  static constexpr int A_LBO = FB_M * 16;        // K-step between core matrices of A
+  static constexpr int W_LBO = KD * 16;
+  static constexpr int ITEMS = (FB_M * (T / 8)) / FB_THREADS;  // (b, 8 targets) per thread
+  static constexpr int TMEM_COLS = KD < 32 ? 32 : KD;
+  static constexpr int COLS_PER_WARP = T / 2;  // output targets handled per warp
+  // Tables and barrier after the operands, then one W-sized pad: an operand read
+  // with the LBO/SBO roles exchanged would still stay inside this CTA's allocation.
+  static constexpr int SMEM = 2 * A_BYTES + 2 * W_BYTES + FB_M * 8 + T * 8 + 64 + W_BYTES;
+};
+
+struct BlockArgs {
+  uint64_t ntiles;
+  int k;
+  int tpos[8];         // target bit positions, targets[0] first (MSB of the matrix index)
+  int tsorted[8];      // ascending
+  const uint4* wimg;   // hi image then lo image (2 * W_BYTES bytes)
+  int* flag;           // status word
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint64_t make_smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo & 0x3FFFFu) >> 4) << 16;
+  d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
+  return d;                // base offset 0, no swizzle
+}
+
+// kind::f16 instruction descriptor: BF16 x BF16 -> F32, both operands K-major.
+__host__ __device__ constexpr uint32_t make_idesc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Returns false if the phase did not complete within FB_WAIT_NS.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  const uint64_t t0 = globaltimer();
+  while (!mbar_try_wait(bar, parity)) {
+    if (globaltimer() - t0 > FB_WAIT_NS) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+template <int NREG>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, float* v);
+
+template <>
+__device__ __forceinline__ void tmem_ld<8>(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <>
+__device__ __forceinline__ void tmem_ld<16>(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <>
+__device__ __forceinline__ void tmem_ld<32>(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+
+// Splits 8 floats into bf16 hi/lo halves, packed 8 per uint4.
+__device__ __forceinline__ void split8(const float* x, uint4& hi, uint4& lo) {
+  float h[8], l[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const float hv = __bfloat162float(__float2bfloat16_rn(x[i]));
+    h[i] = hv;
+    l[i] = x[i] - hv;
+  }
+  hi = make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
+  lo = make_uint4(pack_bf16(l[0], l[1]), pack_bf16(l[2], l[3]), pack_bf16(l[4], l[5]), pack_bf16(l[6], l[7]));
+}
+
+template <int KQ>
+__global__ void __launch_bounds__(FB_THREADS, 1)
+    k_block_tc(float2* __restrict__ psi, const __grid_constant__ BlockArgs a) {
+  using P = FB<KQ>;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sA_hi = smem;
+  uint8_t* sA_lo = smem + P::A_BYTES;
+  uint8_t* sW_hi = smem + 2 * P::A_BYTES;
+  uint8_t* sW_lo = sW_hi + P::W_BYTES;
+  uint64_t* boff = reinterpret_cast<uint64_t*>(sW_lo + P::W_BYTES);
+  uint64_t* toff = boff + FB_M;
+  uint64_t* mbar = toff + P::T;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  const int lane = tid & 31;
+
+  // W image (hi then lo) into shared memory.
+  {
+    const uint4* src = a.wimg;
+    uint4* dst = reinterpret_cast<uint4*>(sW_hi);
+    constexpr int NV = (2 * P::W_BYTES) / 16;
+    for (int i = tid; i < NV; i += FB_THREADS) dst[i] = src[i];
+  }
+  // Offset tables.
+  for (int b = tid; b < FB_M; b += FB_THREADS) boff[b] = qsv_insert_zeros((uint64_t)b, a.tsorted, KQ);
+  for (int t = tid; t < P::T; t += FB_THREADS) {
+    uint64_t off = 0;
+#pragma unroll
+    for (int j = 0; j < KQ; ++j)
+      if ((t >> (KQ - 1 - j)) & 1) off |= 1ull << a.tpos[j];
+    toff[t] = off;
+  }
+  if (tid == 0) {
+    mbar_init(smem_u32(mbar), 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"((uint32_t)P::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t bar = smem_u32(mbar);
+  constexpr uint32_t idesc = make_idesc(FB_M, P::KD);
+  uint32_t phase = 0;
+
+  // Per-thread items: item = it*FB_THREADS + tid -> b = item % 128, tg = item / 128.
+  float2 buf[P::ITEMS][8];
+  auto load_tile = [&](uint64_t tile) {
+    const uint64_t base = qsv_insert_zeros(tile << FB_BATCH_BITS, a.tsorted, KQ);
+#pragma unroll
+    for (int it = 0; it < P::ITEMS; ++it) {
+      const int item = it * FB_THREADS + tid;
+      const int b = item & (FB_M - 1);
+      const int tg = item >> FB_BATCH_BITS;
+      const uint64_t rb = base + boff[b];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) buf[it][j] = __ldcs(&psi[rb + toff[tg * 8 + j]]);
+    }
+  };
+
+  uint64_t tile = blockIdx.x;
+  if (tile < a.ntiles) load_tile(tile);
+  for (; tile < a.ntiles; tile += gridDim.x) {
+    const uint64_t base = qsv_insert_zeros(tile << FB_BATCH_BITS, a.tsorted, KQ);
+    // Split into bf16 hi/lo and write the A operand (K-major, no swizzle).
+#pragma unroll
+    for (int it = 0; it < P::ITEMS; ++it) {
+      const int item = it * FB_THREADS + tid;
+      const int b = item & (FB_M - 1);
+      const int tg = item >> FB_BATCH_BITS;
+      float re[8], im[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        re[j] = buf[it][j].x;
+        im[j] = buf[it][j].y;
+      }
+      uint4 rh, rl, ih, il;
+      split8(re, rh, rl);
+      split8(im, ih, il);
+      const int off_re = tg * P::A_LBO + b * 16;
+      const int off_im = (P::T / 8 + tg) * P::A_LBO + b * 16;
+      *reinterpret_cast<uint4*>(sA_hi + off_re) = rh;
+      *reinterpret_cast<uint4*>(sA_lo + off_re) = rl;
+      *reinterpret_cast<uint4*>(sA_hi + off_im) = ih;
+      *reinterpret_cast<uint4*>(sA_lo + off_im) = il;
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {
+      const uint32_t a_hi = smem_u32(sA_hi), a_lo = smem_u32(sA_lo);
+      const uint32_t w_hi = smem_u32(sW_hi), w_lo = smem_u32(sW_lo);
+      constexpr int KSTEPS = P::KD / 16;
+#pragma unroll
+      for (int s = 0; s < KSTEPS; ++s)
+        tc_mma(tmem, make_smem_desc(a_hi + s * 2 * P::A_LBO, P::A_LBO, 128),
+               make_smem_desc(w_hi + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, s > 0 ? 1u : 0u);
+#pragma unroll
+      for (int s = 0; s < KSTEPS; ++s)
+        tc_mma(tmem, make_smem_desc(a_hi + s * 2 * P::A_LBO, P::A_LBO, 128),
+               make_smem_desc(w_lo + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, 1u);
+#pragma unroll
+      for (int s = 0; s < KSTEPS; ++s)
+        tc_mma(tmem, make_smem_desc(a_lo + s * 2 * P::A_LBO, P::A_LBO, 128),
+               make_smem_desc(w_hi + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, 1u);
+      tc_commit(bar);
+    }
+    // Prefetch the next tile while the tensor cores work.
+    const uint64_t next = tile + gridDim.x;
+    if (next < a.ntiles) load_tile(next);
+    if (!mbar_wait_bounded(bar, phase)) atomicExch(abort_flag, 1);
+    phase ^= 1u;
+    tc_fence_after();
+    __syncthreads();
+    if (*abort_flag) break;
+    // Epilogue: warp w reads TMEM lanes 32*(w%4).. (rows b) and output targets
+    // [h*T/2, (h+1)*T/2) with h = w/4.
+    {
+      const int q = warp & 3;
+      const int h = warp >> 2;
+      const int b = q * 32 + lane;
+      const uint64_t rb = base + boff[b];
+      const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
+      constexpr int CH = P::COLS_PER_WARP < 32 ? P::COLS_PER_WARP : 32;
+#pragma unroll
+      for (int c0 = 0; c0 < P::COLS_PER_WARP; c0 += CH) {
+        float re[CH], im[CH];
+        const int t0 = h * P::COLS_PER_WARP + c0;
+        tmem_ld<CH>(lane_addr + (uint32_t)t0, re);
+        tmem_ld<CH>(lane_addr + (uint32_t)(P::T + t0), im);
+        tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < CH; ++j) __stcs(&psi[rb + toff[t0 + j]], make_float2(re[j], im[j]));
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+  }
+  if (*abort_flag) {
+    // Give the tensor cores a last bounded chance to finish before freeing TMEM.
+    mbar_wait_bounded(bar, phase);
+    if (tid == 0) atomicExch(a.flag, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)P::TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// ---- host: W images ---------------------------------------------------------------------
+uint16_t f32_to_bf16_rn(float f) {
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return (uint16_t)((u >> 16) | ((u & 0xffffu) ? 0x40u : 0u));
+  const uint32_t rounding = 0x7fffu + ((u >> 16) & 1u);
+  return (uint16_t)((u + rounding) >> 16);
+}
+float bf16_to_f32(uint16_t h) {
+  const uint32_t u = (uint32_t)h << 16;
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+}
+
+size_t image_bytes(int k) {
+  const size_t kd = size_t(2) << k;
+  return 2 * kd * kd * 2;  // hi + lo
+}
+
+// Builds the hi/lo bf16 images of W = [[Ur, -Ui], [Ui, Ur]] in the K-major canonical
+// layout: element (row nn, col kk) at (kk/8)*(KD*16) + nn*16 + (kk%8)*2.
+void build_image(int k, const double* U, uint8_t* out) {
+  const int T = 1 << k, KD = 2 * T;
+  uint16_t* hi = reinterpret_cast<uint16_t*>(out);
+  uint16_t* lo = reinterpret_cast<uint16_t*>(out + (size_t)KD * KD * 2);
+  for (int nn = 0; nn < KD; ++nn) {
+    const int tp = nn % T;
+    const bool out_im = nn >= T;
+    for (int kk = 0; kk < KD; ++kk) {
+      const int t = kk % T;
+      const bool in_im = kk >= T;
+      const double ur = U[2 * ((size_t)tp * T + t)], ui = U[2 * ((size_t)tp * T + t) + 1];
+      double w;
+      if (!out_im)
+        w = in_im ? -ui : ur;
+      else
+        w = in_im ? ur : ui;
+      const float wf = (float)w;
+      const uint16_t h = f32_to_bf16_rn(wf);
+      const uint16_t l = f32_to_bf16_rn((float)(w - (double)bf16_to_f32(h)));
+      const size_t e = ((size_t)(kk / 8) * (KD * 16) + (size_t)nn * 16 + (size_t)(kk % 8) * 2) / 2;
+      hi[e] = h;
+      lo[e] = l;
+    }
+  }
+}
+
+template <int KQ>
+int launch_block(qsv_state* s, const BlockArgs& a) {
+  using P = FB<KQ>;
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_block_tc<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM);
+    if (e != cudaSuccess) return set_error(s, QSV_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(e));
+    configured = true;
+  }
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_block_tc<KQ>, FB_THREADS, P::SMEM);
+  if (per_sm < 1) per_sm = 1;
+  // Bound co-resident CTAs so their TMEM allocations always fit (512 columns per SM).
+  per_sm = std::min(per_sm, 512 / P::TMEM_COLS);
+  uint64_t grid = (uint64_t)std::max(1, s->sm_count) * per_sm;
+  if (grid > a.ntiles) grid = a.ntiles;
+  k_block_tc<KQ><<<(unsigned)grid, FB_THREADS, P::SMEM, s->stream>>>((float2*)s->d_amp, a);
+  return check_launch(s, "block_tc");
+}
+
+}  // namespace
+
+struct qsv_plan {
+  int nblocks = 0;
+  void* d_images = nullptr;
+  std::vector<BlockArgs> args;
+  int n = 0;
+};
+
+namespace {
+int launch_args(qsv_state* s, const BlockArgs& a) {
+  switch (a.k) {
+    case 4: return launch_block<4>(s, a);
+    case 5: return launch_block<5>(s, a);
+    default: return launch_block<6>(s, a);
+  }
+}
+
+// Validates a block list and fills per-block launch arguments and image offsets.
+int prepare_blocks(qsv_state* s, int nblocks, const int* ks, const int* targets_flat,
+                   std::vector<BlockArgs>& args, std::vector<size_t>& img_off,
+                   std::vector<size_t>& mat_offs, size_t& total) {
+  total = 0;
+  size_t mat_off = 0;
+  int tofs = 0;
+  args.assign((size_t)nblocks, BlockArgs{});
+  img_off.assign((size_t)nblocks, 0);
+  mat_offs.assign((size_t)nblocks, 0);
+  for (int i = 0; i < nblocks; ++i) {
+    const int k = ks[i];
+    if (k < 4 || k > 6) return set_error(s, QSV_ERR_INVALID, "block %d: k=%d outside [4, 6]", i, k);
+    if (s->n - k < FB_BATCH_BITS)
+      return set_error(s, QSV_ERR_UNSUPPORTED, "block %d: n=%d too small for a %d-qubit tensor-core block", i,
+                       s->n, k);
+    BlockArgs& a = args[(size_t)i];
+    uint64_t seen = 0;
+    int rc = to_positions(s, k, targets_flat + tofs, a.tpos, &seen);
+    if (rc) return rc;
+    a.k = k;
+    for (int j = 0; j < k; ++j) a.tsorted[j] = a.tpos[j];
+    std::sort(a.tsorted, a.tsorted + k);
+    a.ntiles = 1ull << (s->n - k - FB_BATCH_BITS);
+    a.flag = s->d_flag;
+    img_off[(size_t)i] = total;
+    mat_offs[(size_t)i] = mat_off;
+    total += image_bytes(k);
+    mat_off += (size_t)2 << (2 * k);
+    tofs += k;
+  }
+  return QSV_OK;
+}
+}  // namespace
+
+extern "C" int qsv_plan_create(qsv_state* s, int nblocks, const int* ks, const int* targets_flat,
+                               const double* mats_c128, qsv_plan** out) {
+  QSV_CHECK_HANDLE(s);
+  if (!out) return set_error(s, QSV_ERR_INVALID, "null plan output");
+  *out = nullptr;
+  if (s->dtype != QSV_C64) return set_error(s, QSV_ERR_UNSUPPORTED, "fused blocks need a complex64 state");
+  if (nblocks < 1 || !ks || !targets_flat || !mats_c128) return set_error(s, QSV_ERR_INVALID, "bad block list");
+  auto* p = new (std::nothrow) qsv_plan();
+  if (!p) return set_error(s, QSV_ERR_OOM, "host allocation failed");
+  std::vector<size_t> img_off, mat_offs;
+  size_t total = 0;
+  int rc = prepare_blocks(s, nblocks, ks, targets_flat, p->args, img_off, mat_offs, total);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  std::vector<uint8_t> host(total);
+  for (int i = 0; i < nblocks; ++i)
+    build_image(ks[i], mats_c128 + mat_offs[(size_t)i], host.data() + img_off[(size_t)i]);
+  if (cudaMalloc(&p->d_images, total) != cudaSuccess) {
+    cudaGetLastError();
+    delete p;
+    return set_error(s, QSV_ERR_OOM, "plan image allocation failed");
+  }
+  cudaError_t e = cudaMemcpy(p->d_images, host.data(), total, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(p->d_images);
+    delete p;
+    return set_error(s, QSV_ERR_CUDA, "plan upload: %s", cudaGetErrorString(e));
+  }
+  for (int i = 0; i < nblocks; ++i)
+    p->args[(size_t)i].wimg = reinterpret_cast<const uint4*>((const uint8_t*)p->d_images + img_off[(size_t)i]);
+  p->nblocks = nblocks;
+  p->n = s->n;
+  *out = p;
+  return QSV_OK;
+}
+
+extern "C" int qsv_plan_launch(qsv_state* s, const qsv_plan* p, int first, int count) {
+  QSV_CHECK_HANDLE(s);
+  if (!p || first < 0 || count < 0 || first + count > p->nblocks)
+    return set_error(s, QSV_ERR_INVALID, "bad plan range");
+  if (p->n != s->n) return set_error(s, QSV_ERR_INVALID, "plan built for n=%d, state has n=%d", p->n, s->n);
+  for (int i = first; i < first + count; ++i) {
+    BlockArgs a = p->args[(size_t)i];
+    a.flag = s->d_flag;
+    int rc = launch_args(s, a);
+    if (rc) return rc;
+  }
+  return QSV_OK;
+}
+
+extern "C" int qsv_plan_destroy(qsv_plan* p) {
+  if (!p) return QSV_OK;
+  if (p->d_images) cudaFree(p->d_images);
+  delete p;
+  return QSV_OK;
+}
+
+extern "C" int qsv_apply_blocks(qsv_state* s, int nblocks, const int* ks, const int* targets_flat,
+                                const double* mats_c128) {
+  QSV_CHECK_HANDLE(s);
+  if (s->dtype != QSV_C64) return set_error(s, QSV_ERR_UNSUPPORTED, "fused blocks need a complex64 state");
+  if (nblocks < 0 || (nblocks > 0 && (!ks || !targets_flat || !mats_c128)))
+    return set_error(s, QSV_ERR_INVALID, "bad block list");
+  if (nblocks == 0) return QSV_OK;
+  std::vector<BlockArgs> args;
+  std::vector<size_t> img_off, mat_offs;
+  size_t total = 0;
+  int rc = prepare_blocks(s, nblocks, ks, targets_flat, args, img_off, mat_offs, total);
+  if (rc) return rc;
+  // Pinned host staging: wait until the previous upload from it has completed.
+  if (s->images_in_flight) {
+    QSV_CUDA(s, cudaEventSynchronize(s->images_done));
+    s->images_in_flight = false;
+  }
+  if (s->h_images_bytes < total) {
+    if (s->h_images) cudaFreeHost(s->h_images);
+    s->h_images = nullptr;
+    s->h_images_bytes = 0;
+    const size_t want = std::max(total, size_t(1) << 20);
+    if (cudaMallocHost(&s->h_images, want) != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(s, QSV_ERR_OOM, "pinned staging allocation failed");
+    }
+    s->h_images_bytes = want;
+  }
+  if (s->d_images_bytes < total) {
+    QSV_CUDA(s, cudaStreamSynchronize(s->stream));  // old images may still be in use
+    if (s->d_images) cudaFree(s->d_images);
+    s->d_images = nullptr;
+    s->d_images_bytes = 0;
+    const size_t want = std::max(total, size_t(1) << 20);
+    if (cudaMalloc(&s->d_images, want) != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(s, QSV_ERR_OOM, "device image allocation failed");
+    }
+    s->d_images_bytes = want;
+  }
+  if (!s->images_done) QSV_CUDA(s, cudaEventCreateWithFlags(&s->images_done, cudaEventDisableTiming));
+  for (int i = 0; i < nblocks; ++i)
+    build_image(ks[i], mats_c128 + mat_offs[(size_t)i], (uint8_t*)s->h_images + img_off[(size_t)i]);
+  QSV_CUDA(s, cudaMemcpyAsync(s->d_images, s->h_images, total, cudaMemcpyHostToDevice, s->stream));
+  QSV_CUDA(s, cudaEventRecord(s->images_done, s->stream));
+  s->images_in_flight = true;
+  for (int i = 0; i < nblocks; ++i) {
+    BlockArgs& a = args[(size_t)i];
+    a.wimg = reinterpret_cast<const uint4*>((const uint8_t*)s->d_images + img_off[(size_t)i]);
+    rc = launch_args(s, a);
+    if (rc) return rc;
+  }
+  return QSV_OK;
+}

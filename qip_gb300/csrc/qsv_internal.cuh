@@ -1,0 +1,116 @@
+// Internal declarations shared by the translation units of libqsv.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+
+#include "../../include/qsv.h"
+
+// Largest number of qubit positions a single call may name (targets + controls).
+constexpr int QSV_MAXQ = 40;
+// Largest register width of a state handle (2^34 complex64 = 128 GiB).
+constexpr int QSV_MAXN = 34;
+constexpr int QSV_THREADS = 256;
+
+struct qsv_state {
+  int n = 0;
+  int dtype = QSV_C64;
+  int device = 0;
+  int sm_count = 0;
+  size_t amp_bytes = 8;
+  void* d_amp = nullptr;
+  cudaStream_t stream = nullptr;      // stream every call is ordered on
+  cudaStream_t own_stream = nullptr;  // created by qsv_create
+  // Growable device scratch (reductions, feeds, tables).
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  // Device status word written by kernels with bounded waits.
+  int* d_flag = nullptr;
+  // Fused-block matrix images: pinned host staging + device copy.
+  void* h_images = nullptr;
+  size_t h_images_bytes = 0;
+  void* d_images = nullptr;
+  size_t d_images_bytes = 0;
+  cudaEvent_t images_done = nullptr;
+  bool images_in_flight = false;
+  // Pinned staging for host <-> device range copies.
+  void* h_stage = nullptr;
+  size_t h_stage_bytes = 0;
+  char err[512] = {0};
+};
+
+namespace qsv {
+
+extern std::atomic<unsigned long long> g_launches;
+inline void count_launch(unsigned long long k = 1) {
+  g_launches.fetch_add(k, std::memory_order_relaxed);
+}
+
+int set_error(qsv_state* s, int code, const char* fmt, ...);
+int ensure_scratch(qsv_state* s, size_t bytes);
+int check_launch(qsv_state* s, const char* what);
+unsigned grid_for(const qsv_state* s, uint64_t work, unsigned per_block = QSV_THREADS,
+                  unsigned waves = 16);
+
+// Validates qubit indices (range, duplicates) and converts them to bit positions.
+int to_positions(qsv_state* s, int count, const int* qubits, int* pos_out,
+                 uint64_t* seen_mask);
+
+template <typename R> struct C2T;
+template <> struct C2T<float> { using type = float2; };
+template <> struct C2T<double> { using type = double2; };
+
+}  // namespace qsv
+
+#define QSV_CUDA(s, call)                                                          \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return qsv::set_error((s), QSV_ERR_CUDA, "%s: %s", #call,                    \
+                            cudaGetErrorString(e_));                               \
+  } while (0)
+
+#define QSV_CHECK_HANDLE(s)                                                        \
+  do {                                                                             \
+    if ((s) == nullptr || (s)->d_amp == nullptr) return QSV_ERR_INVALID;           \
+  } while (0)
+
+// ---- device helpers --------------------------------------------------------------
+
+// Spreads the bits of g over the positions that are NOT in pos[0..npos) (sorted
+// ascending): the inverse of removing those bit positions.
+__device__ __forceinline__ uint64_t qsv_insert_zeros(uint64_t g, const int* pos, int npos) {
+  for (int i = 0; i < npos; ++i) {
+    const int p = pos[i];
+    const uint64_t low = g & ((1ull << p) - 1ull);
+    g = ((g >> p) << (p + 1)) | low;
+  }
+  return g;
+}
+
+__device__ __forceinline__ float2 qsv_cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 qsv_cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+// acc + a*b
+__device__ __forceinline__ float2 qsv_cfma(float2 a, float2 b, float2 acc) {
+  acc.x = fmaf(a.x, b.x, acc.x);
+  acc.x = fmaf(-a.y, b.y, acc.x);
+  acc.y = fmaf(a.x, b.y, acc.y);
+  acc.y = fmaf(a.y, b.x, acc.y);
+  return acc;
+}
+__device__ __forceinline__ double2 qsv_cfma(double2 a, double2 b, double2 acc) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+  return acc;
+}

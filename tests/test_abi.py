@@ -1,0 +1,46 @@
+"""The C ABI library loads without a GPU and exports every symbol include/*.h declares,
+and the Python binding covers the same set."""
+import ctypes
+import glob
+import os
+import re
+
+from conftest import ROOT
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(qsv_\w+)\s*\(", text):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    from qip_gb300 import _native, build
+
+    path = build.build()
+    assert os.path.exists(path)
+    lib = ctypes.CDLL(path)
+    syms = declared_symbols()
+    assert len(syms) >= 25
+    missing = [s for s in sorted(syms) if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(_native.SIGNATURES) == syms
+
+
+def test_status_strings_without_a_device():
+    from qip_gb300 import _native
+
+    lib = _native.load()
+    assert lib.qsv_status_string(0) == b"ok"
+    assert lib.qsv_status_string(1) == b"invalid argument"
+    assert lib.qsv_launch_count() >= 0
+
+
+def test_library_is_sm103a_only():
+    from qip_gb300 import build
+
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1,0 +1,168 @@
+"""Host logic on CPU: the graph API mirror, the kron-dictionary decomposition and the
+fusion planner, each checked with the oracle as the state executor.  No GPU."""
+import types
+
+import numpy
+import pytest
+
+import qip_gb300 as api_mod
+import statevector as sv
+from conftest import load_npz
+from make_golden import decode
+from qip_gb300 import circuits, fusion, gates
+from qip_gb300.operators import CMat, SwapMat
+from scenarios import SCENARIOS
+
+
+def api_ns():
+    return types.SimpleNamespace(**{k: getattr(api_mod, k) for k in api_mod.__all__})
+
+
+def run_scenarios(backend_constructor, statetype=numpy.complex128, names=None, atol=1e-12):
+    d, meta = load_npz("scenarios.npz")
+    api = api_ns()
+    checked = 0
+    for name, fn in SCENARIOS.items():
+        if names and name not in names:
+            continue
+        runs = fn(api)
+        assert len(runs) == len(meta[name])
+        for r, (outs, feed, measured) in enumerate(runs):
+            o, classic = api.run(*outs, feed=feed, backend_constructor=backend_constructor, statetype=statetype)
+            numpy.testing.assert_allclose(o, d[f"{name}_{r}_state"], rtol=0, atol=atol, err_msg=f"{name}[{r}]")
+            for j, node in enumerate(measured):
+                kind = meta[name][r]["measured"][j]
+                val = classic[node]
+                if kind == "topk":
+                    numpy.testing.assert_allclose(val[1], d[f"{name}_{r}_m{j}_p"], atol=atol)
+                    refp = d[f"{name}_{r}_m{j}_p"]
+                    refm = d[f"{name}_{r}_m{j}_idx"]
+                    for k in range(len(refm)):
+                        if numpy.sum(numpy.abs(refp - refp[k]) < 1e-12) == 1:
+                            assert int(val[0][k]) == int(refm[k]), f"{name}[{r}] top-k index {k}"
+                else:
+                    numpy.testing.assert_allclose(val, d[f"{name}_{r}_m{j}_p"], atol=atol)
+            checked += 1
+    return checked
+
+
+def test_graph_api_mirror_matches_reference_runs():
+    assert run_scenarios(sv.OracleBackend.make_state) >= 40
+
+
+def test_qft_negate_keyword_is_dropped_like_reference():
+    # QubitOpWrapper forwards only construction-time kwargs, so QFFT's negate=True has
+    # no effect and the circuit is the inverse DFT (matches the reference output).
+    n = 5
+    rng = numpy.random.default_rng(0)
+    x = rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)
+    x /= numpy.linalg.norm(x)
+    q = api_mod.Qubit(n=n)
+    o, _ = api_mod.run(api_mod.QFFT(q), feed={q: x}, backend_constructor=sv.OracleBackend.make_state)
+    numpy.testing.assert_allclose(o, numpy.fft.ifft(x, norm="ortho"), atol=1e-13)
+
+
+def test_no_cloning_and_argument_errors():
+    q = api_mod.Qubit(n=1)
+    api_mod.Qubit(q)
+    with pytest.raises(Exception):
+        api_mod.Qubit(q)
+    with pytest.raises(ValueError):
+        api_mod.Qubit(n=2, default=[1, 0, 0])
+    a, b = api_mod.Qubit(n=1), api_mod.Qubit(n=2)
+    with pytest.raises(Exception):
+        api_mod.SwapOp(a, b)
+    with pytest.raises(ValueError):
+        api_mod.C(api_mod.H)(api_mod.Qubit(n=2), api_mod.Qubit(n=1))
+    with pytest.raises(ValueError):
+        r = api_mod.Qubit(n=1)
+        api_mod.run(api_mod.H(r), strict=True, backend_constructor=sv.OracleBackend.make_state)
+
+
+def test_decompose_equals_reference_semantics():
+    """Every kron dictionary of the golden set: the structured ops, applied one by one,
+    give the reference output."""
+    d, cases = load_npz("kron_cases.npz")
+    for c in cases:
+        mats = decode(c["mats"], d, CMat, SwapMat)
+        ops = gates.decompose(mats)
+        v = d[f"k{c['id']}_in"].astype(complex)
+        for op in ops:
+            order, m = op.matrix()
+            v = sv.apply_on(v, c["n"], order, m)
+        numpy.testing.assert_allclose(v, d[f"k{c['id']}_out"], atol=1e-12, err_msg=str(c))
+
+
+def test_decompose_mixed_dictionaries_against_oracle():
+    # Dictionaries the reference cannot pack (mixed key lengths / kinds) follow the
+    # entry-product semantics of the oracle.
+    rng = numpy.random.default_rng(4)
+    n = 6
+    for _ in range(20):
+        a, b, c, e = (int(x) for x in rng.choice(n, 4, replace=False))
+        u2 = numpy.linalg.qr(rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4)))[0]
+        u1 = numpy.linalg.qr(rng.standard_normal((2, 2)) + 1j * rng.standard_normal((2, 2)))[0]
+        for mats in ({(a, b): u2, (c,): u1}, {(a, b): CMat(u1), (c, e): SwapMat(1)},
+                     {(a, b, c): CMat(CMat(u1)), (e,): u1}, {(a, b): u2, (b, c): u2}):
+            v = rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)
+            want = sv.kronselect_dot(mats, v, n)
+            got = v.copy()
+            for op in gates.decompose(mats):
+                order, m = op.matrix()
+                got = sv.apply_on(got, n, order, m)
+            numpy.testing.assert_allclose(got, want, atol=1e-12)
+
+
+def test_decompose_errors_match_reference():
+    with pytest.raises(Exception, match="Type of indices"):
+        gates.decompose({"a": numpy.eye(2)})
+    with pytest.raises(Exception, match="Shape of square submatrix"):
+        gates.decompose({(0, 1): numpy.eye(2)})
+    with pytest.raises(ValueError, match="Cannot pass matrices"):
+        gates.decompose({(0,): types.SimpleNamespace(shape=(2, 2))})
+
+
+def test_decompose_classifies_structure():
+    h = numpy.array([[1, 1], [1, -1]]) / numpy.sqrt(2)
+    assert gates.decompose({0: h})[0].kind == "dense"
+    assert gates.decompose({0: numpy.diag([1, 1j])})[0].kind == "diag"
+    assert gates.decompose({0: numpy.array([[0, 1], [1, 0]])})[0].kind == "mono"
+    assert gates.decompose({0: numpy.eye(2)}) == []
+    op = gates.decompose({(3, 1, 2): CMat(CMat(numpy.diag([1, -1])))})[0]
+    assert op.kind == "diag" and op.controls == (3, 1) and op.targets == (2,)
+    op = gates.decompose({(0, 1, 2): CMat(SwapMat(1))})[0]
+    assert op.kind == "swap" and op.controls == (0,) and op.targets == (1,) and op.swap_b == (2,)
+
+
+@pytest.mark.parametrize("kmax", [3, 4, 5, 6])
+def test_fusion_plan_preserves_the_circuit(kmax):
+    n = 9
+    gl = circuits.brickwork(n, 6, seed=2) + circuits.grover_gates(n, 1, seed=1)[0]
+    ops = [op for g in gl for op in gates.decompose(g)]
+    steps = fusion.plan(ops, kmax=kmax)
+    v0 = numpy.zeros(2 ** n, dtype=complex)
+    v0[0] = 1
+    want = v0
+    for g in gl:
+        want = sv.kronselect_dot(g, want, n)
+    got = v0
+    nblocks = 0
+    for st in steps:
+        if isinstance(st, fusion.Block):
+            assert len(st.qubits) <= kmax
+            got = sv.apply_on(got, n, st.qubits, st.matrix)
+            nblocks += 1
+        else:
+            order, m = st.matrix()
+            got = sv.apply_on(got, n, order, m)
+    numpy.testing.assert_allclose(got, want, atol=1e-11)
+    assert len(steps) < len(ops)
+    assert sum(st.ngates if isinstance(st, fusion.Block) else 1 for st in steps) == len(ops)
+
+
+def test_fusion_keeps_wide_gates_standalone():
+    n = 12
+    ops = [op for g in circuits.grover_gates(n, 1, seed=5)[0] for op in gates.decompose(g)]
+    steps = fusion.plan(ops, kmax=6)
+    wide = [s for s in steps if not isinstance(s, fusion.Block) and s.width > 6]
+    assert len(wide) == 2  # the two (n-1)-controlled Z gates
