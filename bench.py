@@ -1,0 +1,461 @@
+"""Benchmark: random brickwork circuit, n=28, depth 40 (amp-updates/s).
+
+Our arm (default):
+  value      complex64 state, gates fused into <=6-qubit blocks run on the tensor cores
+             (tcgen05, split-bf16 products, FP32 accumulation); device time per step
+             (state reset to |0...0> + the whole circuit), inputs resident in HBM.
+  plain_fp64 the same circuit on the complex128 per-gate kernels (one launch per gate).
+  infidelity 1 - |<psi_fused|psi_fp64>|^2 computed on the GPU in FP64.
+  e2e        the same metric through the backend plugin with host buffers: build the
+             state, one kronselect_dot per gate with host numpy matrices, get_state()
+             back to host memory; host<->device copies inside the timed region.
+  roofline   the fused block kernel: algorithmic bytes per launch (read + write of the
+             2^n complex64 state) over its mean CUDA-event launch time.
+  cpu_baseline  the reference's own Cython/OpenMP kernel (cdot_loop) on the machine's cores,
+             a bounded sample of the same gate list at the same n.
+--impl reference: the reference CPU kernel alone, same metric/config, one JSON line.
+
+Multi-GPU: every rank runs an independent replica (the state vector is not sharded);
+value = total amp-updates of all ranks / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT, DEPTH_DEFAULT, SEED = 28, 40, 1234
+METRIC = "amp-updates/s (brickwork circuit, fused FP32 tensor-core blocks vs plain FP64 per-gate)"
+THROTTLE_REASONS = {
+    0x1: "gpu_idle", 0x2: "applications_clocks_setting", 0x4: "sw_power_cap", 0x8: "hw_slowdown",
+    0x10: "sync_boost", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown",
+    0x100: "display_clock_setting",
+}
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sms, mx, reasons = [], None, set()
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 3:
+                continue
+            try:
+                sms.append(float(parts[0]))
+                mx = float(parts[1])
+                mask = int(parts[2], 16) if parts[2].startswith("0x") else int(parts[2])
+            except ValueError:
+                continue
+            for bit, name in THROTTLE_REASONS.items():
+                if mask & bit and name != "gpu_idle":
+                    reasons.add(name)
+        if not sms:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sms)}
+
+
+# ---- reference CPU kernel --------------------------------------------------------------------
+
+def load_reference_kernels():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import build_ref
+
+    if not build_ref.available():
+        build_ref.build()
+    if not build_ref.available():
+        return None
+    kronprod, _ = build_ref.load()
+    return kronprod
+
+
+def ref_pack(mats):
+    """Pack a kron dictionary the way the reference's util.kronselect_dot hands it to
+    cdot_loop: an int32 index array and an array of complex128 / CMat / SwapMat."""
+    keys = [k if isinstance(k, tuple) else (k,) for k in mats]
+    vals = [mats[k] for k in mats]
+    cind = numpy.array([numpy.array(k, dtype=numpy.int32) for k in keys])
+    cm = numpy.empty(len(vals), dtype=object)
+    for i, m in enumerate(vals):
+        cm[i] = m.astype(numpy.complex128) if isinstance(m, numpy.ndarray) else m
+    return cind, cm
+
+
+def cpu_reference_sample(n, gates, seconds_cap=30.0):
+    """Time the reference cdot_loop over a bounded prefix-sample of the gate list at full
+    n (state + arena ping-pong as CythonBackend does).  Returns (amp_updates/s, info)."""
+    from qip_gb300 import circuits
+
+    kp = load_reference_kernels()
+    if kp is None:
+        return None, {"kind": "unavailable", "why": "reference kernels not built"}
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    # A representative sample: 3 Haar single-qubit gates and 2 controlled-Z gates.
+    haar = [g for g in gates if len(next(iter(g))) == 1][:3]
+    cz = [g for g in gates if len(next(iter(g))) == 2][:2]
+    sample = haar + cz
+    vec = numpy.zeros(2 ** n, dtype=numpy.complex128)
+    vec[0] = 1.0
+    out = numpy.zeros(2 ** n, dtype=numpy.complex128)
+    packed = [ref_pack(g) for g in sample]
+    done = 0.0
+    t0 = time.perf_counter()
+    used = []
+    for g, (ci, cm) in zip(sample, packed):
+        kp.cdot_loop(ci, cm, vec, n, out)
+        vec, out = out, vec
+        done += circuits.gate_amp_updates([g], n)
+        used.append(g)
+        if time.perf_counter() - t0 > seconds_cap:
+            break
+    dt = time.perf_counter() - t0
+    info = {"kind": "reference", "cores": int(os.environ.get("OMP_NUM_THREADS", cores)),
+            "sample": f"{len(used)} gates of the n={n} brickwork ({sum(len(next(iter(g))) == 1 for g in used)} "
+                      f"Haar 1-qubit, {sum(len(next(iter(g))) == 2 for g in used)} CZ) through the reference "
+                      f"Cython cdot_loop, complex128, {dt:.1f} s"}
+    return done / dt, info
+
+
+# ---- GPU arm -----------------------------------------------------------------------------------
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+
+    if ws > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return ws, rank, local
+
+
+def barrier_max(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def run_ours(args):
+    import torch
+
+    from qip_gb300 import GpuBackend, _native as nat, circuits, fusion, gates as gmod
+
+    ws, rank, local = dist_setup(args)
+    n, depth = args.n, args.depth
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    gl = circuits.brickwork(n, depth, seed=SEED)
+    amp_updates = circuits.gate_amp_updates(gl, n)
+    ops = [op for g in gl for op in gmod.decompose(g)]
+    t_plan0 = time.perf_counter()
+    steps = fusion.plan(ops, kmax=args.kmax)
+    t_plan = time.perf_counter() - t_plan0
+    blocks = [s for s in steps if isinstance(s, fusion.Block) and len(s.qubits) >= 4]
+    lib = nat.load()
+
+    st = GpuBackend.make_state(n, [], [], statetype=numpy.complex64, fusion=True)
+    st.set_stream(stream.cuda_stream)
+    # Device-resident plan: block images uploaded once; a step launches kernels only.
+    ks = nat.int_array([len(b.qubits) for b in blocks])
+    tg = nat.int_array([q for b in blocks for q in b.qubits])
+    mats = numpy.ascontiguousarray(numpy.concatenate([b.matrix.reshape(-1) for b in blocks])).view(numpy.float64)
+    plan = ctypes.c_void_p()
+    nat.check(lib.qsv_plan_create(st.handle, len(blocks), nat.ip(ks), nat.ip(tg), nat.dp(mats), ctypes.byref(plan)),
+              st.handle, "plan_create")
+    block_index = {id(b): i for i, b in enumerate(blocks)}
+    seq = []  # ("block", i) | ("op", GateOp)
+    for s_ in steps:
+        if isinstance(s_, fusion.Block) and id(s_) in block_index:
+            seq.append(("block", block_index[id(s_)]))
+        elif isinstance(s_, fusion.Block):
+            for op in gmod.classify_matrix(s_.qubits, (), s_.matrix):
+                seq.append(("op", op))
+        else:
+            seq.append(("op", s_))
+
+    def reset():
+        nat.check(lib.qsv_set_product_state(st.handle, 0, None, None, None), st.handle, "reset")
+
+    ev_pairs = []
+
+    def fused_step(record):
+        reset()
+        for kind, x in seq:
+            if kind == "block":
+                if record:
+                    a = torch.cuda.Event(enable_timing=True)
+                    b = torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    nat.check(lib.qsv_plan_launch(st.handle, plan, x, 1), st.handle, "plan_launch")
+                    b.record(stream)
+                    ev_pairs.append((a, b))
+                else:
+                    nat.check(lib.qsv_plan_launch(st.handle, plan, x, 1), st.handle, "plan_launch")
+            else:
+                st.apply_op(x)
+
+    for _ in range(args.warmup):
+        fused_step(False)
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches0 = nat.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            fused_step(True)
+        e1.record(stream)
+        e1.synchronize()
+    launches = nat.launch_count() - launches0
+    st.synchronize()
+    t_fused = e0.elapsed_time(e1) * 1e-3 / args.steps
+    t_fused = barrier_max(t_fused, ws)
+    block_ms = [a.elapsed_time(b) for a, b in ev_pairs]
+    mean_block_s = statistics.mean(block_ms) * 1e-3 if block_ms else float("nan")
+    value = ws * amp_updates / t_fused
+
+    parts = set(args.parts.split(","))
+    if "plain" not in parts:
+        lib.qsv_plan_destroy(plan)
+        st.close()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "amp-updates/s", "n_gpus": ws,
+                              "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_fused * 1e3,
+                              "partial": sorted(parts), "mean_block_ms": mean_block_s * 1e3,
+                              "gpu_launches": int(launches)}), flush=True)
+        return
+    # Plain complex128 per-gate path (the FP64 baseline of the metric).
+    ref = GpuBackend.make_state(n, [], [], statetype=numpy.complex128, fusion=False)
+    ref.set_stream(stream.cuda_stream)
+    plain_ops = ops
+
+    def plain_step():
+        nat.check(lib.qsv_set_product_state(ref.handle, 0, None, None, None), ref.handle, "reset")
+        for op in plain_ops:
+            ref.apply_op(op)
+
+    plain_step()
+    torch.cuda.synchronize()
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    psteps = max(1, min(2, args.steps))
+    p0.record(stream)
+    for _ in range(psteps):
+        plain_step()
+    p1.record(stream)
+    p1.synchronize()
+    t_plain = barrier_max(p0.elapsed_time(p1) * 1e-3 / psteps, ws)
+    # Infidelity of the fused FP32 result against the FP64 result.
+    fused_step(False)
+    st.synchronize()
+    re_, im_ = ctypes.c_double(), ctypes.c_double()
+    nat.check(lib.qsv_inner_product(st.handle, ref.handle, ctypes.byref(re_), ctypes.byref(im_)), st.handle, "inner")
+    nrm = numpy.zeros(1)
+    nrm_ref = numpy.zeros(1)
+    nat.check(lib.qsv_norm2(st.handle, nat.dp(nrm)), st.handle)
+    nat.check(lib.qsv_norm2(ref.handle, nat.dp(nrm_ref)), ref.handle)
+    infid = 1.0 - (re_.value ** 2 + im_.value ** 2) / (nrm[0] * nrm_ref[0])
+    ref.close()
+    lib.qsv_plan_destroy(plan)
+    st.close()
+    torch.cuda.synchronize()
+
+    # e2e through the plugin (StateType calls with host buffers).
+    def e2e_step():
+        s2 = GpuBackend.make_state(n, [], [], statetype=numpy.complex64, fusion=True, max_block=args.kmax)
+        for g in gl:
+            s2.kronselect_dot(g)
+        out = s2.get_state()
+        s2.close()
+        return out
+
+    e2e_steps = max(1, min(args.steps, 3))
+    e2e_step()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        host = e2e_step()
+    t_e2e = barrier_max((time.perf_counter() - t0) / e2e_steps, ws)
+    h2d = sum(fusion_image_bytes(len(b.qubits)) for b in blocks) + sum(
+        numpy.asarray(op.mat).nbytes for kind, op in seq if kind == "op" and op.mat is not None)
+    d2h = host.nbytes
+    del host
+
+    peak, peak_src = read_peaks()
+    alg_bytes = 2 * (2 ** n) * 8
+    achieved = alg_bytes / mean_block_s / 1e9
+    result = {
+        "metric": METRIC, "value": value, "unit": "amp-updates/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_fused * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64",
+        "data": "synthetic: seeded Haar-random brickwork, |0...0> input",
+        "config": {"workload": f"brickwork n={n} depth {depth} (Haar 2x2 on every qubit, CZ even/odd pairs, "
+                               f"C(Swap) every 10 layers)", "n": n, "depth": depth, "gates": len(gl),
+                   "amp_updates_per_step": amp_updates, "fusion_kmax": args.kmax,
+                   "fused_blocks": len(blocks), "standalone_ops": sum(1 for k, _ in seq if k == "op"),
+                   "plan_seconds": t_plan, "parallelism": f"replicas x{ws}",
+                   "l2": f"state {2 ** n * 8 / 2 ** 30:.0f} GiB > L2; no flush needed"},
+        "plain_fp64": {"value": ws * amp_updates / t_plain, "ms_per_step": t_plain * 1e3, "steps": psteps,
+                       "launches_per_step": len(ops)},
+        "speedup_fused_vs_plain_fp64": t_plain / t_fused,
+        "infidelity_vs_fp64": infid,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "k_block_tc (fused block, k<=6)",
+                     "per_launch_bytes": alg_bytes, "mean_launch_ms": mean_block_s * 1e3,
+                     "peak_source": f"{peak_src} hbm_gbs"},
+        "e2e": {"value": ws * amp_updates / t_e2e, "unit": "amp-updates/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "seconds_per_step": t_e2e, "steps": e2e_steps},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu and "cpu" in parts:
+        v, info = cpu_reference_sample(n, gl, seconds_cap=args.cpu_seconds)
+        info = dict(info)
+        info["value"] = v
+        info["unit"] = "amp-updates/s"
+        result["cpu_baseline"] = info
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def fusion_image_bytes(k):
+    kd = 2 << k
+    return 2 * kd * kd * 2
+
+
+def run_reference(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from qip_gb300 import circuits
+
+    n, depth = args.n, args.depth
+    gl = circuits.brickwork(n, depth, seed=SEED)
+    kp = load_reference_kernels()
+    if kp is None:
+        print(json.dumps({"impl": "reference", "unavailable": "reference Cython kernels could not be built here"}))
+        return
+    vals = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        v, info = cpu_reference_sample(n, gl, seconds_cap=max(5.0, args.cpu_seconds / 2))
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.mean(vals)
+    amp = circuits.gate_amp_updates(gl, n)
+    info = dict(info)
+    info["value"] = value
+    info["unit"] = "amp-updates/s"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "amp-updates/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": amp / value * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic: seeded Haar-random brickwork, |0...0> input",
+        "config": {"workload": f"brickwork n={n} depth {depth}", "n": n, "depth": depth,
+                   "note": "reference CPU kernel timed on a bounded gate sample per step; ms_per_step "
+                           "extrapolates the full circuit"},
+        "cpu_baseline": info,
+        "e2e": {"value": value, "unit": "amp-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--depth", type=int, default=DEPTH_DEFAULT)
+    ap.add_argument("--kmax", type=int, default=6)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--parts", default="fused,plain,e2e,cpu",
+                    help="comma list of fused,plain,e2e,cpu (profiling runs use fused only)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -328,6 +328,14 @@ __global__ void __launch_bounds__(QSV_THREADS)
 }
 
 // ---- measurement reductions ---------------------------------------------------------------
+// Precision plan.  GB300 has little FP64 throughput, so per-element work stays off the
+// FP64 pipe where the state allows it: for complex64 states each |a|^2 is formed as an
+// exact FP32 pair (products by fma, then TwoSum of the two squares) and accumulated per
+// thread in double-float (Knuth TwoSum, ~48-bit precision at FP32 rate).  complex128
+// states accumulate in FP64.  Thread partials are combined in FP64 through a pairwise
+// tree and block partials with Neumaier compensation, so the result carries FP64-level
+// error whatever the state size.
+
 // Neumaier-compensated FP64 accumulation.
 struct Acc {
   double s = 0.0, c = 0.0;
@@ -340,6 +348,61 @@ struct Acc {
     s = t;
   }
   __device__ __forceinline__ double value() const { return s + c; }
+};
+
+// Double-float accumulator: value = hi + lo.
+struct DF {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float a) {
+    const float t = hi + a;
+    const float z = t - hi;
+    lo += (hi - (t - z)) + (a - z);
+    hi = t;
+  }
+  __device__ __forceinline__ void merge(const DF& o) {
+    add(o.hi);
+    lo += o.lo;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+template <typename R>
+struct Sq;
+
+template <>
+struct Sq<float> {
+  struct Term {
+    float s, e;  // |v|^2 = s + e (to ~2^-46 relative)
+  };
+  static __device__ __forceinline__ Term term(float2 v) {
+    const float px = v.x * v.x, py = v.y * v.y;
+    const float ex = fmaf(v.x, v.x, -px), ey = fmaf(v.y, v.y, -py);
+    const float t = px + py;
+    const float z = t - px;
+    const float e2 = (px - (t - z)) + (py - z);
+    return {t, ex + ey + e2};
+  }
+  struct Accum {
+    DF d;
+    __device__ __forceinline__ void add(const Term& t) {
+      d.add(t.s);
+      d.lo += t.e;
+    }
+    __device__ __forceinline__ void merge(const Accum& o) { d.merge(o.d); }
+    __device__ __forceinline__ double value() const { return d.value(); }
+  };
+};
+
+template <>
+struct Sq<double> {
+  using Term = double;
+  static __device__ __forceinline__ Term term(double2 v) { return fma(v.x, v.x, v.y * v.y); }
+  struct Accum {
+    double s = 0.0;
+    __device__ __forceinline__ void add(Term t) { s += t; }
+    __device__ __forceinline__ void merge(const Accum& o) { s += o.s; }
+    __device__ __forceinline__ double value() const { return s; }
+  };
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -379,6 +442,7 @@ template <typename R>
 __global__ void __launch_bounds__(QSV_THREADS)
     k_probs_partial(const CT<R>* __restrict__ psi, const __grid_constant__ ProbArgs a,
                     double* __restrict__ partial) {
+  using S = Sq<R>;
   __shared__ double sh[32];
   const uint64_t blk = blockIdx.x + (uint64_t)blockIdx.y * gridDim.x;
   if (blk >= a.nbins * a.nchunks) return;
@@ -389,14 +453,21 @@ __global__ void __launch_bounds__(QSV_THREADS)
     if ((bin >> j) & 1ull) binbase |= a.binbit[j];
   const uint64_t r0 = chunk * a.chunk;
   const uint64_t r1 = min(r0 + a.chunk, a.nrest);
-  Acc acc;
-  for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-    const uint64_t idx = qsv_insert_zeros(r, a.pos, a.npos) | binbase;
-    const CT<R> v = psi[idx];
-    const double x = (double)v.x, y = (double)v.y;
-    acc.add(fma(x, x, y * y));
+  const uint64_t bd = blockDim.x;
+  typename S::Accum acc[4];
+  uint64_t r = r0 + threadIdx.x;
+  for (; r + 3 * bd < r1; r += 4 * bd) {
+    CT<R> v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = psi[qsv_insert_zeros(r + u * bd, a.pos, a.npos) | binbase];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u].add(S::term(v[u]));
   }
-  const double tot = block_sum(acc.value(), sh);
+  for (; r < r1; r += bd) acc[0].add(S::term(psi[qsv_insert_zeros(r, a.pos, a.npos) | binbase]));
+  acc[0].merge(acc[1]);
+  acc[2].merge(acc[3]);
+  acc[0].merge(acc[2]);
+  const double tot = block_sum(acc[0].value(), sh);
   if (threadIdx.x == 0) partial[blk] = tot;
 }
 
@@ -405,18 +476,14 @@ template <typename R>
 __global__ void __launch_bounds__(QSV_THREADS)
     k_probs_perbin(const CT<R>* __restrict__ psi, const __grid_constant__ ProbArgs a,
                    double* __restrict__ out) {
+  using S = Sq<R>;
   const uint64_t bin = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (bin >= a.nbins) return;
   uint64_t binbase = 0;
   for (int j = 0; j < a.m; ++j)
     if ((bin >> j) & 1ull) binbase |= a.binbit[j];
-  Acc acc;
-  for (uint64_t r = 0; r < a.nrest; ++r) {
-    const uint64_t idx = qsv_insert_zeros(r, a.pos, a.npos) | binbase;
-    const CT<R> v = psi[idx];
-    const double x = (double)v.x, y = (double)v.y;
-    acc.add(fma(x, x, y * y));
-  }
+  typename S::Accum acc;
+  for (uint64_t r = 0; r < a.nrest; ++r) acc.add(S::term(psi[qsv_insert_zeros(r, a.pos, a.npos) | binbase]));
   out[bin] = acc.value();
 }
 
@@ -446,47 +513,61 @@ __global__ void __launch_bounds__(QSV_THREADS)
   if (lane == 0) out[warp] = s + cc;
 }
 
-// All single-qubit marginals in one pass.  Block b owns amplitudes
-// [b*chunk, (b+1)*chunk) with chunk = 2^cbits >= 2^13; thread t visits t + 256*j.
-// Positions 0..7 are fixed per thread, 8..cbits-1 vary with j, >= cbits fixed per block.
-// partial[b*(n+1) + p] = sum |a|^2 over the chunk with bit p set; [.. + n] = chunk total.
+// All single-qubit marginals in one read of the state.  Chunk c holds amplitudes
+// [c*8192, (c+1)*8192); thread t of a block visits c*8192 + t + 256*j for j < 32, so
+// state bits 0..7 are fixed per thread, bits 8..12 are the bits of j and bits 13.. the
+// bits of c.  Blocks stride over chunks.  partial[block*(n+1) + p] = mass with state
+// bit p set; partial[block*(n+1) + n] = total mass.
+constexpr int MARG_CHUNK_BITS = 13;
+
 template <typename R>
 __global__ void __launch_bounds__(QSV_THREADS)
-    k_marginals_partial(const CT<R>* __restrict__ psi, int n, int cbits,
-                        double* __restrict__ partial) {
+    k_marginals(const CT<R>* __restrict__ psi, int n, uint64_t nchunks, double* __restrict__ partial) {
+  using S = Sq<R>;
   __shared__ double sh[32];
-  const uint64_t base = (uint64_t)blockIdx.x << cbits;
-  const uint64_t per_thread = 1ull << (cbits - 8);
-  double tot = 0.0;
-  double vb[QSV_MAXN];  // varying bits 8..cbits-1 (indexed by p-8)
+  typename S::Accum tot, vj[5], vc[QSV_MAXN - MARG_CHUNK_BITS];
+  for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const CT<R>* base = psi + (c << MARG_CHUNK_BITS) + threadIdx.x;
+    typename S::Accum tc;
 #pragma unroll
-  for (int p = 0; p < QSV_MAXN; ++p) vb[p] = 0.0;
-  for (uint64_t j = 0; j < per_thread; ++j) {
-    const uint64_t idx = base + threadIdx.x + (j << 8);
-    const CT<R> v = psi[idx];
-    const double x = (double)v.x, y = (double)v.y;
-    const double pr = fma(x, x, y * y);
-    tot += pr;
+    for (int j0 = 0; j0 < 32; j0 += 8) {
+      CT<R> v[8];
 #pragma unroll
-    for (int p = 0; p < QSV_MAXN - 8; ++p)
-      if (p < cbits - 8 && ((j >> p) & 1ull)) vb[p] += pr;
-  }
-  const double blocktot = block_sum(tot, sh);
-  if (threadIdx.x == 0) partial[(uint64_t)blockIdx.x * (n + 1) + n] = blocktot;
-  for (int p = 0; p < 8 && p < n; ++p) {
-    const double s = block_sum(((threadIdx.x >> p) & 1u) ? tot : 0.0, sh);
-    if (threadIdx.x == 0) partial[(uint64_t)blockIdx.x * (n + 1) + p] = s;
-  }
+      for (int u = 0; u < 8; ++u) v[u] = base[(j0 + u) << 8];
 #pragma unroll
-  for (int p = 0; p < QSV_MAXN - 8; ++p) {
-    if (p < cbits - 8) {
-      const double s = block_sum(vb[p], sh);
-      if (threadIdx.x == 0) partial[(uint64_t)blockIdx.x * (n + 1) + 8 + p] = s;
+      for (int u = 0; u < 8; ++u) {
+        const int j = j0 + u;
+        const auto t = S::term(v[u]);
+        tc.add(t);
+#pragma unroll
+        for (int b = 0; b < 5; ++b)
+          if ((j >> b) & 1) vj[b].add(t);
+      }
     }
+    tot.merge(tc);
+#pragma unroll
+    for (int b = 0; b < QSV_MAXN - MARG_CHUNK_BITS; ++b)
+      if (b < n - MARG_CHUNK_BITS && ((c >> b) & 1ull)) vc[b].merge(tc);
   }
-  for (int p = cbits; p < n; ++p) {
-    if (threadIdx.x == 0)
-      partial[(uint64_t)blockIdx.x * (n + 1) + p] = ((blockIdx.x >> (p - cbits)) & 1u) ? blocktot : 0.0;
+  double* row = partial + (uint64_t)blockIdx.x * (n + 1);
+  const double t = tot.value();
+  double r = block_sum(t, sh);
+  if (threadIdx.x == 0) row[n] = r;
+  for (int p = 0; p < 8; ++p) {
+    r = block_sum(((threadIdx.x >> p) & 1u) ? t : 0.0, sh);
+    if (threadIdx.x == 0) row[p] = r;
+  }
+#pragma unroll
+  for (int b = 0; b < 5; ++b) {
+    r = block_sum(vj[b].value(), sh);
+    if (threadIdx.x == 0) row[8 + b] = r;
+  }
+#pragma unroll
+  for (int b = 0; b < QSV_MAXN - MARG_CHUNK_BITS; ++b) {
+    if (b < n - MARG_CHUNK_BITS) {
+      r = block_sum(vc[b].value(), sh);
+      if (threadIdx.x == 0) row[MARG_CHUNK_BITS + b] = r;
+    }
   }
 }
 
@@ -1087,20 +1168,18 @@ int qsv_qubit_marginals(qsv_state* s, double* out, double* norm2) {
     if (norm2) *norm2 = tot;
     return QSV_OK;
   }
-  int cbits = 13;
-  while (cbits < n && ((1ull << (n - cbits)) > (uint64_t)std::max(1, s->sm_count) * 64)) ++cbits;
-  if (cbits > n) cbits = n;
-  const uint64_t nblocks = 1ull << (n - cbits);
+  const uint64_t nchunks = 1ull << (n - MARG_CHUNK_BITS);
+  const uint64_t nblocks = std::min<uint64_t>(nchunks, (uint64_t)std::max(1, s->sm_count) * 4);
   const size_t bytes = (nblocks * (n + 1) + (n + 1)) * sizeof(double);
   int rc = ensure_scratch(s, bytes);
   if (rc) return rc;
   double* partial = (double*)s->d_scratch;
   double* col = partial + nblocks * (n + 1);
   if (is_c64(s))
-    k_marginals_partial<float><<<(unsigned)nblocks, QSV_THREADS, 0, s->stream>>>((const float2*)s->d_amp, n, cbits, partial);
+    k_marginals<float><<<(unsigned)nblocks, QSV_THREADS, 0, s->stream>>>((const float2*)s->d_amp, n, nchunks, partial);
   else
-    k_marginals_partial<double><<<(unsigned)nblocks, QSV_THREADS, 0, s->stream>>>((const double2*)s->d_amp, n, cbits, partial);
-  rc = check_launch(s, "marginals_partial");
+    k_marginals<double><<<(unsigned)nblocks, QSV_THREADS, 0, s->stream>>>((const double2*)s->d_amp, n, nchunks, partial);
+  rc = check_launch(s, "marginals");
   if (rc) return rc;
   const unsigned fblocks = (unsigned)(((n + 1) * 32 + QSV_THREADS - 1) / QSV_THREADS);
   k_columns_finish<<<fblocks, QSV_THREADS, 0, s->stream>>>(partial, nblocks, n + 1, col);

@@ -45,25 +45,42 @@ template <int KQ>
 struct FB {
   static constexpr int T = 1 << KQ;            // target combinations
   static constexpr int KD = 2 * T;             // GEMM K = N
+  static constexpr int EBITS = FB_BATCH_BITS + KQ;  // bits of the tile index
+  static constexpr int TILE = FB_M * T;        // amplitudes per tile
   static constexpr int A_BYTES = FB_M * KD * 2;  // one bf16 copy of the tile
   static constexpr int W_BYTES = KD * KD * 2;    // one bf16 copy of W
+  static constexpr int RAW_BYTES = TILE * 8;     // complex64 staging of one tile
   static constexpr int A_LBO = FB_M * 16;        // K-step between core matrices of A
   static constexpr int W_LBO = KD * 16;
+  static constexpr int VEC = TILE / 2 / FB_THREADS;             // float4 (2 amplitudes) per thread
   static constexpr int ITEMS = (FB_M * (T / 8)) / FB_THREADS;  // (b, 8 targets) per thread
   static constexpr int TMEM_COLS = KD < 32 ? 32 : KD;
   static constexpr int COLS_PER_WARP = T / 2;  // output targets handled per warp
-  // Tables and barrier after the operands, then one W-sized pad: an operand read
-  // with the LBO/SBO roles exchanged would still stay inside this CTA's allocation.
-  static constexpr int SMEM = 2 * A_BYTES + 2 * W_BYTES + FB_M * 8 + T * 8 + 64 + W_BYTES;
+  // Tables: eb[128] u16, et[T] u16, swz[TILE/16] u8, dephi[T] u64; then the mbarrier.
+  static constexpr int TAB_BYTES = FB_M * 2 + T * 2 + TILE / 16 + T * 8;
+  static constexpr int SMEM = 2 * A_BYTES + 2 * W_BYTES + RAW_BYTES + ((TAB_BYTES + 15) / 16) * 16 + 64;
+  // The direct variant stages nothing: no RAW buffer.
+  static constexpr int SMEM_DIRECT = SMEM - RAW_BYTES;
 };
 
+// Tile geometry.  A tile covers the 2^k target combinations t and 128 groups b (the
+// 7 lowest non-target bit positions).  Its 7+k bit positions, sorted, are P; tile
+// element e (bit i of e <-> position P[i]) lives at tile_base + dep(e).  P always starts
+// with positions 0..6, so dep(e) = (e & 127) + dephi[e >> 7] and 16-byte pairs of
+// consecutive e are adjacent amplitudes.  The shared staging buffer stores element e at
+// word e ^ (swz[e >> 4] << 1): a host-chosen XOR of 16-byte slots that keeps the
+// (b-consecutive) transposing accesses spread over the banks for any placement.
 struct BlockArgs {
   uint64_t ntiles;
   int k;
-  int tpos[8];         // target bit positions, targets[0] first (MSB of the matrix index)
-  int tsorted[8];      // ascending
-  const uint4* wimg;   // hi image then lo image (2 * W_BYTES bytes)
-  int* flag;           // status word
+  int staged;           // 1: address-order staging (targets in the low 7 bits), 0: direct
+  int ptile[16];        // the 7+k tile positions, ascending (zero insertion -> tile base)
+  uint16_t eb[FB_M];    // e of group b
+  uint16_t et[64];      // e of target combination t (targets[0] = MSB of t)
+  uint8_t swz[512];     // 3-bit slot swizzle per (e >> 4)
+  uint64_t dephi[64];   // address offset of e >> 7
+  const uint4* wimg;    // hi image then lo image (2 * W_BYTES bytes)
+  int* flag;            // status word
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -200,18 +217,29 @@ __device__ __forceinline__ void split8(const float* x, uint4& hi, uint4& lo) {
   lo = make_uint4(pack_bf16(l[0], l[1]), pack_bf16(l[2], l[3]), pack_bf16(l[4], l[5]), pack_bf16(l[6], l[7]));
 }
 
-template <int KQ>
+// STAGED = false ("direct"): each thread loads (b, 8 targets) items straight from
+// global memory and the epilogue stores TMEM rows straight back; coalesced when the 7
+// lowest address bits are batch bits.  STAGED = true: the tile moves through a shared
+// staging buffer in address order (16-byte coalesced global accesses for any target
+// placement) at the cost of two extra shared-memory passes.
+template <int KQ, bool STAGED>
 __global__ void __launch_bounds__(FB_THREADS, 1)
     k_block_tc(float2* __restrict__ psi, const __grid_constant__ BlockArgs a) {
   using P = FB<KQ>;
+  constexpr int SMEM_USED = STAGED ? P::SMEM : P::SMEM_DIRECT;
+  constexpr int RAW = STAGED ? P::RAW_BYTES : 0;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA_hi = smem;
   uint8_t* sA_lo = smem + P::A_BYTES;
   uint8_t* sW_hi = smem + 2 * P::A_BYTES;
   uint8_t* sW_lo = sW_hi + P::W_BYTES;
-  uint64_t* boff = reinterpret_cast<uint64_t*>(sW_lo + P::W_BYTES);
-  uint64_t* toff = boff + FB_M;
-  uint64_t* mbar = toff + P::T;
+  float2* raw = reinterpret_cast<float2*>(sW_lo + P::W_BYTES);
+  float4* raw4 = reinterpret_cast<float4*>(raw);
+  uint16_t* eb = reinterpret_cast<uint16_t*>(sW_lo + P::W_BYTES + RAW);
+  uint16_t* et = eb + FB_M;
+  uint8_t* swz = reinterpret_cast<uint8_t*>(et + P::T);
+  uint64_t* dephi = reinterpret_cast<uint64_t*>(swz + P::TILE / 16);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + SMEM_USED - 64);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
 
@@ -219,22 +247,19 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   const int warp = tid >> 5;
   const int lane = tid & 31;
 
-  // W image (hi then lo) into shared memory.
+  // W image (hi then lo) and the geometry tables into shared memory.
   {
     const uint4* src = a.wimg;
     uint4* dst = reinterpret_cast<uint4*>(sW_hi);
     constexpr int NV = (2 * P::W_BYTES) / 16;
     for (int i = tid; i < NV; i += FB_THREADS) dst[i] = src[i];
   }
-  // Offset tables.
-  for (int b = tid; b < FB_M; b += FB_THREADS) boff[b] = qsv_insert_zeros((uint64_t)b, a.tsorted, KQ);
-  for (int t = tid; t < P::T; t += FB_THREADS) {
-    uint64_t off = 0;
-#pragma unroll
-    for (int j = 0; j < KQ; ++j)
-      if ((t >> (KQ - 1 - j)) & 1) off |= 1ull << a.tpos[j];
-    toff[t] = off;
+  for (int i = tid; i < FB_M; i += FB_THREADS) eb[i] = a.eb[i];
+  for (int i = tid; i < P::T; i += FB_THREADS) {
+    et[i] = a.et[i];
+    dephi[i] = a.dephi[i];
   }
+  for (int i = tid; i < P::TILE / 16; i += FB_THREADS) swz[i] = a.swz[i];
   if (tid == 0) {
     mbar_init(smem_u32(mbar), 1);
     *abort_flag = 0;
@@ -255,36 +280,62 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   constexpr uint32_t idesc = make_idesc(FB_M, P::KD);
   uint32_t phase = 0;
 
-  // Per-thread items: item = it*FB_THREADS + tid -> b = item % 128, tg = item / 128.
-  float2 buf[P::ITEMS][8];
-  auto load_tile = [&](uint64_t tile) {
-    const uint64_t base = qsv_insert_zeros(tile << FB_BATCH_BITS, a.tsorted, KQ);
+  auto slot = [&](int e) -> int { return e ^ ((int)swz[e >> 4] << 1); };
+  auto dep = [&](int e) -> uint64_t { return (uint64_t)(e & (FB_M - 1)) + dephi[e >> FB_BATCH_BITS]; };
+
+  // Staged: thread u-th pair holds elements e, e+1 with e = 2*(u*256 + tid) (adjacent
+  // amplitudes).  Direct: item it holds (b, targets tg*8..tg*8+7).
+  float4 buf[P::VEC];
+  float2 buf2[P::ITEMS][8];
+  auto load_tile = [&](uint64_t base) {
+    if constexpr (STAGED) {
 #pragma unroll
-    for (int it = 0; it < P::ITEMS; ++it) {
-      const int item = it * FB_THREADS + tid;
-      const int b = item & (FB_M - 1);
-      const int tg = item >> FB_BATCH_BITS;
-      const uint64_t rb = base + boff[b];
+      for (int u = 0; u < P::VEC; ++u) {
+        const int e = 2 * (u * FB_THREADS + tid);
+        buf[u] = __ldcs(reinterpret_cast<const float4*>(psi + base + dep(e)));
+      }
+    } else {
 #pragma unroll
-      for (int j = 0; j < 8; ++j) buf[it][j] = __ldcs(&psi[rb + toff[tg * 8 + j]]);
+      for (int it = 0; it < P::ITEMS; ++it) {
+        const int item = it * FB_THREADS + tid;
+        const int b = item & (FB_M - 1);
+        const int tg = item >> FB_BATCH_BITS;
+        const uint64_t rb = base + dep(eb[b]);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) buf2[it][j] = __ldcs(&psi[rb + dep(et[tg * 8 + j])]);
+      }
     }
   };
 
   uint64_t tile = blockIdx.x;
-  if (tile < a.ntiles) load_tile(tile);
+  uint64_t base = 0;
+  if (tile < a.ntiles) {
+    base = qsv_insert_zeros(tile, a.ptile, P::EBITS);
+    load_tile(base);
+  }
   for (; tile < a.ntiles; tile += gridDim.x) {
-    const uint64_t base = qsv_insert_zeros(tile << FB_BATCH_BITS, a.tsorted, KQ);
-    // Split into bf16 hi/lo and write the A operand (K-major, no swizzle).
+    // 1. Stage the tile in address order.
+    if constexpr (STAGED) {
+#pragma unroll
+      for (int u = 0; u < P::VEC; ++u) {
+        const int e = 2 * (u * FB_THREADS + tid);
+        raw4[slot(e) >> 1] = buf[u];
+      }
+      __syncthreads();
+    }
+    // 2. Transpose into the A operand: row b, K = [Re t | Im t], bf16 hi/lo split.
 #pragma unroll
     for (int it = 0; it < P::ITEMS; ++it) {
       const int item = it * FB_THREADS + tid;
       const int b = item & (FB_M - 1);
       const int tg = item >> FB_BATCH_BITS;
+      const int eb_ = eb[b];
       float re[8], im[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        re[j] = buf[it][j].x;
-        im[j] = buf[it][j].y;
+        const float2 v = STAGED ? raw[slot(eb_ | et[tg * 8 + j])] : buf2[it][j];
+        re[j] = v.x;
+        im[j] = v.y;
       }
       uint4 rh, rl, ih, il;
       split8(re, rh, rl);
@@ -300,6 +351,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
+    // 3. Three split-bf16 products into TMEM.
     if (tid == 0) {
       const uint32_t a_hi = smem_u32(sA_hi), a_lo = smem_u32(sA_lo);
       const uint32_t w_hi = smem_u32(sW_hi), w_lo = smem_u32(sW_lo);
@@ -318,21 +370,25 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
                make_smem_desc(w_hi + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, 1u);
       tc_commit(bar);
     }
-    // Prefetch the next tile while the tensor cores work.
+    // 4. Prefetch the next tile while the tensor cores work.
     const uint64_t next = tile + gridDim.x;
-    if (next < a.ntiles) load_tile(next);
+    uint64_t next_base = 0;
+    if (next < a.ntiles) {
+      next_base = qsv_insert_zeros(next, a.ptile, P::EBITS);
+      load_tile(next_base);
+    }
     if (!mbar_wait_bounded(bar, phase)) atomicExch(abort_flag, 1);
     phase ^= 1u;
     tc_fence_after();
     __syncthreads();
     if (*abort_flag) break;
-    // Epilogue: warp w reads TMEM lanes 32*(w%4).. (rows b) and output targets
-    // [h*T/2, (h+1)*T/2) with h = w/4.
+    // 5. Epilogue: TMEM lane b -> the staging buffer.  Warp w reads lanes 32*(w%4)..
+    //    and output targets [h*T/2, (h+1)*T/2) with h = w/4.
     {
       const int q = warp & 3;
       const int h = warp >> 2;
       const int b = q * 32 + lane;
-      const uint64_t rb = base + boff[b];
+      const int eb_ = eb[b];
       const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
       constexpr int CH = P::COLS_PER_WARP < 32 ? P::COLS_PER_WARP : 32;
 #pragma unroll
@@ -342,13 +398,29 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         tmem_ld<CH>(lane_addr + (uint32_t)t0, re);
         tmem_ld<CH>(lane_addr + (uint32_t)(P::T + t0), im);
         tmem_ld_wait();
+        if constexpr (STAGED) {
 #pragma unroll
-        for (int j = 0; j < CH; ++j) __stcs(&psi[rb + toff[t0 + j]], make_float2(re[j], im[j]));
+          for (int j = 0; j < CH; ++j) raw[slot(eb_ | et[t0 + j])] = make_float2(re[j], im[j]);
+        } else {
+          const uint64_t rb = base + dep(eb_);
+#pragma unroll
+          for (int j = 0; j < CH; ++j) __stcs(&psi[rb + dep(et[t0 + j])], make_float2(re[j], im[j]));
+        }
       }
     }
     tc_fence_before();
     __syncthreads();
+    if constexpr (STAGED) {
+      // 6. Write the tile back in address order.
+#pragma unroll
+      for (int u = 0; u < P::VEC; ++u) {
+        const int e = 2 * (u * FB_THREADS + tid);
+        __stcs(reinterpret_cast<float4*>(psi + base + dep(e)), raw4[slot(e) >> 1]);
+      }
+      __syncthreads();
+    }
     tc_fence_after();
+    base = next_base;
   }
   if (*abort_flag) {
     // Give the tensor cores a last bounded chance to finish before freeing TMEM.
@@ -412,24 +484,109 @@ void build_image(int k, const double* U, uint8_t* out) {
   }
 }
 
-template <int KQ>
-int launch_block(qsv_state* s, const BlockArgs& a) {
+// Tile geometry of a block on target positions tpos[0..k) (tpos[0] = MSB of t):
+// sorted tile positions, the e-index maps of groups and targets, the address table
+// and the staging swizzle (see BlockArgs).
+void tile_geometry(int k, const int* tpos, BlockArgs& a) {
+  const int ebits = FB_BATCH_BITS + k;
+  uint64_t tmask = 0;
+  for (int j = 0; j < k; ++j) tmask |= 1ull << tpos[j];
+  // Direct loads/stores stay coalesced while few targets sit in the 7 lowest bits.
+  a.staged = __builtin_popcountll(tmask & 0x7Full) >= 3 ? 1 : 0;
+  int batch[FB_BATCH_BITS];
+  for (int p = 0, nb = 0; nb < FB_BATCH_BITS; ++p)
+    if (!((tmask >> p) & 1ull)) batch[nb++] = p;
+  uint64_t pmask = tmask;
+  for (int i = 0; i < FB_BATCH_BITS; ++i) pmask |= 1ull << batch[i];
+  int eidx[64];
+  for (int p = 0, e = 0; p < 64; ++p)
+    if ((pmask >> p) & 1ull) {
+      a.ptile[e] = p;
+      eidx[p] = e++;
+    }
+  for (int b = 0; b < FB_M; ++b) {
+    int e = 0;
+    for (int i = 0; i < FB_BATCH_BITS; ++i)
+      if ((b >> i) & 1) e |= 1 << eidx[batch[i]];
+    a.eb[b] = (uint16_t)e;
+  }
+  const int T = 1 << k;
+  for (int t = 0; t < T; ++t) {
+    int e = 0;
+    for (int j = 0; j < k; ++j)
+      if ((t >> (k - 1 - j)) & 1) e |= 1 << eidx[tpos[j]];
+    a.et[t] = (uint16_t)e;
+  }
+  for (int x = 0; x < (1 << (ebits - FB_BATCH_BITS)); ++x) {
+    uint64_t off = 0;
+    for (int j = 0; j < ebits - FB_BATCH_BITS; ++j)
+      if ((x >> j) & 1) off |= 1ull << a.ptile[FB_BATCH_BITS + j];
+    a.dephi[x] = off;
+  }
+  // Swizzle: lanes of a warp hold 32 consecutive b, i.e. vary the e-bits of batch bits
+  // 0..4.  Word position of e in a 128-byte row = (e & 15) ^ (swz << 1); choose the
+  // 3-bit constant of each e-bit >= 4 so those lanes span as many word positions as
+  // possible (rank over GF(2)); e-bits < 4 contribute themselves.
+  int c[16] = {0};
+  unsigned span[16];  // basis vectors (4-bit) by leading bit
+  for (int i = 0; i < 16; ++i) span[i] = 0;
+  auto insert = [&](unsigned v) -> bool {
+    for (int bit = 3; bit >= 0; --bit) {
+      if (!((v >> bit) & 1u)) continue;
+      if (!span[bit]) {
+        span[bit] = v;
+        return true;
+      }
+      v ^= span[bit];
+    }
+    return false;
+  };
+  for (int i = 0; i < 5; ++i) {
+    const int e = eidx[batch[i]];
+    if (e < 4) insert(1u << e);
+  }
+  for (int i = 0; i < 5; ++i) {
+    const int e = eidx[batch[i]];
+    if (e < 4) continue;
+    for (unsigned cand = 1; cand < 8; ++cand) {
+      if (insert(cand << 1)) {
+        c[e] = (int)cand;
+        break;
+      }
+    }
+  }
+  for (int y = 0; y < (1 << (ebits - 4)); ++y) {
+    int v = 0;
+    for (int j = 0; j < ebits - 4; ++j)
+      if ((y >> j) & 1) v ^= c[4 + j];
+    a.swz[y] = (uint8_t)v;
+  }
+}
+
+template <int KQ, bool STAGED>
+int launch_block_variant(qsv_state* s, const BlockArgs& a) {
   using P = FB<KQ>;
+  constexpr int SMEM = STAGED ? P::SMEM : P::SMEM_DIRECT;
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_block_tc<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM);
+    cudaError_t e = cudaFuncSetAttribute(k_block_tc<KQ, STAGED>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
     if (e != cudaSuccess) return set_error(s, QSV_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(e));
     configured = true;
   }
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_block_tc<KQ>, FB_THREADS, P::SMEM);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_block_tc<KQ, STAGED>, FB_THREADS, SMEM);
   if (per_sm < 1) per_sm = 1;
   // Bound co-resident CTAs so their TMEM allocations always fit (512 columns per SM).
   per_sm = std::min(per_sm, 512 / P::TMEM_COLS);
   uint64_t grid = (uint64_t)std::max(1, s->sm_count) * per_sm;
   if (grid > a.ntiles) grid = a.ntiles;
-  k_block_tc<KQ><<<(unsigned)grid, FB_THREADS, P::SMEM, s->stream>>>((float2*)s->d_amp, a);
+  k_block_tc<KQ, STAGED><<<(unsigned)grid, FB_THREADS, SMEM, s->stream>>>((float2*)s->d_amp, a);
   return check_launch(s, "block_tc");
+}
+
+template <int KQ>
+int launch_block(qsv_state* s, const BlockArgs& a) {
+  return a.staged ? launch_block_variant<KQ, true>(s, a) : launch_block_variant<KQ, false>(s, a);
 }
 
 }  // namespace
@@ -468,12 +625,12 @@ int prepare_blocks(qsv_state* s, int nblocks, const int* ks, const int* targets_
                        s->n, k);
     BlockArgs& a = args[(size_t)i];
     uint64_t seen = 0;
-    int rc = to_positions(s, k, targets_flat + tofs, a.tpos, &seen);
+    int tpos[8];
+    int rc = to_positions(s, k, targets_flat + tofs, tpos, &seen);
     if (rc) return rc;
     a.k = k;
-    for (int j = 0; j < k; ++j) a.tsorted[j] = a.tpos[j];
-    std::sort(a.tsorted, a.tsorted + k);
     a.ntiles = 1ull << (s->n - k - FB_BATCH_BITS);
+    tile_geometry(k, tpos, a);
     a.flag = s->d_flag;
     img_off[(size_t)i] = total;
     mat_offs[(size_t)i] = mat_off;
