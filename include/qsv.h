@@ -133,6 +133,24 @@ int qsv_collapse(qsv_state* s, int m, const int* qubits, uint64_t value, double 
  * remaining qubits keep their order.  Replaces reduce_measure (kronprod.pyx:449-490). */
 int qsv_reduce(qsv_state* s, int m, const int* qubits, uint64_t value, double scale);
 
+/* Marginal probabilities of a caller-owned state without allocating device memory.
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc when they
+ * need the distribution — their device memory belongs to another allocator (e.g. a
+ * framework that has reserved all of HBM), or they run in a loop where allocating is
+ * not allowed.  Same result as qsv_probabilities (out[v], bit j of v <-> qubits[j]) for
+ * a state of 2^n amplitudes of `dtype` at device address d_amp; d_out is a device
+ * buffer of 2^m doubles; work is queued on `stream` (NULL = the default stream) and
+ * nothing is copied to the host.  Partial sums use a file-scope device array of 2^16
+ * doubles (512 KiB, held by every GPU that loads the library until exit), so
+ * m <= QSV_STATIC_MAX_MEASURED (16); larger m returns QSV_ERR_INVALID.  The first call
+ * on a device looks up that array's address (once per device, with the device
+ * current), so make the first call before any stream capture.  Every call shares the
+ * array: calls that overlap on the GPU (different streams, or concurrent threads)
+ * race and must be ordered by the caller.  Errors: qsv_last_error(NULL). */
+#define QSV_STATIC_MAX_MEASURED 16
+int qsv_probabilities_static(const void* d_amp, int n, int dtype, int m, const int* qubits,
+                             double* d_out, void* stream);
+
 /* <a|b> = sum conj(a_i) b_i in FP64 (compensated), states of equal n, any dtypes.
  * Used for infidelity 1 - |<a|b>|^2 / (<a|a><b|b>).  No reference counterpart. */
 int qsv_inner_product(qsv_state* a, qsv_state* b, double* re, double* im);

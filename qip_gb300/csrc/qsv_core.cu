@@ -1328,3 +1328,112 @@ int qsv_inner_product(qsv_state* a, qsv_state* b, double* re, double* im) {
 }
 
 }  // extern "C"
+
+// ======================================================================================
+// Allocation-free marginal probabilities
+// ======================================================================================
+// Some callers cannot allocate device memory at the moment they need probabilities: a
+// host whose HBM is owned by another allocator (e.g. a framework's caching allocator
+// that has reserved the whole device), or a latency-critical loop where an allocation
+// (and the synchronisation it implies) is not allowed.  qsv_probabilities_static serves
+// them: the caller passes the state and the output buffer, and the per-block partial
+// sums go to the file-scope array below instead of a cudaMalloc'ed scratch.  Every GPU
+// that loads this library holds the array (512 KiB) until the process exits.
+constexpr size_t QSV_STATIC_PARTIALS = size_t(1) << 16;  // doubles: 512 KiB
+static __device__ __align__(256) double g_static_partials[QSV_STATIC_PARTIALS];
+
+namespace {
+constexpr int QSV_MAX_DEVICES = 64;
+std::mutex g_static_mu;
+double* g_static_ptr[QSV_MAX_DEVICES] = {nullptr};
+int g_static_sms[QSV_MAX_DEVICES] = {0};
+
+// Device address of g_static_partials on the current device (looked up once per device;
+// in host code the symbol's name is only a host-side stand-in).
+int static_partials(double** out, int* sms) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return set_error(nullptr, QSV_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= QSV_MAX_DEVICES) return set_error(nullptr, QSV_ERR_UNSUPPORTED, "device ordinal %d", dev);
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_partials);
+    if (e != cudaSuccess)
+      return set_error(nullptr, QSV_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    int count = 0;
+    e = cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return set_error(nullptr, QSV_ERR_CUDA, "device attribute: %s", cudaGetErrorString(e));
+    g_static_ptr[dev] = static_cast<double*>(p);
+    g_static_sms[dev] = count;
+  }
+  *out = g_static_ptr[dev];
+  *sms = g_static_sms[dev];
+  return QSV_OK;
+}
+
+template <typename R>
+int launch_probs_static(const void* d_amp, int n, int m, const int* pos_in_order, double* d_out,
+                        cudaStream_t stream, double* partial, int sms) {
+  ProbArgs a;
+  a.m = m;
+  a.npos = m;
+  const uint64_t nbins = 1ull << m;
+  a.nbins = nbins;
+  a.nrest = 1ull << (n - m);
+  for (int j = 0; j < m; ++j) {
+    a.binbit[j] = 1ull << pos_in_order[j];
+    a.pos[j] = pos_in_order[j];
+  }
+  std::sort(a.pos, a.pos + m);
+  // Chunk the rest index so that nbins * nchunks partials fit the static array.
+  const uint64_t target = std::min<uint64_t>((uint64_t)std::max(1, sms) * 32, QSV_STATIC_PARTIALS);
+  uint64_t chunk = 4096;
+  while (chunk < a.nrest && (nbins * ((a.nrest + chunk - 1) / chunk) > target)) chunk <<= 1;
+  if (chunk > a.nrest) chunk = a.nrest;
+  a.chunk = chunk;
+  a.nchunks = (a.nrest + chunk - 1) / chunk;
+  const uint64_t nblk = nbins * a.nchunks;
+  if (nblk > QSV_STATIC_PARTIALS)
+    return set_error(nullptr, QSV_ERR_INVALID, "%llu partial sums exceed the static scratch of %zu",
+                     (unsigned long long)nblk, QSV_STATIC_PARTIALS);
+  dim3 grid;
+  grid.x = (unsigned)std::min<uint64_t>(nblk, 65535ull * 1024);
+  grid.y = (unsigned)((nblk + grid.x - 1) / grid.x);
+  k_probs_partial<R><<<grid, QSV_THREADS, 0, stream>>>((const CT<R>*)d_amp, a, partial);
+  int rc = check_launch(nullptr, "probs_partial (static scratch)");
+  if (rc) return rc;
+  const unsigned fblocks = (unsigned)((nbins * 32 + QSV_THREADS - 1) / QSV_THREADS);
+  k_probs_finish<<<fblocks, QSV_THREADS, 0, stream>>>(partial, a.nchunks, nbins, d_out);
+  return check_launch(nullptr, "probs_finish (static scratch)");
+}
+}  // namespace
+
+extern "C" int qsv_probabilities_static(const void* d_amp, int n, int dtype, int m, const int* qubits,
+                                        double* d_out, void* stream) {
+  if (!d_amp || !d_out) return set_error(nullptr, QSV_ERR_INVALID, "null state or output pointer");
+  if (n < 1 || n > QSV_MAXN) return set_error(nullptr, QSV_ERR_INVALID, "n=%d outside [1, %d]", n, QSV_MAXN);
+  if (dtype != QSV_C64 && dtype != QSV_C128) return set_error(nullptr, QSV_ERR_INVALID, "unknown dtype %d", dtype);
+  if (m < 0 || m > n || m > QSV_STATIC_MAX_MEASURED)
+    return set_error(nullptr, QSV_ERR_INVALID,
+                     "%d measured qubits: the allocation-free path takes at most %d (2^%d outcomes)", m,
+                     QSV_STATIC_MAX_MEASURED, QSV_STATIC_MAX_MEASURED);
+  if (m > 0 && !qubits) return set_error(nullptr, QSV_ERR_INVALID, "null qubit list");
+  int pos[QSV_MAXQ];
+  uint64_t seen = 0;
+  for (int j = 0; j < m; ++j) {
+    const int q = qubits[j];
+    if (q < 0 || q >= n) return set_error(nullptr, QSV_ERR_INVALID, "qubit index %d out of range for n=%d", q, n);
+    const int p = n - 1 - q;
+    if (seen & (1ull << p)) return set_error(nullptr, QSV_ERR_INVALID, "qubit %d repeated", q);
+    seen |= 1ull << p;
+    pos[j] = p;
+  }
+  double* partial = nullptr;
+  int sms = 0;
+  int rc = static_partials(&partial, &sms);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  return dtype == QSV_C64 ? launch_probs_static<float>(d_amp, n, m, pos, d_out, st, partial, sms)
+                          : launch_probs_static<double>(d_amp, n, m, pos, d_out, st, partial, sms);
+}
