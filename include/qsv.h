@@ -155,6 +155,65 @@ int qsv_probabilities_static(const void* d_amp, int n, int dtype, int m, const i
  * Used for infidelity 1 - |<a|b>|^2 / (<a|a><b|b>).  No reference counterpart. */
 int qsv_inner_product(qsv_state* a, qsv_state* b, double* re, double* im);
 
+/* ---- batched states and adjoint gradients ----------------------------------------------
+ * A batch is nsets states of 2^n amplitudes back to back in one caller-owned device
+ * buffer (e.g. a [nsets, 2^n] torch tensor); every call is asynchronous on `stream`.
+ * No reference counterpart: the reference has no batching and no gradients; these serve
+ * the adjoint-method differentiation of parameterised circuits. */
+/* Every state of the batch := |0...0>. */
+int qsv_batch_reset(void* psi, int nsets, int n, int dtype, void* stream);
+/* psi[s] <- M_s psi[s] on `target` (qubit index), controlled by `control` (-1: none);
+ * mats holds nsets row-major 2x2 matrices of the batch's dtype. */
+int qsv_batch_apply_1q(void* psi, int nsets, int n, int dtype, int target, int control,
+                       const void* mats, void* stream);
+/* lambda[s] := (sum_i Z_i) psi[s] and energies[s] := <psi[s]| sum_i Z_i |psi[s]> (FP64,
+ * device array).  scratch: caller-owned device doubles for partial sums. */
+int qsv_batch_observable_sumz(const void* psi, void* lam, int nsets, int n, int dtype,
+                              double* energies, double* scratch, size_t scratch_doubles,
+                              void* stream);
+/* One adjoint step for gate g: when generator is 1 (Y) or 2 (Z) the gate is
+ * exp(-i theta P/2) on `target` and grads[s * grad_stride] := Im <lambda[s]| P |psi[s]>
+ * (= dE/dtheta); then psi[s] <- M_s psi[s] and lambda[s] <- M_s lambda[s] with
+ * M_s = U_s^+ given in mats_dagger. */
+int qsv_batch_adjoint_step(void* psi, void* lam, int nsets, int n, int dtype, int target,
+                           int control, const void* mats_dagger, int generator, double* grads,
+                           int grad_stride, double* scratch, size_t scratch_doubles,
+                           void* stream);
+
+/* ---- many small circuits in one persistent launch --------------------------------------
+ * No reference counterpart (the reference runs one circuit per run() call).  A batch
+ * object holds a gate table, a circuit table, per-qubit product-state feeds and the
+ * output states of every circuit in device memory.  qsv_circuits_run replays one
+ * persistent launch (captured once into a CUDA graph on the given, non-default
+ * stream): one CTA per SM takes circuits from an atomic counter (in table order, so
+ * put long circuits first); n <= 14 circuits run entirely in shared memory. */
+typedef struct qsv_circuits qsv_circuits;
+/* Gate record (48 bytes).  kind 0 DENSE1: 2x2 complex64 m on q0; 1 PHASE1: |1> of q0 gets
+ * phase (m[0], m[1]); 2 X on q0; 3 CX: target q0, control q1; 4 CSWAP: control q0, swap
+ * q1 and q2.  Qubit indices: 0 = most significant bit of the circuit's state. */
+struct qsv_gate_rec {
+  int32_t kind;
+  int32_t q0, q1, q2;
+  float m[8];
+};
+/* Circuit record (32 bytes): n (3..24), gate count, offset of its first gate, offset of
+ * its output state (amplitudes) and of its feeds (2 complex64 values per qubit, qubit 0
+ * first; the input is the product of the per-qubit feeds). */
+struct qsv_circuit_rec {
+  int32_t n, ngates;
+  int64_t gate_offset;
+  int64_t state_offset;
+  int64_t feed_offset;
+};
+int qsv_circuits_create(const void* gates, int64_t ngates, const void* circuits, int ncircuits,
+                        const void* feeds_c64, int64_t nfeeds, qsv_circuits** out);
+int qsv_circuits_run(qsv_circuits* b, void* stream);
+/* Final state of one circuit (2^n complex64) to host memory.  Blocks. */
+int qsv_circuits_read(qsv_circuits* b, int circuit, void* host_out);
+/* Per-circuit device timestamps [start, end] in ns (2 * ncircuits values).  Blocks. */
+int qsv_circuits_times(qsv_circuits* b, unsigned long long* host_out);
+int qsv_circuits_destroy(qsv_circuits* b);
+
 /* ---- function oracle -----------------------------------------------------------------
  * |x>|q>|r> -> |x>|f(x) xor q>|r> with f given as a table of 2^n1 values.
  * Replaces func_apply (qip/ext/func_apply.pyx:9-112). */

@@ -62,6 +62,22 @@ SIGNATURES = {
     "qsv_probabilities_static": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_int_p,
                                                 ctypes.c_void_p, ctypes.c_void_p]),
     "qsv_inner_product": (ctypes.c_int, [_handle, _handle, _c_double_p, _c_double_p]),
+    "qsv_batch_reset": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+    "qsv_batch_apply_1q": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    "qsv_batch_observable_sumz": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                 ctypes.c_void_p]),
+    "qsv_batch_adjoint_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                              ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                              ctypes.c_size_t, ctypes.c_void_p]),
+    "qsv_circuits_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
+    "qsv_circuits_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "qsv_circuits_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "qsv_circuits_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "qsv_circuits_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "qsv_func_apply": (ctypes.c_int, [_handle, ctypes.c_int, _c_int_p, ctypes.c_int, _c_int_p, _c_int64_p]),
 }
 

@@ -1,0 +1,172 @@
+"""Adjoint-method gradients of parameterised circuits behind a torch.autograd.Function.
+
+Workload: the hardware-efficient ansatz of ``circuits.ansatz_layers`` — per layer RY(theta)
+on every qubit, RZ(phi) on every qubit, then a CNOT ring (i, i+1 mod n) — on |0...0>,
+objective E = <psi| sum_i Z_i |psi>, for a batch of parameter sets at once.
+
+Forward: every gate is one batched launch (all parameter sets, each with its own 2x2
+matrix built on the device from its angle); then lambda = (sum Z) psi and E in FP64.
+Backward (adjoint method, no checkpoints): walk the gates in reverse; at a rotation,
+dE/dtheta = Im <lambda| P |psi> (P = Y or Z) is reduced per set, then psi and lambda
+are un-computed by U^+ in the same pass.  Two state vectors per set (psi, lambda).
+
+There is no reference counterpart (the reference has no gradients); results are checked
+against central finite differences and the parameter-shift rule on the FP64 oracle and
+on the reference's own kernel (tests/golden).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import List, Tuple
+
+import numpy
+import torch
+
+from . import _native as nat
+
+RY, RZ, CNOT = 0, 1, 2
+
+
+@dataclass
+class Ansatz:
+    n: int
+    layers: int
+
+    @property
+    def nparams(self) -> int:
+        return 2 * self.n * self.layers
+
+    def gates(self) -> List[Tuple[int, int, int, int]]:
+        """(kind, target, control, param index or -1), in application order.  Parameter
+        layout: layer-major, RY block then RZ block (as ``circuits.ansatz_layers``)."""
+        out = []
+        n = self.n
+        for l in range(self.layers):
+            for q in range(n):
+                out.append((RY, q, -1, (2 * l) * n + q))
+            for q in range(n):
+                out.append((RZ, q, -1, (2 * l + 1) * n + q))
+            for q in range(n):
+                out.append((CNOT, (q + 1) % n, q, -1))
+        return out
+
+
+def _dtype(statetype):
+    if statetype in (torch.complex64, numpy.complex64):
+        return torch.complex64, nat.QSV_C64
+    return torch.complex128, nat.QSV_C128
+
+
+def gate_matrices(ansatz: Ansatz, thetas: torch.Tensor, cdtype) -> Tuple[torch.Tensor, torch.Tensor]:
+    """Per-gate, per-set 2x2 matrices U and U^+ as [G, B, 4] tensors on the device."""
+    B = thetas.shape[0]
+    gates = ansatz.gates()
+    G = len(gates)
+    th = thetas.to(torch.float64)
+    U = torch.zeros((G, B, 4), dtype=torch.complex128, device=thetas.device)
+    kinds = torch.tensor([g[0] for g in gates], device=thetas.device)
+    pidx = torch.tensor([max(g[3], 0) for g in gates], device=thetas.device)
+    ang = th[:, pidx].T  # [G, B]
+    c, s = torch.cos(ang / 2), torch.sin(ang / 2)
+    e = torch.exp(-0.5j * ang.to(torch.complex128))
+    ry = (kinds == RY)[:, None]
+    rz = (kinds == RZ)[:, None]
+    cx = (kinds == CNOT)[:, None]
+    zero = torch.zeros_like(c, dtype=torch.complex128)
+    one = torch.ones_like(c, dtype=torch.complex128)
+    U[:, :, 0] = torch.where(ry, c.to(torch.complex128), torch.where(rz, e, zero))
+    U[:, :, 1] = torch.where(ry, -s.to(torch.complex128), torch.where(cx, one, zero))
+    U[:, :, 2] = torch.where(ry, s.to(torch.complex128), torch.where(cx, one, zero))
+    U[:, :, 3] = torch.where(ry, c.to(torch.complex128), torch.where(rz, torch.conj(e), zero))
+    Ud = torch.stack([U[..., 0].conj(), U[..., 2].conj(), U[..., 1].conj(), U[..., 3].conj()], dim=-1)
+    return U.to(cdtype).contiguous(), Ud.to(cdtype).contiguous()
+
+
+def _stream_ptr() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _check(rc: int, what: str):
+    if rc != 0:
+        nat.check(rc, None, what)
+
+
+def forward_states(ansatz: Ansatz, U: torch.Tensor, cdtype, qdtype) -> torch.Tensor:
+    lib = nat.load()
+    B = U.shape[1]
+    n = ansatz.n
+    psi = torch.empty((B, 2 ** n), dtype=cdtype, device=U.device)
+    st = ctypes.c_void_p(_stream_ptr())
+    _check(lib.qsv_batch_reset(ctypes.c_void_p(psi.data_ptr()), B, n, qdtype, st), "batch_reset")
+    stride = U.stride(0) * U.element_size()
+    base = U.data_ptr()
+    for g, (kind, tgt, ctl, _) in enumerate(ansatz.gates()):
+        _check(lib.qsv_batch_apply_1q(ctypes.c_void_p(psi.data_ptr()), B, n, qdtype, tgt, ctl,
+                                      ctypes.c_void_p(base + g * stride), st), "batch_apply_1q")
+    return psi
+
+
+def _scratch(B: int, device) -> torch.Tensor:
+    return torch.empty(B * 4096, dtype=torch.float64, device=device)
+
+
+class SumZExpectation(torch.autograd.Function):
+    """E[b] = <psi(thetas[b])| sum_i Z_i |psi(thetas[b])> with adjoint gradients."""
+
+    @staticmethod
+    def forward(ctx, thetas: torch.Tensor, ansatz: Ansatz, statetype=torch.complex64):
+        if not thetas.is_cuda:
+            raise ValueError("thetas must live on the CUDA device")
+        cdtype, qdtype = _dtype(statetype)
+        U, Ud = gate_matrices(ansatz, thetas.detach(), cdtype)
+        psi = forward_states(ansatz, U, cdtype, qdtype)
+        lam = torch.empty_like(psi)
+        B = thetas.shape[0]
+        energies = torch.empty(B, dtype=torch.float64, device=thetas.device)
+        scratch = _scratch(B, thetas.device)
+        lib = nat.load()
+        _check(lib.qsv_batch_observable_sumz(ctypes.c_void_p(psi.data_ptr()), ctypes.c_void_p(lam.data_ptr()),
+                                             B, ansatz.n, qdtype, ctypes.c_void_p(energies.data_ptr()),
+                                             ctypes.c_void_p(scratch.data_ptr()), scratch.numel(),
+                                             ctypes.c_void_p(_stream_ptr())), "observable")
+        ctx.ansatz, ctx.qdtype = ansatz, qdtype
+        ctx.buffers = (psi, lam, Ud, scratch)
+        ctx.tdtype = thetas.dtype
+        return energies.to(thetas.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_e: torch.Tensor):
+        psi, lam, Ud, scratch = ctx.buffers
+        ctx.buffers = None
+        grads = adjoint_sweep(ctx.ansatz, psi, lam, Ud, scratch, ctx.qdtype)
+        return (grad_e.to(torch.float64)[:, None] * grads).to(ctx.tdtype), None, None
+
+
+def adjoint_sweep(ansatz: Ansatz, psi, lam, Ud, scratch, qdtype) -> torch.Tensor:
+    """Reverse sweep; consumes psi and lambda.  Returns dE/dtheta as [B, P] float64."""
+    lib = nat.load()
+    B = psi.shape[0]
+    P = ansatz.nparams
+    grads = torch.zeros((B, P), dtype=torch.float64, device=psi.device)
+    st = ctypes.c_void_p(_stream_ptr())
+    stride = Ud.stride(0) * Ud.element_size()
+    gates = ansatz.gates()
+    gp = grads.data_ptr()
+    for g in range(len(gates) - 1, -1, -1):
+        kind, tgt, ctl, pi = gates[g]
+        gen = {RY: 1, RZ: 2}.get(kind, 0)
+        gptr = ctypes.c_void_p(gp + 8 * pi) if gen else None
+        _check(lib.qsv_batch_adjoint_step(ctypes.c_void_p(psi.data_ptr()), ctypes.c_void_p(lam.data_ptr()), B,
+                                          ansatz.n, qdtype, tgt, ctl, ctypes.c_void_p(Ud.data_ptr() + g * stride),
+                                          gen, gptr, P, ctypes.c_void_p(scratch.data_ptr()), scratch.numel(), st),
+               "adjoint_step")
+    return grads
+
+
+def energy_and_grad(thetas: torch.Tensor, ansatz: Ansatz, statetype=torch.complex64):
+    """Convenience: (E [B], dE/dtheta [B, P]) through the autograd Function."""
+    th = thetas.detach().clone().requires_grad_(True)
+    e = SumZExpectation.apply(th, ansatz, statetype)
+    e.sum().backward()
+    return e.detach(), th.grad

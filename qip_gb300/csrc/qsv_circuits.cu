@@ -1,0 +1,315 @@
+// Many independent small circuits in one persistent launch.
+//
+// One CTA per SM takes circuits from a global counter (an atomicAdd work queue: no
+// CTA ever waits on another).  The host orders circuits by estimated cost, longest
+// first, so the tail of the launch is short.  A circuit of n <= 14 qubits lives entirely
+// in shared memory (2^14 complex64 = 128 KiB): its product-state input is built there
+// from the per-qubit feeds, every gate is applied there, and the final state is
+// written to global memory once.  Larger circuits (n <= 24) are built and updated in
+// their global output slot, one CTA-wide pass per gate.  Each circuit records device
+// timestamps (%globaltimer) when its CTA starts and finishes it.
+//
+// The launch (counter reset + kernel) is captured once into a CUDA graph owned by the
+// batch object and replayed by qsv_circuits_run.
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "qsv_internal.cuh"
+
+using namespace qsv;
+
+namespace {
+
+constexpr int CB_THREADS = 512;
+constexpr int CB_SMEM_QUBITS = 14;
+constexpr int CB_MAX_QUBITS = 24;
+
+enum GateKind : int32_t { G_DENSE1 = 0, G_PHASE1 = 1, G_X = 2, G_CX = 3, G_CSWAP = 4 };
+
+}  // namespace
+
+// Record layouts qsv_gate_rec / qsv_circuit_rec are declared in include/qsv.h
+// (mirrored by qip_gb300/batch.py).
+
+struct qsv_circuits {
+  int ncirc = 0;
+  qsv_gate_rec* d_gates = nullptr;
+  qsv_circuit_rec* d_circs = nullptr;
+  float2* d_feeds = nullptr;
+  float2* d_states = nullptr;
+  unsigned long long* d_times = nullptr;
+  int* d_counter = nullptr;
+  size_t state_amps = 0;
+  std::vector<qsv_circuit_rec> h_circs;
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  int sm_count = 0;
+};
+
+namespace {
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint64_t ins0(uint64_t g, int p) {
+  return ((g >> p) << (p + 1)) | (g & ((1ull << p) - 1ull));
+}
+
+// Applies one gate to a state of 2^n amplitudes at v (shared or global memory).
+__device__ __forceinline__ void apply_gate(float2* v, int n, const qsv_gate_rec& g) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int p0 = n - 1 - g.q0;
+  switch (g.kind) {
+    case G_DENSE1: {
+      const float2 m00 = make_float2(g.m[0], g.m[1]), m01 = make_float2(g.m[2], g.m[3]);
+      const float2 m10 = make_float2(g.m[4], g.m[5]), m11 = make_float2(g.m[6], g.m[7]);
+      const uint64_t pairs = 1ull << (n - 1), hi = 1ull << p0;
+      for (uint64_t k = tid; k < pairs; k += nt) {
+        const uint64_t i0 = ins0(k, p0);
+        const float2 x = v[i0], y = v[i0 + hi];
+        float2 o0 = make_float2(0.f, 0.f), o1 = o0;
+        o0 = qsv_cfma(m00, x, o0);
+        o0 = qsv_cfma(m01, y, o0);
+        o1 = qsv_cfma(m10, x, o1);
+        o1 = qsv_cfma(m11, y, o1);
+        v[i0] = o0;
+        v[i0 + hi] = o1;
+      }
+      break;
+    }
+    case G_PHASE1: {
+      const float2 ph = make_float2(g.m[0], g.m[1]);
+      const uint64_t cnt = 1ull << (n - 1), hi = 1ull << p0;
+      for (uint64_t k = tid; k < cnt; k += nt) {
+        const uint64_t i = ins0(k, p0) | hi;
+        v[i] = qsv_cmul(ph, v[i]);
+      }
+      break;
+    }
+    case G_X: {
+      const uint64_t pairs = 1ull << (n - 1), hi = 1ull << p0;
+      for (uint64_t k = tid; k < pairs; k += nt) {
+        const uint64_t i0 = ins0(k, p0);
+        const float2 x = v[i0];
+        v[i0] = v[i0 + hi];
+        v[i0 + hi] = x;
+      }
+      break;
+    }
+    case G_CX: {
+      const int pc = n - 1 - g.q1;
+      const int lo = min(p0, pc), hp = max(p0, pc);
+      const uint64_t cnt = 1ull << (n - 2), tb = 1ull << p0, cb = 1ull << pc;
+      for (uint64_t k = tid; k < cnt; k += nt) {
+        const uint64_t i0 = ins0(ins0(k, lo), hp) | cb;
+        const float2 x = v[i0];
+        v[i0] = v[i0 + tb];
+        v[i0 + tb] = x;
+      }
+      break;
+    }
+    case G_CSWAP: {
+      const int pc = n - 1 - g.q0, pa = n - 1 - g.q1, pb = n - 1 - g.q2;
+      int s0 = pc, s1 = pa, s2 = pb;  // sort ascending for zero insertion
+      if (s0 > s1) { const int t = s0; s0 = s1; s1 = t; }
+      if (s1 > s2) { const int t = s1; s1 = s2; s2 = t; }
+      if (s0 > s1) { const int t = s0; s0 = s1; s1 = t; }
+      const uint64_t cnt = 1ull << (n - 3);
+      for (uint64_t k = tid; k < cnt; k += nt) {
+        const uint64_t base = ins0(ins0(ins0(k, s0), s1), s2) | (1ull << pc);
+        const uint64_t ia = base | (1ull << pa), ib = base | (1ull << pb);
+        const float2 x = v[ia];
+        v[ia] = v[ib];
+        v[ib] = x;
+      }
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// Product state: amp[i] = prod_q feed_q[bit of qubit q in i].
+__device__ __forceinline__ void build_product(float2* v, int n, const float2* feed) {
+  const uint64_t total = 1ull << n;
+  for (uint64_t i = threadIdx.x; i < total; i += blockDim.x) {
+    float2 acc = make_float2(1.f, 0.f);
+    for (int q = 0; q < n; ++q) acc = qsv_cmul(acc, feed[2 * q + ((i >> (n - 1 - q)) & 1ull)]);
+    v[i] = acc;
+  }
+}
+
+__global__ void __launch_bounds__(CB_THREADS, 1)
+    k_circuits(const qsv_gate_rec* __restrict__ gates, const qsv_circuit_rec* __restrict__ circs, int ncirc,
+               float2* __restrict__ states, const float2* __restrict__ feeds, unsigned long long* __restrict__ times,
+               int* __restrict__ counter) {
+  extern __shared__ float2 sv[];
+  __shared__ int cur;
+  for (;;) {
+    if (threadIdx.x == 0) cur = atomicAdd(counter, 1);
+    __syncthreads();
+    const int c = cur;
+    __syncthreads();
+    if (c >= ncirc) break;
+    const qsv_circuit_rec cr = circs[c];
+    if (threadIdx.x == 0) times[2 * (size_t)c] = gtimer();
+    const qsv_gate_rec* gl = gates + cr.gate_offset;
+    float2* out = states + cr.state_offset;
+    const bool local = cr.n <= CB_SMEM_QUBITS;
+    float2* v = local ? sv : out;
+    build_product(v, cr.n, feeds + cr.feed_offset);
+    __syncthreads();
+    for (int k = 0; k < cr.ngates; ++k) {
+      const qsv_gate_rec g = gl[k];
+      apply_gate(v, cr.n, g);
+      __syncthreads();
+    }
+    if (local) {
+      const uint64_t total = 1ull << cr.n;
+      for (uint64_t i = threadIdx.x; i < total; i += blockDim.x) out[i] = sv[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      times[2 * (size_t)c + 1] = gtimer();
+    }
+  }
+}
+
+int capture(qsv_circuits* b, cudaStream_t stream) {
+  const size_t smem = sizeof(float2) << CB_SMEM_QUBITS;
+  cudaError_t e = cudaFuncSetAttribute(k_circuits, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return set_error(nullptr, QSV_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(e));
+  cudaGraph_t g = nullptr;
+  e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return set_error(nullptr, QSV_ERR_CUDA, "begin capture: %s", cudaGetErrorString(e));
+  cudaMemsetAsync(b->d_counter, 0, sizeof(int), stream);
+  const int grid = std::min(b->ncirc, std::max(1, b->sm_count));
+  k_circuits<<<grid, CB_THREADS, smem, stream>>>(b->d_gates, b->d_circs, b->ncirc, b->d_states, b->d_feeds,
+                                                 b->d_times, b->d_counter);
+  cudaError_t le = cudaGetLastError();
+  e = cudaStreamEndCapture(stream, &g);
+  if (le != cudaSuccess || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return set_error(nullptr, QSV_ERR_CUDA, "capture: %s", cudaGetErrorString(le != cudaSuccess ? le : e));
+  }
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return set_error(nullptr, QSV_ERR_CUDA, "instantiate: %s", cudaGetErrorString(e));
+  b->graph_stream = stream;
+  return QSV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qsv_circuits_create(const void* gates, int64_t ngates, const void* circuits, int ncirc, const void* feeds,
+                        int64_t nfeeds, qsv_circuits** out) {
+  if (!out || !gates || !circuits || !feeds || ncirc < 1 || ngates < 0 || nfeeds < 0)
+    return set_error(nullptr, QSV_ERR_INVALID, "bad circuit batch");
+  *out = nullptr;
+  const auto* gr = static_cast<const qsv_gate_rec*>(gates);
+  const auto* cr = static_cast<const qsv_circuit_rec*>(circuits);
+  size_t amps = 0;
+  for (int c = 0; c < ncirc; ++c) {
+    const qsv_circuit_rec& r = cr[c];
+    if (r.n < 3 || r.n > CB_MAX_QUBITS || r.ngates < 0 || r.gate_offset < 0 || r.gate_offset + r.ngates > ngates ||
+        r.feed_offset < 0 || r.feed_offset + 2 * r.n > nfeeds || r.state_offset < 0)
+      return set_error(nullptr, QSV_ERR_INVALID, "circuit %d: bad record (n=%d)", c, r.n);
+    amps = std::max(amps, (size_t)r.state_offset + ((size_t)1 << r.n));
+    for (int64_t k = r.gate_offset; k < r.gate_offset + r.ngates; ++k) {
+      const qsv_gate_rec& g = gr[k];
+      const int need = g.kind == G_CX ? 2 : (g.kind == G_CSWAP ? 3 : 1);
+      const int qs[3] = {g.q0, g.q1, g.q2};
+      if (g.kind < G_DENSE1 || g.kind > G_CSWAP)
+        return set_error(nullptr, QSV_ERR_INVALID, "circuit %d gate %lld: kind %d", c, (long long)k, g.kind);
+      for (int i = 0; i < need; ++i)
+        if (qs[i] < 0 || qs[i] >= r.n)
+          return set_error(nullptr, QSV_ERR_INVALID, "circuit %d gate %lld: qubit %d", c, (long long)k, qs[i]);
+      for (int i = 0; i < need; ++i)
+        for (int j = i + 1; j < need; ++j)
+          if (qs[i] == qs[j])
+            return set_error(nullptr, QSV_ERR_INVALID, "circuit %d gate %lld: repeated qubit", c, (long long)k);
+    }
+  }
+  auto* b = new (std::nothrow) qsv_circuits();
+  if (!b) return set_error(nullptr, QSV_ERR_OOM, "host allocation failed");
+  b->ncirc = ncirc;
+  b->state_amps = amps;
+  b->h_circs.assign(cr, cr + ncirc);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  bool ok = cudaMalloc(&b->d_gates, std::max<int64_t>(1, ngates) * sizeof(qsv_gate_rec)) == cudaSuccess &&
+            cudaMalloc(&b->d_circs, ncirc * sizeof(qsv_circuit_rec)) == cudaSuccess &&
+            cudaMalloc(&b->d_feeds, std::max<int64_t>(1, nfeeds) * sizeof(float2)) == cudaSuccess &&
+            cudaMalloc(&b->d_states, amps * sizeof(float2)) == cudaSuccess &&
+            cudaMalloc(&b->d_times, 2 * (size_t)ncirc * sizeof(unsigned long long)) == cudaSuccess &&
+            cudaMalloc(&b->d_counter, sizeof(int)) == cudaSuccess;
+  if (ok)
+    ok = cudaMemcpy(b->d_gates, gates, ngates * sizeof(qsv_gate_rec), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(b->d_circs, circuits, ncirc * sizeof(qsv_circuit_rec), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(b->d_feeds, feeds, nfeeds * sizeof(float2), cudaMemcpyHostToDevice) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    qsv_circuits_destroy(b);
+    return set_error(nullptr, QSV_ERR_OOM, "circuit batch allocation/upload failed");
+  }
+  *out = b;
+  return QSV_OK;
+}
+
+int qsv_circuits_run(qsv_circuits* b, void* stream) {
+  if (!b) return set_error(nullptr, QSV_ERR_INVALID, "null batch");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (b->graph && b->graph_stream != st) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  if (!b->graph) {
+    if (!st) return set_error(nullptr, QSV_ERR_INVALID, "a non-default stream is needed to capture the launch");
+    int rc = capture(b, st);
+    if (rc) return rc;
+  }
+  cudaError_t e = cudaGraphLaunch(b->graph, st);
+  if (e != cudaSuccess) return set_error(nullptr, QSV_ERR_CUDA, "graph launch: %s", cudaGetErrorString(e));
+  count_launch();
+  return QSV_OK;
+}
+
+int qsv_circuits_read(qsv_circuits* b, int circuit, void* host_out) {
+  if (!b || !host_out || circuit < 0 || circuit >= b->ncirc) return set_error(nullptr, QSV_ERR_INVALID, "bad read");
+  const qsv_circuit_rec& r = b->h_circs[(size_t)circuit];
+  cudaError_t e = cudaMemcpy(host_out, b->d_states + r.state_offset, (sizeof(float2) << r.n), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return set_error(nullptr, QSV_ERR_CUDA, "read: %s", cudaGetErrorString(e));
+  return QSV_OK;
+}
+
+int qsv_circuits_times(qsv_circuits* b, unsigned long long* host_out) {
+  if (!b || !host_out) return set_error(nullptr, QSV_ERR_INVALID, "bad read");
+  cudaError_t e = cudaMemcpy(host_out, b->d_times, 2 * (size_t)b->ncirc * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return set_error(nullptr, QSV_ERR_CUDA, "times: %s", cudaGetErrorString(e));
+  return QSV_OK;
+}
+
+int qsv_circuits_destroy(qsv_circuits* b) {
+  if (!b) return QSV_OK;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->d_gates);
+  cudaFree(b->d_circs);
+  cudaFree(b->d_feeds);
+  cudaFree(b->d_states);
+  cudaFree(b->d_times);
+  cudaFree(b->d_counter);
+  delete b;
+  return QSV_OK;
+}
+
+}  // extern "C"

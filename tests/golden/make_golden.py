@@ -286,6 +286,35 @@ def main():
     v0[0] = 1
     arrays["ansatz_n6"] = run_ref(circuits.ansatz_layers(6, 3, thetas), 6, v0)
     arrays["ansatz_n6_thetas"] = thetas
+    # Parameter-shift gradient of <sum Z> for the RY/RZ/CNOT-ring ansatz through the
+    # reference kernel (E(theta + pi/2) - E(theta - pi/2)) / 2 per angle.
+    def sumz(vec, nq):
+        idx = numpy.arange(2 ** nq)
+        w = nq - 2 * numpy.array([bin(i).count("1") for i in idx])
+        return float(numpy.sum(w * numpy.abs(vec) ** 2))
+
+    def energy(th, nq, layers):
+        v = numpy.zeros(2 ** nq, dtype=numpy.complex128)
+        v[0] = 1
+        return sumz(run_ref(circuits.ansatz_layers(nq, layers, th), nq, v), nq)
+
+    nq, layers = 6, 2
+    trng = numpy.random.default_rng(77)
+    thetas = trng.uniform(0, 2 * numpy.pi, (3, 2 * nq * layers))
+    energies, grads = [], []
+    for th in thetas:
+        energies.append(energy(th, nq, layers))
+        g = []
+        for j in range(th.size):
+            tp, tm = th.copy(), th.copy()
+            tp[j] += numpy.pi / 2
+            tm[j] -= numpy.pi / 2
+            g.append((energy(tp, nq, layers) - energy(tm, nq, layers)) / 2)
+        grads.append(g)
+    arrays["ansatz_ps_thetas"] = thetas
+    arrays["ansatz_ps_energies"] = numpy.array(energies)
+    arrays["ansatz_ps_grads"] = numpy.array(grads)
+    arrays["ansatz_ps_shape"] = numpy.array([nq, layers])
     numpy.savez_compressed(os.path.join(HERE, "workloads.npz"), **arrays)
     print("workloads written")
 

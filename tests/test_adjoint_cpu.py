@@ -1,0 +1,52 @@
+"""Adjoint-gradient host logic on CPU: the oracle's finite-difference gradient is pinned
+to the reference's parameter-shift gradient (tests/golden), and the ansatz gate list /
+per-gate matrices agree with the circuit generator."""
+import numpy
+import torch
+
+import statevector as sv
+from conftest import load_npz
+from qip_gb300 import adjoint, circuits
+
+
+def oracle_energy(th, n, layers):
+    v = numpy.zeros(2 ** n, dtype=complex)
+    v[0] = 1
+    for g in circuits.ansatz_layers(n, layers, th):
+        v = sv.kronselect_dot(g, v, n)
+    w = n - 2 * numpy.array([bin(i).count("1") for i in range(2 ** n)])
+    return float(numpy.sum(w * numpy.abs(v) ** 2))
+
+
+def test_oracle_gradients_match_reference_parameter_shift():
+    d = load_npz("workloads.npz")[0]
+    n, layers = (int(x) for x in d["ansatz_ps_shape"])
+    for th, e, g in zip(d["ansatz_ps_thetas"], d["ansatz_ps_energies"], d["ansatz_ps_grads"]):
+        assert abs(oracle_energy(th, n, layers) - e) < 1e-12
+        h = 1e-3
+        fd = []
+        for j in range(th.size):
+            tp, tm = th.copy(), th.copy()
+            tp[j] += h
+            tm[j] -= h
+            fd.append((oracle_energy(tp, n, layers) - oracle_energy(tm, n, layers)) / (2 * h))
+        numpy.testing.assert_allclose(fd, g, atol=1e-5)
+
+
+def test_ansatz_gate_list_matches_circuit_generator():
+    n, layers = 5, 2
+    a = adjoint.Ansatz(n, layers)
+    th = numpy.random.default_rng(0).uniform(0, 6, a.nparams)
+    U, Ud = adjoint.gate_matrices(a, torch.tensor(th[None, :]), torch.complex128)
+    dicts = circuits.ansatz_layers(n, layers, th)
+    assert len(dicts) == len(a.gates())
+    for g, (kind, tgt, ctl, pi) in enumerate(a.gates()):
+        (key, m), = dicts[g].items()
+        m2 = U[g, 0].numpy().reshape(2, 2)
+        if kind == adjoint.CNOT:
+            assert key == (ctl, tgt)
+            numpy.testing.assert_allclose(m.m, m2)
+        else:
+            assert key == (tgt,)
+            numpy.testing.assert_allclose(m, m2, atol=1e-15)
+        numpy.testing.assert_allclose(Ud[g, 0].numpy().reshape(2, 2), m2.conj().T, atol=1e-15)

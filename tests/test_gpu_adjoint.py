@@ -1,0 +1,49 @@
+"""Adjoint gradients on the GPU (batched kernels behind torch.autograd.Function) against
+the reference's parameter-shift gradient and the FP64 oracle's central differences."""
+import numpy
+import pytest
+import torch
+
+from conftest import load_npz
+from qip_gb300 import adjoint
+from test_adjoint_cpu import oracle_energy
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("statetype,atol", [(torch.complex128, 1e-10), (torch.complex64, 2e-5)])
+def test_adjoint_matches_reference_parameter_shift(statetype, atol):
+    d = load_npz("workloads.npz")[0]
+    n, layers = (int(x) for x in d["ansatz_ps_shape"])
+    th = torch.tensor(d["ansatz_ps_thetas"], device="cuda")
+    e, g = adjoint.energy_and_grad(th, adjoint.Ansatz(n, layers), statetype)
+    numpy.testing.assert_allclose(e.cpu().numpy(), d["ansatz_ps_energies"], atol=atol)
+    numpy.testing.assert_allclose(g.cpu().numpy(), d["ansatz_ps_grads"], atol=atol * 10)
+
+
+def test_adjoint_matches_oracle_finite_differences():
+    n, layers = 9, 3
+    a = adjoint.Ansatz(n, layers)
+    rng = numpy.random.default_rng(5)
+    th = rng.uniform(0, 2 * numpy.pi, (2, a.nparams))
+    e, g = adjoint.energy_and_grad(torch.tensor(th, device="cuda"), a, torch.complex128)
+    for b in range(2):
+        assert abs(e[b].item() - oracle_energy(th[b], n, layers)) < 1e-10
+        for j in rng.choice(a.nparams, 12, replace=False):
+            tp, tm = th[b].copy(), th[b].copy()
+            tp[j] += 1e-3
+            tm[j] -= 1e-3
+            fd = (oracle_energy(tp, n, layers) - oracle_energy(tm, n, layers)) / 2e-3
+            assert abs(g[b, j].item() - fd) < 1e-5
+
+
+def test_adjoint_upstream_gradient_and_batch_independence():
+    n, layers = 8, 2
+    a = adjoint.Ansatz(n, layers)
+    th = torch.tensor(numpy.random.default_rng(2).uniform(0, 6, (4, a.nparams)), device="cuda", requires_grad=True)
+    e = adjoint.SumZExpectation.apply(th, a, torch.complex128)
+    w = torch.tensor([1.0, -2.0, 0.5, 0.0], device="cuda", dtype=torch.float64)
+    (e * w).sum().backward()
+    e1, g1 = adjoint.energy_and_grad(th.detach()[1:2], a, torch.complex128)
+    numpy.testing.assert_allclose(th.grad[1].cpu().numpy(), -2.0 * g1[0].cpu().numpy(), atol=1e-11)
+    assert torch.all(th.grad[3] == 0)
