@@ -437,6 +437,240 @@ def run_reference(args):
     }), flush=True)
 
 
+# ---- supplementary workloads (one JSON line each; not the headline) -----------------------
+
+def _events():
+    import torch
+
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def run_qft16(args):
+    """QFT on n=16 qubits of a seeded N(0,1) state, complex128, through the graph API
+    run() (state in, full state and top-4-qubit distribution out), against the inverse
+    DFT (the QFT's known answer) and the reference's Cython kernel."""
+    import torch
+
+    from qip_gb300 import GpuBackend, QFFT, Qubit, StochasticMeasure, circuits, run
+
+    n = 16
+    rng = numpy.random.default_rng(2024)
+    x = rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)
+    x /= numpy.linalg.norm(x)
+    q = Qubit(n=n)
+    out = QFFT(q)
+    top = out.split([4])
+    sm = StochasticMeasure(top[0])
+    want = numpy.fft.ifft(x, norm="ortho")
+    i = numpy.arange(2 ** n)
+    outcome = sum(((i >> (n - 1 - j)) & 1) << j for j in range(4))  # bit j <-> qubit j
+    want_p = numpy.bincount(outcome, weights=numpy.abs(want) ** 2, minlength=16)
+    amp = circuits.gate_amp_updates(circuits.qft_gates(n), n)
+    for _ in range(args.warmup):
+        run(sm, top[1], feed={q: x}, backend_constructor=GpuBackend.make_state)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o, classic = run(sm, top[1], feed={q: x}, backend_constructor=GpuBackend.make_state)
+    dt = (time.perf_counter() - t0) / args.steps
+    err = float(numpy.max(numpy.abs(o - want)))
+    perr = float(numpy.max(numpy.abs(classic[sm] - want_p)))
+    res = {"metric": "amp-updates/s (QFT n=16 complex128 through run(), e2e)", "value": amp / dt,
+           "unit": "amp-updates/s", "ms_per_run": dt * 1e3, "steps": args.steps, "dtype": "c128",
+           "config": {"workload": "QFT n=16 on a seeded N(0,1) state + distribution of the top 4 qubits"},
+           "max_abs_err_vs_inverse_dft": err, "max_abs_err_top4_probs": perr}
+    kp = load_reference_kernels()
+    if kp is not None:
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+        gl = circuits.qft_gates(n)
+        packed = [ref_pack(g) for g in gl]
+        vec = x.astype(numpy.complex128).copy()
+        o2 = numpy.zeros_like(vec)
+        t0 = time.perf_counter()
+        for ci, cm in packed:
+            kp.cdot_loop(ci, cm, vec, n, o2)
+            vec, o2 = o2, vec
+        rt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"kind": "reference", "value": amp / rt, "unit": "amp-updates/s",
+                               "cores": int(os.environ["OMP_NUM_THREADS"]),
+                               "sample": f"the full QFT gate list through the reference cdot_loop ({rt:.2f} s)",
+                               "max_abs_diff_vs_ours": float(numpy.max(numpy.abs(vec - o)))}
+    print(json.dumps(res), flush=True)
+
+
+def run_hbm(args):
+    """QFT + 8 amplitude-amplification iterations at n=32 complex64 (fused) and n=31
+    complex128 (per-gate); all single-qubit marginals; per-pass achieved GB/s.  Checked
+    against Grover's closed form (the QFT of |0...0> is the uniform state)."""
+    import torch
+
+    from qip_gb300 import GpuBackend, _native as nat, circuits, fusion, gates as gmod
+
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    peak, peak_src = read_peaks()
+    out = {"metric": "achieved HBM GB/s per pass and amp-updates/s (QFT + 8 Grover iterations)",
+           "unit": "GB/s", "peak": peak, "peak_source": peak_src, "runs": []}
+    for n, dt, fusion_on in ((args.hbm_n64, numpy.complex64, True), (args.hbm_n128, numpy.complex128, False)):
+        gl, marked = circuits.grover_gates(n, 8, seed=7)
+        amp = circuits.gate_amp_updates(gl, n)
+        ops = [op for g in gl for op in gmod.decompose(g)]
+        st = GpuBackend.make_state(n, [], [], statetype=dt, fusion=fusion_on)
+        st.set_stream(stream.cuda_stream)
+        size = 8 if dt == numpy.complex64 else 16
+        per_kind = {}
+        e0, e1 = _events()
+        if fusion_on:
+            steps = fusion.plan(ops, kmax=6)
+        else:
+            steps = ops
+        t_all0, t_all1 = _events()
+        t_all0.record(stream)
+        for stp in steps:
+            a, b = _events()
+            a.record(stream)
+            if isinstance(stp, fusion.Block) and len(stp.qubits) >= 4:
+                st.apply_blocks([stp])
+                kind, touched = "fused_block", 2 ** n
+            elif isinstance(stp, fusion.Block):
+                for op in gmod.classify_matrix(stp.qubits, (), stp.matrix):
+                    st.apply_op(op)
+                kind, touched = "small_block", 2 ** n
+            else:
+                st.apply_op(stp)
+                kind = f"{stp.kind}{len(stp.targets)}c{len(stp.controls)}"
+                touched = 2 ** (n - len(stp.controls)) if stp.kind != "diag" else 2 ** (n - len(stp.controls) - len(stp.targets))
+            b.record(stream)
+            per_kind.setdefault(kind, []).append((a, b, touched))
+        t_all1.record(stream)
+        t_all1.synchronize()
+        total_s = t_all0.elapsed_time(t_all1) * 1e-3
+        kinds = {}
+        for k, lst in per_kind.items():
+            ms = [a.elapsed_time(b) for a, b, _ in lst]
+            byt = sum(2 * t * size for _, _, t in lst)
+            kinds[k] = {"passes": len(lst), "mean_ms": statistics.mean(ms),
+                        "GB_s": byt / (sum(ms) * 1e-3) / 1e9}
+        marg, nrm = st.qubit_marginals()
+        N = 2.0 ** n
+        th = numpy.arcsin(1 / numpy.sqrt(N))
+        pm = numpy.sin(17 * th) ** 2
+        pu = (1 - pm) / (N - 1)
+        bits = numpy.array([(marked >> (n - 1 - q)) & 1 for q in range(n)])
+        want = pm * bits + pu * (N / 2 - bits)
+        amp_m = st.get_relative_range(marked, marked + 1)[0]
+        st.close()
+        out["runs"].append({
+            "n": n, "dtype": "c64" if dt == numpy.complex64 else "c128", "fused": fusion_on,
+            "gates": len(gl), "passes": len(steps), "seconds": total_s, "amp_updates_per_s": amp / total_s,
+            "per_pass": kinds, "max_abs_err_marginals": float(numpy.max(numpy.abs(marg - want))),
+            "norm2": nrm, "marked_prob": float(abs(amp_m) ** 2), "marked_prob_expected": float(pm)})
+        torch.cuda.synchronize()
+    fb = out["runs"][0]["per_pass"].get("fused_block")
+    out["value"] = fb["GB_s"] if fb else None
+    out["frac"] = out["value"] / peak if fb else None
+    print(json.dumps(out), flush=True)
+
+
+def run_batched(args):
+    """4096 independent circuits (n ~ U[8,20], depth ~ U[20,100]) in one persistent launch,
+    replayed from a CUDA graph: circuits/s and per-circuit latency percentiles."""
+    import torch
+
+    from qip_gb300 import batch, circuits
+
+    circs, feeds, sizes = batch.random_batch(args.batch_count, seed=4096)
+    b = batch.CircuitBatch(circs, feeds, sizes)
+    stream = torch.cuda.Stream()
+    for _ in range(args.warmup):
+        b.run(stream.cuda_stream)
+    stream.synchronize()
+    e0, e1 = _events()
+    e0.record(stream)
+    for _ in range(args.steps):
+        b.run(stream.cuda_stream)
+    e1.record(stream)
+    e1.synchronize()
+    dt = e0.elapsed_time(e1) * 1e-3 / args.steps
+    lat = b.latencies_ns() / 1e6
+    res = {"metric": "circuits/s (batched uneven circuits, one persistent launch)", "value": args.batch_count / dt,
+           "unit": "circuits/s", "ms_per_step": dt * 1e3, "steps": args.steps, "dtype": "c64",
+           "config": {"workload": f"{args.batch_count} circuits, n~U[8,20], depth~U[20,100], "
+                                  "gates H/X/Rm/CNOT/C(Swap)/Haar, random product feeds"},
+           "latency_ms": {"p50": float(numpy.percentile(lat, 50)), "p99": float(numpy.percentile(lat, 99)),
+                          "max": float(lat.max())}}
+    b.close()
+    kp = load_reference_kernels()
+    if kp is not None:
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+        t0 = time.perf_counter()
+        done = 0
+        for gl, f, n in zip(circs, feeds, sizes):
+            st = numpy.ones(1, dtype=numpy.complex128)
+            for v in f:
+                st = numpy.kron(st, v)
+            o2 = numpy.zeros_like(st)
+            for g in gl:
+                ci, cm = ref_pack(g)
+                kp.cdot_loop(ci, cm, st, n, o2)
+                st, o2 = o2, st
+            done += 1
+            if time.perf_counter() - t0 > args.cpu_seconds:
+                break
+        rt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"kind": "reference", "value": done / rt, "unit": "circuits/s",
+                               "cores": int(os.environ["OMP_NUM_THREADS"]),
+                               "sample": f"first {done} circuits of the same list through the reference cdot_loop"}
+    print(json.dumps(res), flush=True)
+
+
+def run_adjoint(args):
+    """Adjoint gradients: n=24, 20 layers of RY/RZ on every qubit + CNOT ring (960 angles),
+    objective <sum Z>, batch of 64 parameter sets, complex64."""
+    import torch
+
+    from qip_gb300 import adjoint
+
+    n, L, B = args.adj_n, args.adj_layers, args.adj_batch
+    a = adjoint.Ansatz(n, L)
+    th = torch.tensor(numpy.random.default_rng(2025).uniform(0, 2 * numpy.pi, (B, a.nparams)), device="cuda")
+    fwd, bwd = [], []
+    for rep in range(args.warmup + args.steps):
+        thr = th.clone().requires_grad_(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e = adjoint.SumZExpectation.apply(thr, a, torch.complex64)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        e.sum().backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        if rep >= args.warmup:
+            fwd.append(t1 - t0)
+            bwd.append(t2 - t1)
+    g = thr.grad
+    tf, tb = statistics.mean(fwd), statistics.mean(bwd)
+    # Spot check against complex128 central differences (h=1e-3) on a few angles.
+    checks = []
+    for j in (0, a.nparams // 2, a.nparams - 1):
+        tp, tm = th[:1].clone(), th[:1].clone()
+        tp[0, j] += 1e-3
+        tm[0, j] -= 1e-3
+        with torch.no_grad():
+            ep = adjoint.SumZExpectation.apply(tp, a, torch.complex128)
+            em = adjoint.SumZExpectation.apply(tm, a, torch.complex128)
+        fd = float((ep - em).item() / 2e-3)
+        checks.append(abs(fd - float(g[0, j].item())))
+    print(json.dumps({
+        "metric": "gradient vectors/s (adjoint method, batch of parameter sets)", "value": B / (tf + tb),
+        "unit": "gradients/s", "dtype": "c64", "steps": args.steps,
+        "config": {"workload": f"ansatz n={n}, {L} layers RY/RZ + CNOT ring, {a.nparams} angles, batch {B}, "
+                               "objective <sum Z>"},
+        "forward_s": tf, "backward_s": tb, "backward_over_forward": tb / tf,
+        "grad_components_per_s": B * a.nparams / (tf + tb),
+        "max_abs_err_vs_fd_c128": max(checks)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -450,11 +684,20 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--parts", default="fused,plain,e2e,cpu",
                     help="comma list of fused,plain,e2e,cpu (profiling runs use fused only)")
+    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "qft16", "hbm", "batched", "adjoint"])
+    ap.add_argument("--hbm-n64", type=int, default=32)
+    ap.add_argument("--hbm-n128", type=int, default=31)
+    ap.add_argument("--batch-count", type=int, default=4096)
+    ap.add_argument("--adj-n", type=int, default=24)
+    ap.add_argument("--adj-layers", type=int, default=20)
+    ap.add_argument("--adj-batch", type=int, default=64)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
-    else:
+    elif args.workload == "brickwork":
         run_ours(args)
+    else:
+        {"qft16": run_qft16, "hbm": run_hbm, "batched": run_batched, "adjoint": run_adjoint}[args.workload](args)
 
 
 if __name__ == "__main__":

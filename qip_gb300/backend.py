@@ -20,7 +20,7 @@ from typing import Callable, List, Mapping, Optional, Sequence, Tuple, Union
 import numpy
 
 from . import _native as nat
-from .fusion import Block, plan
+from .fusion import Block, plan, plan_prefix
 from .gates import GateOp, classify_matrix, decompose
 from .util import InitialState, IndexType, MatrixType
 
@@ -145,6 +145,9 @@ class GpuBackend(StateType):
     """
 
     FLUSH_LIMIT = 8192
+    # Queued gates beyond this are planned incrementally: blocks that no later gate can
+    # join are launched while the executor keeps feeding gates.
+    PARTIAL_FLUSH = 384
 
     def __init__(self, n: int, handle: ctypes.c_void_p, statetype, fusion: bool, max_block: int = 6):
         super().__init__(n, None)
@@ -154,6 +157,7 @@ class GpuBackend(StateType):
         self.fusion = bool(fusion)
         self.max_block = int(max_block)
         self._pending: List[GateOp] = []
+        self._next_partial = self.PARTIAL_FLUSH
         self.stats = {"ops": 0, "blocks": 0, "block_gates": 0, "launch_calls": 0}
 
     # ---- construction ---------------------------------------------------------------
@@ -231,9 +235,22 @@ class GpuBackend(StateType):
             self._pending.extend(ops)
             if len(self._pending) >= self.FLUSH_LIMIT:
                 self.flush()
+            elif len(self._pending) >= self._next_partial:
+                self._partial_flush()
         else:
             for op in ops:
                 self.apply_op(op)
+
+    def _kmax(self) -> int:
+        return min(self.max_block, max(1, self.n - 7)) if self.n >= 11 else 3
+
+    def _partial_flush(self) -> None:
+        steps, rest = plan_prefix(self._pending, kmax=self._kmax(), nqubits=self.n)
+        if steps:
+            self._pending = rest
+            self.run_plan(steps)
+        # Retry once a further chunk of gates has arrived (keeps planning linear).
+        self._next_partial = len(self._pending) + self.PARTIAL_FLUSH // 3
 
     def apply_ops(self, ops: Sequence[GateOp]) -> None:
         """Queue (fusion) or launch (per-gate) pre-decomposed operations."""
@@ -304,8 +321,7 @@ class GpuBackend(StateType):
         if not self._pending:
             return
         pending, self._pending = self._pending, []
-        kmax = min(self.max_block, max(1, self.n - 7)) if self.n >= 11 else 3
-        self.run_plan(plan(pending, kmax=kmax))
+        self.run_plan(plan(pending, kmax=self._kmax()))
 
     # ---- readout -------------------------------------------------------------------------
     def get_state(self) -> numpy.ndarray:

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <mutex>
+#include <thread>
 #include <new>
 #include <vector>
 
@@ -905,6 +906,53 @@ int launch_probs(qsv_state* s, int m, const int* pos_in_order, double* d_out_or_
 
 }  // namespace
 
+namespace {
+constexpr size_t kStageMinBytes = size_t(32) << 20;  // reads below this go straight to the caller
+constexpr size_t kStageChunk = size_t(64) << 20;     // two pinned halves of this size per handle
+
+// memcpy split over a few host threads (host memory bandwidth needs several cores).
+void parallel_copy(char* dst, const char* src, size_t len) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const unsigned nt = std::min<unsigned>(16, hw);
+  if (nt <= 1 || len < (size_t(4) << 20)) {
+    memcpy(dst, src, len);
+    return;
+  }
+  std::vector<std::thread> pool;
+  const size_t slice = (len + nt - 1) / nt;
+  for (unsigned t = 1; t < nt; ++t) {
+    const size_t off = t * slice;
+    if (off >= len) break;
+    pool.emplace_back([=] { memcpy(dst + off, src + off, std::min(slice, len - off)); });
+  }
+  memcpy(dst, src, std::min(slice, len));
+  for (auto& th : pool) th.join();
+}
+
+// Writes one byte per 4 KiB page of [p, p+len) from several threads so the kernel maps
+// the pages in parallel; the bytes are overwritten by the copy that follows.
+void parallel_touch(char* p, size_t len) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const unsigned nt = std::min<unsigned>(16, hw);
+  auto touch = [](char* a, size_t n) {
+    for (size_t i = 0; i < n; i += 4096) reinterpret_cast<volatile char*>(a)[i] = 0;
+  };
+  if (nt <= 1) {
+    touch(p, len);
+    return;
+  }
+  std::vector<std::thread> pool;
+  const size_t slice = ((len + nt - 1) / nt + 4095) & ~size_t(4095);
+  for (unsigned t = 1; t < nt; ++t) {
+    const size_t off = t * slice;
+    if (off >= len) break;
+    pool.emplace_back([=] { touch(p + off, std::min(slice, len - off)); });
+  }
+  touch(p, std::min(slice, len));
+  for (auto& th : pool) th.join();
+}
+}  // namespace
+
 // ======================================================================================
 // C ABI
 // ======================================================================================
@@ -974,9 +1022,11 @@ int qsv_destroy(qsv_state* s) {
   if (s->d_flag) cudaFree(s->d_flag);
   if (s->d_scratch) cudaFree(s->d_scratch);
   if (s->d_images) cudaFree(s->d_images);
-  if (s->h_images) cudaFreeHost(s->h_images);
+  for (int i = 0; i < qsv_state::kImageSlots; ++i) {
+    if (s->h_img[i]) cudaFreeHost(s->h_img[i]);
+    if (s->img_ev[i]) cudaEventDestroy(s->img_ev[i]);
+  }
   if (s->h_stage) cudaFreeHost(s->h_stage);
-  if (s->images_done) cudaEventDestroy(s->images_done);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
   delete s;
   return QSV_OK;
@@ -1076,10 +1126,56 @@ int qsv_read_range(qsv_state* s, void* host, uint64_t start, uint64_t count) {
   if (start + count > (1ull << s->n) || (count && !host))
     return set_error(s, QSV_ERR_INVALID, "range outside the state");
   if (!count) return QSV_OK;
-  QSV_CUDA(s, cudaMemcpyAsync(host, (const char*)s->d_amp + start * s->amp_bytes, count * s->amp_bytes,
-                              cudaMemcpyDeviceToHost, s->stream));
-  QSV_CUDA(s, cudaStreamSynchronize(s->stream));
-  return QSV_OK;
+  const size_t bytes = count * s->amp_bytes;
+  const char* src = (const char*)s->d_amp + start * s->amp_bytes;
+  if (bytes < kStageMinBytes) {
+    QSV_CUDA(s, cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, s->stream));
+    QSV_CUDA(s, cudaStreamSynchronize(s->stream));
+    return QSV_OK;
+  }
+  // Large reads: DMA into two pinned staging halves while host threads copy the
+  // previous chunk into the (pageable) destination.
+  if (!s->h_stage) {
+    if (cudaMallocHost(&s->h_stage, 2 * kStageChunk) != cudaSuccess) {
+      cudaGetLastError();
+      s->h_stage = nullptr;
+      QSV_CUDA(s, cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, s->stream));
+      QSV_CUDA(s, cudaStreamSynchronize(s->stream));
+      return QSV_OK;
+    }
+    s->h_stage_bytes = 2 * kStageChunk;
+  }
+  cudaEvent_t ev[2];
+  QSV_CUDA(s, cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+  QSV_CUDA(s, cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
+  char* dst = static_cast<char*>(host);
+  // Fault in the destination's pages from several threads while queued kernels still
+  // run (first touch of fresh host memory costs about as much as the copy itself).
+  parallel_touch(dst, bytes);
+  char* stage = static_cast<char*>(s->h_stage);
+  const size_t nchunks = (bytes + kStageChunk - 1) / kStageChunk;
+  int rc = QSV_OK;
+  for (size_t i = 0; i <= nchunks && rc == QSV_OK; ++i) {
+    if (i < nchunks) {
+      const size_t off = i * kStageChunk, len = std::min(kStageChunk, bytes - off);
+      cudaError_t e = cudaMemcpyAsync(stage + (i & 1) * kStageChunk, src + off, len, cudaMemcpyDeviceToHost, s->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[i & 1], s->stream);
+      if (e != cudaSuccess) rc = set_error(s, QSV_ERR_CUDA, "staged read: %s", cudaGetErrorString(e));
+    }
+    if (i > 0 && rc == QSV_OK) {
+      const size_t j = i - 1, off = j * kStageChunk, len = std::min(kStageChunk, bytes - off);
+      cudaError_t e = cudaEventSynchronize(ev[j & 1]);
+      if (e != cudaSuccess) {
+        rc = set_error(s, QSV_ERR_CUDA, "staged read: %s", cudaGetErrorString(e));
+        break;
+      }
+      parallel_copy(dst + off, stage + (j & 1) * kStageChunk, len);
+    }
+  }
+  if (rc) cudaStreamSynchronize(s->stream);
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  return rc;
 }
 
 int qsv_apply_matrix(qsv_state* s, int k, const int* targets, int ncontrols, const int* controls,

@@ -74,6 +74,7 @@ struct BlockArgs {
   uint64_t ntiles;
   int k;
   int staged;           // 1: address-order staging (targets in the low 7 bits), 0: direct
+  int vec2;             // direct: target combinations t, t^1 are adjacent amplitudes (16-byte pairs)
   int ptile[16];        // the 7+k tile positions, ascending (zero insertion -> tile base)
   uint16_t eb[FB_M];    // e of group b
   uint16_t et[64];      // e of target combination t (targets[0] = MSB of t)
@@ -294,6 +295,20 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         const int e = 2 * (u * FB_THREADS + tid);
         buf[u] = __ldcs(reinterpret_cast<const float4*>(psi + base + dep(e)));
       }
+    } else if (a.vec2) {
+#pragma unroll
+      for (int it = 0; it < P::ITEMS; ++it) {
+        const int item = it * FB_THREADS + tid;
+        const int b = item & (FB_M - 1);
+        const int tg = item >> FB_BATCH_BITS;
+        const uint64_t rb = base + dep(eb[b]);
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {
+          const float4 v = __ldcs(reinterpret_cast<const float4*>(psi + rb + dep(et[tg * 8 + j])));
+          buf2[it][j] = make_float2(v.x, v.y);
+          buf2[it][j + 1] = make_float2(v.z, v.w);
+        }
+      }
     } else {
 #pragma unroll
       for (int it = 0; it < P::ITEMS; ++it) {
@@ -401,6 +416,12 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         if constexpr (STAGED) {
 #pragma unroll
           for (int j = 0; j < CH; ++j) raw[slot(eb_ | et[t0 + j])] = make_float2(re[j], im[j]);
+        } else if (a.vec2) {
+          const uint64_t rb = base + dep(eb_);
+#pragma unroll
+          for (int j = 0; j < CH; j += 2)
+            __stcs(reinterpret_cast<float4*>(psi + rb + dep(et[t0 + j])),
+                   make_float4(re[j], im[j], re[j + 1], im[j + 1]));
         } else {
           const uint64_t rb = base + dep(eb_);
 #pragma unroll
@@ -493,6 +514,8 @@ void tile_geometry(int k, const int* tpos, BlockArgs& a) {
   for (int j = 0; j < k; ++j) tmask |= 1ull << tpos[j];
   // Direct loads/stores stay coalesced while few targets sit in the 7 lowest bits.
   a.staged = __builtin_popcountll(tmask & 0x7Full) >= 3 ? 1 : 0;
+  // t's least significant bit is tpos[k-1]; at address bit 0, t and t^1 are adjacent.
+  a.vec2 = tpos[k - 1] == 0 ? 1 : 0;
   int batch[FB_BATCH_BITS];
   for (int p = 0, nb = 0; nb < FB_BATCH_BITS; ++p)
     if (!((tmask >> p) & 1ull)) batch[nb++] = p;
@@ -713,40 +736,42 @@ extern "C" int qsv_apply_blocks(qsv_state* s, int nblocks, const int* ks, const 
   size_t total = 0;
   int rc = prepare_blocks(s, nblocks, ks, targets_flat, args, img_off, mat_offs, total);
   if (rc) return rc;
-  // Pinned host staging: wait until the previous upload from it has completed.
-  if (s->images_in_flight) {
-    QSV_CUDA(s, cudaEventSynchronize(s->images_done));
-    s->images_in_flight = false;
+  // Pinned staging slot from the ring: wait only if this slot's last upload is pending.
+  const int slot = s->img_next;
+  s->img_next = (slot + 1) % qsv_state::kImageSlots;
+  if (!s->img_ev[slot]) QSV_CUDA(s, cudaEventCreateWithFlags(&s->img_ev[slot], cudaEventDisableTiming));
+  if (s->img_busy[slot]) {
+    QSV_CUDA(s, cudaEventSynchronize(s->img_ev[slot]));
+    s->img_busy[slot] = false;
   }
-  if (s->h_images_bytes < total) {
-    if (s->h_images) cudaFreeHost(s->h_images);
-    s->h_images = nullptr;
-    s->h_images_bytes = 0;
+  if (s->h_img_bytes[slot] < total) {
+    if (s->h_img[slot]) cudaFreeHost(s->h_img[slot]);
+    s->h_img[slot] = nullptr;
+    s->h_img_bytes[slot] = 0;
     const size_t want = std::max(total, size_t(1) << 20);
-    if (cudaMallocHost(&s->h_images, want) != cudaSuccess) {
+    if (cudaMallocHost(&s->h_img[slot], want) != cudaSuccess) {
       cudaGetLastError();
       return set_error(s, QSV_ERR_OOM, "pinned staging allocation failed");
     }
-    s->h_images_bytes = want;
+    s->h_img_bytes[slot] = want;
   }
   if (s->d_images_bytes < total) {
     QSV_CUDA(s, cudaStreamSynchronize(s->stream));  // old images may still be in use
     if (s->d_images) cudaFree(s->d_images);
     s->d_images = nullptr;
     s->d_images_bytes = 0;
-    const size_t want = std::max(total, size_t(1) << 20);
+    const size_t want = std::max(total, size_t(4) << 20);
     if (cudaMalloc(&s->d_images, want) != cudaSuccess) {
       cudaGetLastError();
       return set_error(s, QSV_ERR_OOM, "device image allocation failed");
     }
     s->d_images_bytes = want;
   }
-  if (!s->images_done) QSV_CUDA(s, cudaEventCreateWithFlags(&s->images_done, cudaEventDisableTiming));
-  for (int i = 0; i < nblocks; ++i)
-    build_image(ks[i], mats_c128 + mat_offs[(size_t)i], (uint8_t*)s->h_images + img_off[(size_t)i]);
-  QSV_CUDA(s, cudaMemcpyAsync(s->d_images, s->h_images, total, cudaMemcpyHostToDevice, s->stream));
-  QSV_CUDA(s, cudaEventRecord(s->images_done, s->stream));
-  s->images_in_flight = true;
+  uint8_t* himg = static_cast<uint8_t*>(s->h_img[slot]);
+  for (int i = 0; i < nblocks; ++i) build_image(ks[i], mats_c128 + mat_offs[(size_t)i], himg + img_off[(size_t)i]);
+  QSV_CUDA(s, cudaMemcpyAsync(s->d_images, himg, total, cudaMemcpyHostToDevice, s->stream));
+  QSV_CUDA(s, cudaEventRecord(s->img_ev[slot], s->stream));
+  s->img_busy[slot] = true;
   for (int i = 0; i < nblocks; ++i) {
     BlockArgs& a = args[(size_t)i];
     a.wimg = reinterpret_cast<const uint4*>((const uint8_t*)s->d_images + img_off[(size_t)i]);

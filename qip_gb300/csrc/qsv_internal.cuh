@@ -31,13 +31,17 @@ struct qsv_state {
   size_t scratch_bytes = 0;
   // Device status word written by kernels with bounded waits.
   int* d_flag = nullptr;
-  // Fused-block matrix images: pinned host staging + device copy.
-  void* h_images = nullptr;
-  size_t h_images_bytes = 0;
+  // Fused-block matrix images: a ring of pinned host staging slots (a slot is reused
+  // only after its upload completed, so the host rarely waits for queued kernels) and
+  // one device buffer (stream order keeps uploads behind the kernels reading it).
+  static constexpr int kImageSlots = 32;
+  void* h_img[kImageSlots] = {nullptr};
+  size_t h_img_bytes[kImageSlots] = {0};
+  cudaEvent_t img_ev[kImageSlots] = {nullptr};
+  bool img_busy[kImageSlots] = {false};
+  int img_next = 0;
   void* d_images = nullptr;
   size_t d_images_bytes = 0;
-  cudaEvent_t images_done = nullptr;
-  bool images_in_flight = false;
   // Pinned staging for host <-> device range copies.
   void* h_stage = nullptr;
   size_t h_stage_bytes = 0;

@@ -57,8 +57,28 @@ def block_matrix(gates: Sequence[GateOp]) -> Tuple[Tuple[int, ...], numpy.ndarra
     return qs, U
 
 
+def _emit(chosen: List[GateOp]) -> Step:
+    if len(chosen) == 1:
+        return chosen[0]
+    qs, U = block_matrix(chosen)
+    return Block(qs, U, len(chosen), sum(g.amp_update_weight() for g in chosen))
+
+
 def plan(gates: Sequence[GateOp], kmax: int = 6) -> List[Step]:
     """Group ``gates`` (program order) into fused blocks and standalone gates."""
+    steps, rest = plan_prefix(gates, kmax, nqubits=None)
+    assert not rest
+    return steps
+
+
+def plan_prefix(gates: Sequence[GateOp], kmax: int = 6, nqubits=None) -> Tuple[List[Step], List[GateOp]]:
+    """Greedy plan of ``gates``.  With ``nqubits`` given, stop at the first block that
+    later gates could still join and return (steps so far, gates not yet planned): a
+    block is final once it is full (kmax qubits, or every qubit of the register) and
+    each of its qubits is blocked by a gate left out of it.  The steps returned are
+    exactly the first steps of ``plan`` over any extension of ``gates``, so a caller
+    can launch them while gates keep arriving.  With ``nqubits=None`` plans
+    everything."""
     remaining = list(gates)
     steps: List[Step] = []
     while remaining:
@@ -84,10 +104,10 @@ def plan(gates: Sequence[GateOp], kmax: int = 6) -> List[Step]:
             else:
                 blocked |= q
                 rest.append(g)
+        if nqubits is not None:
+            full = len(S) == kmax or len(S) == nqubits
+            if not (full and S <= blocked):
+                return steps, remaining
         remaining = rest
-        if len(chosen) == 1:
-            steps.append(chosen[0])
-            continue
-        qs, U = block_matrix(chosen)
-        steps.append(Block(qs, U, len(chosen), sum(g.amp_update_weight() for g in chosen)))
-    return steps
+        steps.append(_emit(chosen))
+    return steps, []

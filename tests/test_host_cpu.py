@@ -166,3 +166,25 @@ def test_fusion_keeps_wide_gates_standalone():
     steps = fusion.plan(ops, kmax=6)
     wide = [s for s in steps if not isinstance(s, fusion.Block) and s.width > 6]
     assert len(wide) == 2  # the two (n-1)-controlled Z gates
+
+
+def test_incremental_plan_equals_full_plan():
+    n = 14
+    gl = circuits.brickwork(n, 10, seed=4) + circuits.grover_gates(n, 1, seed=2)[0] + circuits.brickwork(n, 3, seed=5)
+    ops = [op for g in gl for op in gates.decompose(g)]
+    full = fusion.plan(ops, kmax=6)
+    got, pending = [], []
+    for i, op in enumerate(ops):
+        pending.append(op)
+        if len(pending) >= 50 and i % 7 == 0:
+            steps, pending = fusion.plan_prefix(pending, kmax=6, nqubits=n)
+            got.extend(steps)
+    got.extend(fusion.plan(pending, kmax=6))
+    assert len(got) == len(full)
+    for a, b in zip(got, full):
+        assert type(a) is type(b)
+        if isinstance(a, fusion.Block):
+            assert a.qubits == b.qubits and a.ngates == b.ngates
+            numpy.testing.assert_allclose(a.matrix, b.matrix, atol=1e-13)
+        else:
+            assert a is b
