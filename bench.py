@@ -671,6 +671,50 @@ def run_adjoint(args):
         "max_abs_err_vs_fd_c128": max(checks)}), flush=True)
 
 
+def run_block_placements(args):
+    """One fused k-qubit block per target placement (high bits, low bits, mixed), timed
+    with CUDA events: the fused kernel's achieved HBM bandwidth by placement."""
+    import torch
+
+    from qip_gb300 import GpuBackend, _native as nat
+
+    n = args.n
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    st = GpuBackend.make_state(n, [], [], statetype=numpy.complex64, fusion=True)
+    st.set_stream(stream.cuda_stream)
+    lib = nat.load()
+    rng = numpy.random.default_rng(3)
+    k = args.kmax
+    bits_list = [list(range(n - k, n)), list(range(k)), [0, 1] + list(range(n - k + 2, n)),
+                 [0, 1, 2, 3] + list(range(n - k + 4, n)), [1, 2, 3] + list(range(n - k + 3, n)),
+                 [0, 2, 4, 6, 8, 10][:k], sorted(int(x) for x in rng.choice(n, k, replace=False))]
+    peak, _ = read_peaks()
+    rows = []
+    for bits in bits_list:
+        tg = [n - 1 - b for b in bits]  # qubit indices
+        u = numpy.linalg.qr(rng.standard_normal((2 ** k, 2 ** k)) + 1j * rng.standard_normal((2 ** k, 2 ** k)))[0]
+        ks, tgt = nat.int_array([k]), nat.int_array(sorted(tg))
+        mats = numpy.ascontiguousarray(u.astype(numpy.complex128)).view(numpy.float64)
+        p = ctypes.c_void_p()
+        nat.check(lib.qsv_plan_create(st.handle, 1, nat.ip(ks), nat.ip(tgt), nat.dp(mats), ctypes.byref(p)), st.handle)
+        for _ in range(args.warmup):
+            nat.check(lib.qsv_plan_launch(st.handle, p, 0, 1), st.handle)
+        e0, e1 = _events()
+        e0.record(stream)
+        for _ in range(args.steps):
+            nat.check(lib.qsv_plan_launch(st.handle, p, 0, 1), st.handle)
+        e1.record(stream)
+        e1.synchronize()
+        lib.qsv_plan_destroy(p)
+        ms = e0.elapsed_time(e1) / args.steps
+        gbs = 2 * (2 ** n) * 8 / (ms * 1e-3) / 1e9
+        rows.append({"target_bits": bits, "ms": ms, "GB_s": gbs, "frac": gbs / peak})
+    st.close()
+    print(json.dumps({"metric": "fused block kernel GB/s by target placement", "unit": "GB/s", "n": n, "k": k,
+                      "placements": rows}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -684,7 +728,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--parts", default="fused,plain,e2e,cpu",
                     help="comma list of fused,plain,e2e,cpu (profiling runs use fused only)")
-    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "qft16", "hbm", "batched", "adjoint"])
+    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "qft16", "hbm", "batched", "adjoint", "blocks"])
     ap.add_argument("--hbm-n64", type=int, default=32)
     ap.add_argument("--hbm-n128", type=int, default=31)
     ap.add_argument("--batch-count", type=int, default=4096)
@@ -697,7 +741,8 @@ def main():
     elif args.workload == "brickwork":
         run_ours(args)
     else:
-        {"qft16": run_qft16, "hbm": run_hbm, "batched": run_batched, "adjoint": run_adjoint}[args.workload](args)
+        {"qft16": run_qft16, "hbm": run_hbm, "batched": run_batched, "adjoint": run_adjoint,
+         "blocks": run_block_placements}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -210,7 +210,9 @@ struct Dense1Args {
   CT<R> m00, m01, m10, m11;
 };
 
-template <typename R>
+// REAL: the matrix has no imaginary parts (H, RY, ...): half the multiplies, which
+// matters for complex128 where the FP64 pipe, not HBM, bounds the pass on GB300.
+template <typename R, bool REAL>
 __global__ void __launch_bounds__(QSV_THREADS)
     k_dense1(CT<R>* __restrict__ psi, const __grid_constant__ Dense1Args<R> a) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -221,11 +223,18 @@ __global__ void __launch_bounds__(QSV_THREADS)
     const CT<R> x = psi[i0];
     const CT<R> y = psi[i0 + hi];
     CT<R> o0, o1;
-    o0.x = R(0); o0.y = R(0); o1 = o0;
-    o0 = qsv_cfma(a.m00, x, o0);
-    o0 = qsv_cfma(a.m01, y, o0);
-    o1 = qsv_cfma(a.m10, x, o1);
-    o1 = qsv_cfma(a.m11, y, o1);
+    if constexpr (REAL) {
+      o0.x = a.m00.x * x.x + a.m01.x * y.x;
+      o0.y = a.m00.x * x.y + a.m01.x * y.y;
+      o1.x = a.m10.x * x.x + a.m11.x * y.x;
+      o1.y = a.m10.x * x.y + a.m11.x * y.y;
+    } else {
+      o0.x = R(0); o0.y = R(0); o1 = o0;
+      o0 = qsv_cfma(a.m00, x, o0);
+      o0 = qsv_cfma(a.m01, y, o0);
+      o1 = qsv_cfma(a.m10, x, o1);
+      o1 = qsv_cfma(a.m11, y, o1);
+    }
     psi[i0] = o0;
     psi[i0 + hi] = o1;
   }
@@ -270,7 +279,9 @@ struct MonoArgs {
   CT<R> ph[1 << K];
 };
 
-template <typename R, int K>
+// PURE: every phase is exactly 1, so the gate only moves amplitudes (no arithmetic is
+// compiled in at all, bit-exact and bandwidth-bound in either precision).
+template <typename R, int K, bool PURE>
 __global__ void __launch_bounds__(QSV_THREADS)
     k_mono(CT<R>* __restrict__ psi, const __grid_constant__ MonoArgs<R, K> a) {
   constexpr int D = 1 << K;
@@ -286,7 +297,9 @@ __global__ void __launch_bounds__(QSV_THREADS)
 #pragma unroll
       for (int c = 1; c < D; ++c)
         if (a.perm[r] == c) x = v[c];
-      if (!((a.exact >> r) & 1u)) x = qsv_cmul(a.ph[r], x);
+      if constexpr (!PURE) {
+        if (!((a.exact >> r) & 1u)) x = qsv_cmul(a.ph[r], x);
+      }
       psi[base + a.off[r]] = x;
     }
   }
@@ -759,7 +772,11 @@ int launch_dense(qsv_state* s, const GateGeom& g, const double* mat) {
     a.m01 = to_ct<R>(mat + 2);
     a.m10 = to_ct<R>(mat + 4);
     a.m11 = to_ct<R>(mat + 6);
-    k_dense1<R><<<grid_for(s, ngroups), QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, a);
+    const bool real = mat[1] == 0.0 && mat[3] == 0.0 && mat[5] == 0.0 && mat[7] == 0.0;
+    if (real)
+      k_dense1<R, true><<<grid_for(s, ngroups), QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, a);
+    else
+      k_dense1<R, false><<<grid_for(s, ngroups), QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, a);
     return check_launch(s, "dense1");
   }
   auto* a = new (std::nothrow) DenseArgs<R, K>();
@@ -832,7 +849,10 @@ int launch_mono(qsv_state* s, const GateGeom& g, const int* perm, const double* 
     a.ph[r] = to_ct<R>(phase + 2 * r);
     if (phase[2 * r] == 1.0 && phase[2 * r + 1] == 0.0) a.exact |= 1u << r;
   }
-  k_mono<R, K><<<grid_for(s, a.ngroups), QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, a);
+  if (a.exact == (1u << D) - 1u)
+    k_mono<R, K, true><<<grid_for(s, a.ngroups), QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, a);
+  else
+    k_mono<R, K, false><<<grid_for(s, a.ngroups), QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, a);
   return check_launch(s, "monomial");
 }
 

@@ -74,7 +74,8 @@ struct BlockArgs {
   uint64_t ntiles;
   int k;
   int staged;           // 1: address-order staging (targets in the low 7 bits), 0: direct
-  int vec2;             // direct: target combinations t, t^1 are adjacent amplitudes (16-byte pairs)
+  int vec;              // direct: amplitudes per global access (1, 2 or 4): t's lowest bits are
+                        // the target bits 0.. of the address, so t..t+vec-1 are adjacent
   int ptile[16];        // the 7+k tile positions, ascending (zero insertion -> tile base)
   uint16_t eb[FB_M];    // e of group b
   uint16_t et[64];      // e of target combination t (targets[0] = MSB of t)
@@ -205,6 +206,21 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   return *reinterpret_cast<uint32_t*>(&h);
 }
 
+// 256-bit global accesses (4 adjacent complex64 amplitudes, 32-byte aligned), streaming.
+__device__ __forceinline__ void ld_v8(const float2* p, float2* v) {
+  float f[8];
+  asm volatile("ld.global.cs.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(f[0]), "=f"(f[1]), "=f"(f[2]), "=f"(f[3]), "=f"(f[4]), "=f"(f[5]), "=f"(f[6]), "=f"(f[7])
+               : "l"(p));
+#pragma unroll
+  for (int i = 0; i < 4; ++i) v[i] = make_float2(f[2 * i], f[2 * i + 1]);
+}
+__device__ __forceinline__ void st_v8(float2* p, const float* re, const float* im) {
+  asm volatile("st.global.cs.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(re[0]), "f"(im[0]), "f"(re[1]),
+               "f"(im[1]), "f"(re[2]), "f"(im[2]), "f"(re[3]), "f"(im[3])
+               : "memory");
+}
+
 // Splits 8 floats into bf16 hi/lo halves, packed 8 per uint4.
 __device__ __forceinline__ void split8(const float* x, uint4& hi, uint4& lo) {
   float h[8], l[8];
@@ -295,7 +311,17 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         const int e = 2 * (u * FB_THREADS + tid);
         buf[u] = __ldcs(reinterpret_cast<const float4*>(psi + base + dep(e)));
       }
-    } else if (a.vec2) {
+    } else if (a.vec == 4) {
+#pragma unroll
+      for (int it = 0; it < P::ITEMS; ++it) {
+        const int item = it * FB_THREADS + tid;
+        const int b = item & (FB_M - 1);
+        const int tg = item >> FB_BATCH_BITS;
+        const uint64_t rb = base + dep(eb[b]);
+#pragma unroll
+        for (int j = 0; j < 8; j += 4) ld_v8(psi + rb + dep(et[tg * 8 + j]), &buf2[it][j]);
+      }
+    } else if (a.vec == 2) {
 #pragma unroll
       for (int it = 0; it < P::ITEMS; ++it) {
         const int item = it * FB_THREADS + tid;
@@ -416,7 +442,11 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         if constexpr (STAGED) {
 #pragma unroll
           for (int j = 0; j < CH; ++j) raw[slot(eb_ | et[t0 + j])] = make_float2(re[j], im[j]);
-        } else if (a.vec2) {
+        } else if (a.vec == 4 && CH % 4 == 0) {
+          const uint64_t rb = base + dep(eb_);
+#pragma unroll
+          for (int j = 0; j < CH; j += 4) st_v8(psi + rb + dep(et[t0 + j]), &re[j], &im[j]);
+        } else if (a.vec >= 2) {
           const uint64_t rb = base + dep(eb_);
 #pragma unroll
           for (int j = 0; j < CH; j += 2)
@@ -513,9 +543,14 @@ void tile_geometry(int k, const int* tpos, BlockArgs& a) {
   uint64_t tmask = 0;
   for (int j = 0; j < k; ++j) tmask |= 1ull << tpos[j];
   // Direct loads/stores stay coalesced while few targets sit in the 7 lowest bits.
-  a.staged = __builtin_popcountll(tmask & 0x7Full) >= 3 ? 1 : 0;
-  // t's least significant bit is tpos[k-1]; at address bit 0, t and t^1 are adjacent.
-  a.vec2 = tpos[k - 1] == 0 ? 1 : 0;
+  // Direct loads/stores stay sector-efficient when the block's targets below bit 7 form
+  // a prefix 0..L-1 of the address and t's lowest bits are exactly those (tpos in
+  // descending bit order): t..t+3 are then adjacent amplitudes (one 32-byte sector).
+  int L = 0;
+  while (L < k && tpos[k - 1 - L] == L) ++L;
+  const int low = __builtin_popcountll(tmask & 0x7Full);
+  a.vec = L >= 2 ? 4 : (L == 1 ? 2 : 1);
+  a.staged = (low > L && low >= 3) ? 1 : 0;
   int batch[FB_BATCH_BITS];
   for (int p = 0, nb = 0; nb < FB_BATCH_BITS; ++p)
     if (!((tmask >> p) & 1ull)) batch[nb++] = p;
