@@ -689,6 +689,8 @@ def run_block_placements(args):
     bits_list = [list(range(n - k, n)), list(range(k)), [0, 1] + list(range(n - k + 2, n)),
                  [0, 1, 2, 3] + list(range(n - k + 4, n)), [1, 2, 3] + list(range(n - k + 3, n)),
                  [0, 2, 4, 6, 8, 10][:k], sorted(int(x) for x in rng.choice(n, k, replace=False))]
+    for low in ([3, 4], [1, 2], [4, 5, 6], [1, 2, 3, 4], [5, 6]):
+        bits_list.append(low + list(range(n - k + len(low), n)))
     peak, _ = read_peaks()
     rows = []
     for bits in bits_list:

@@ -70,10 +70,26 @@ struct FB {
 // consecutive e are adjacent amplitudes.  The shared staging buffer stores element e at
 // word e ^ (swz[e >> 4] << 1): a host-chosen XOR of 16-byte slots that keeps the
 // (b-consecutive) transposing accesses spread over the banks for any placement.
+//
+// Shuffle mode (for targets among address bits 0..4 that are not a prefix): lane x of a
+// warp always loads and stores address bit pattern x of 32 consecutive amplitudes.
+// Kernel target order t' lists the targets by ascending position (the block matrix is
+// permuted to match, tperm), so the j targets in bits 0..4 are t' bits 0..j-1.  After
+// the load, up to three exchange rounds (shfl.xor on lane bit = that target's address
+// bit, register bit i) move t' bits 0..2 into register bits 0..2: each group of 8
+// registers then holds one row m and 8 consecutive t' of the A operand.  The epilogue
+// reads TMEM row m = 32*(warp%4) + lane, columns t' = (warp/4)*T/2 + c, and j exchange
+// rounds (lane bits whose group bit is above address bit 4 <-> c bits 0..j-1) restore
+// 32 consecutive amplitudes per store.  All addresses and operand offsets are sums of
+// per-bit contributions listed in the tables below.
+constexpr int MODE_DIRECT = 0;
+constexpr int MODE_STAGED = 1;
+constexpr int MODE_SHUF = 2;
+
 struct BlockArgs {
   uint64_t ntiles;
   int k;
-  int staged;           // 1: address-order staging (targets in the low 7 bits), 0: direct
+  int mode;             // MODE_DIRECT, MODE_STAGED or MODE_SHUF
   int vec;              // direct: amplitudes per global access (1, 2 or 4): t's lowest bits are
                         // the target bits 0.. of the address, so t..t+vec-1 are adjacent
   int ptile[16];        // the 7+k tile positions, ascending (zero insertion -> tile base)
@@ -81,6 +97,17 @@ struct BlockArgs {
   uint16_t et[64];      // e of target combination t (targets[0] = MSB of t)
   uint8_t swz[512];     // 3-bit slot swizzle per (e >> 4)
   uint64_t dephi[64];   // address offset of e >> 7
+  // Shuffle mode tables (see above).
+  int nld, nst;         // exchange rounds after the load / in the epilogue
+  int ld_lane[3];       // lane bit of load round i (register bit i)
+  int st_lane[5];       // lane bit of epilogue round i (register bit i)
+  uint64_t ld_warp[3];  // address contribution of warp bits (lane x contributes x)
+  uint64_t ld_reg[32];  // address offset of load register r
+  uint32_t a_lw[8];     // A byte offset of lane bits 0..4 and warp bits 0..2 after the load rounds
+  uint32_t a_it[4];     // A byte offset of register group it (registers 8*it .. 8*it+7)
+  uint64_t st_lw[8];    // address contribution of lane bits 0..4, warp bits 0..1 (row quadrant), warp bit 2
+  uint64_t st_reg[32];  // address offset of epilogue register c
+  uint8_t tperm[64];    // kernel target order t' -> block matrix index t (identity unless shuffle)
   const uint4* wimg;    // hi image then lo image (2 * W_BYTES bytes)
   int* flag;            // status word
 };
@@ -234,17 +261,21 @@ __device__ __forceinline__ void split8(const float* x, uint4& hi, uint4& lo) {
   lo = make_uint4(pack_bf16(l[0], l[1]), pack_bf16(l[2], l[3]), pack_bf16(l[4], l[5]), pack_bf16(l[6], l[7]));
 }
 
-// STAGED = false ("direct"): each thread loads (b, 8 targets) items straight from
-// global memory and the epilogue stores TMEM rows straight back; coalesced when the 7
-// lowest address bits are batch bits.  STAGED = true: the tile moves through a shared
-// staging buffer in address order (16-byte coalesced global accesses for any target
-// placement) at the cost of two extra shared-memory passes.
-template <int KQ, bool STAGED>
+// MODE_DIRECT: each thread loads (b, 8 targets) items straight from global memory and
+// the epilogue stores TMEM rows straight back; coalesced when the 5 lowest address bits
+// are batch bits (or the low targets are an address prefix, vec > 1).  MODE_STAGED: the
+// tile moves through a shared staging buffer in address order (16-byte coalesced global
+// accesses for any placement) at the cost of two extra shared-memory passes.
+// MODE_SHUF: lane = 5 lowest address bits, warp shuffles transpose in registers.
+template <int KQ, int MODE>
 __global__ void __launch_bounds__(FB_THREADS, 1)
     k_block_tc(float2* __restrict__ psi, const __grid_constant__ BlockArgs a) {
   using P = FB<KQ>;
+  constexpr bool STAGED = MODE == MODE_STAGED;
+  constexpr bool SHUF = MODE == MODE_SHUF;
   constexpr int SMEM_USED = STAGED ? P::SMEM : P::SMEM_DIRECT;
   constexpr int RAW = STAGED ? P::RAW_BYTES : 0;
+  constexpr int R = P::T / 2;  // shuffle mode: amplitudes per thread
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA_hi = smem;
   uint8_t* sA_lo = smem + P::A_BYTES;
@@ -304,8 +335,34 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   // amplitudes).  Direct: item it holds (b, targets tg*8..tg*8+7).
   float4 buf[P::VEC];
   float2 buf2[P::ITEMS][8];
+  float2 v[SHUF ? R : 1];
+  // Shuffle mode: per-thread sums of the lane/warp contributions.
+  uint64_t ld_lw = 0, st_lw = 0;
+  uint32_t a_lw = 0;
+  if constexpr (SHUF) {
+    ld_lw = (uint64_t)lane;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      if ((warp >> i) & 1) ld_lw += a.ld_warp[i];
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+      if ((lane >> i) & 1) {
+        a_lw += a.a_lw[i];
+        st_lw += a.st_lw[i];
+      }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      if ((warp >> i) & 1) {
+        a_lw += a.a_lw[5 + i];
+        st_lw += a.st_lw[5 + i];
+      }
+  }
   auto load_tile = [&](uint64_t base) {
-    if constexpr (STAGED) {
+    if constexpr (SHUF) {
+      const float2* src = psi + base + ld_lw;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = __ldcs(src + a.ld_reg[r]);
+    } else if constexpr (STAGED) {
 #pragma unroll
       for (int u = 0; u < P::VEC; ++u) {
         const int e = 2 * (u * FB_THREADS + tid);
@@ -365,8 +422,48 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
       __syncthreads();
     }
     // 2. Transpose into the A operand: row b, K = [Re t | Im t], bf16 hi/lo split.
+    if constexpr (SHUF) {
 #pragma unroll
-    for (int it = 0; it < P::ITEMS; ++it) {
+      for (int i = 0; i < 3; ++i) {
+        if (i < a.nld) {
+          const int lb = a.ld_lane[i];
+          const bool up = (lane >> lb) & 1;
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            if (r & (1 << i)) continue;
+            const int r1 = r | (1 << i);
+            const float2 send = up ? v[r] : v[r1];
+            float2 got;
+            got.x = __shfl_xor_sync(0xffffffffu, send.x, 1 << lb);
+            got.y = __shfl_xor_sync(0xffffffffu, send.y, 1 << lb);
+            if (up)
+              v[r] = got;
+            else
+              v[r1] = got;
+          }
+        }
+      }
+#pragma unroll
+      for (int it = 0; it < R / 8; ++it) {
+        float re[8], im[8];
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+          re[g] = v[8 * it + g].x;
+          im[g] = v[8 * it + g].y;
+        }
+        uint4 rh, rl, ih, il;
+        split8(re, rh, rl);
+        split8(im, ih, il);
+        const uint32_t off_re = a_lw + a.a_it[it];
+        const uint32_t off_im = off_re + (P::T / 8) * P::A_LBO;
+        *reinterpret_cast<uint4*>(sA_hi + off_re) = rh;
+        *reinterpret_cast<uint4*>(sA_lo + off_re) = rl;
+        *reinterpret_cast<uint4*>(sA_hi + off_im) = ih;
+        *reinterpret_cast<uint4*>(sA_lo + off_im) = il;
+      }
+    }
+#pragma unroll
+    for (int it = 0; it < (SHUF ? 0 : P::ITEMS); ++it) {
       const int item = it * FB_THREADS + tid;
       const int b = item & (FB_M - 1);
       const int tg = item >> FB_BATCH_BITS;
@@ -425,7 +522,42 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
     if (*abort_flag) break;
     // 5. Epilogue: TMEM lane b -> the staging buffer.  Warp w reads lanes 32*(w%4)..
     //    and output targets [h*T/2, (h+1)*T/2) with h = w/4.
-    {
+    if constexpr (SHUF) {
+      constexpr int CHS = P::COLS_PER_WARP;
+      const int q = warp & 3;
+      const int h = warp >> 2;
+      const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
+      float re[CHS], im[CHS];
+      tmem_ld<CHS>(lane_addr + (uint32_t)(h * CHS), re);
+      tmem_ld<CHS>(lane_addr + (uint32_t)(P::T + h * CHS), im);
+      tmem_ld_wait();
+#pragma unroll
+      for (int i = 0; i < 5; ++i) {
+        if (i < KQ - 1 && i < a.nst) {
+          const int lb = a.st_lane[i];
+          const bool up = (lane >> lb) & 1;
+#pragma unroll
+          for (int c = 0; c < CHS; ++c) {
+            if (c & (1 << i)) continue;
+            const int c1 = c | (1 << i);
+            const float sr = up ? re[c] : re[c1];
+            const float si = up ? im[c] : im[c1];
+            const float gr = __shfl_xor_sync(0xffffffffu, sr, 1 << lb);
+            const float gi = __shfl_xor_sync(0xffffffffu, si, 1 << lb);
+            if (up) {
+              re[c] = gr;
+              im[c] = gi;
+            } else {
+              re[c1] = gr;
+              im[c1] = gi;
+            }
+          }
+        }
+      }
+      float2* dst = psi + base + st_lw;
+#pragma unroll
+      for (int c = 0; c < CHS; ++c) __stcs(dst + a.st_reg[c], make_float2(re[c], im[c]));
+    } else {
       const int q = warp & 3;
       const int h = warp >> 2;
       const int b = q * 32 + lane;
@@ -508,16 +640,17 @@ size_t image_bytes(int k) {
 }
 
 // Builds the hi/lo bf16 images of W = [[Ur, -Ui], [Ui, Ur]] in the K-major canonical
-// layout: element (row nn, col kk) at (kk/8)*(KD*16) + nn*16 + (kk%8)*2.
-void build_image(int k, const double* U, uint8_t* out) {
+// layout: element (row nn, col kk) at (kk/8)*(KD*16) + nn*16 + (kk%8)*2.  Rows and
+// columns follow the kernel target order: U is read at (tperm[t'], tperm[t]).
+void build_image(int k, const double* U, const uint8_t* tperm, uint8_t* out) {
   const int T = 1 << k, KD = 2 * T;
   uint16_t* hi = reinterpret_cast<uint16_t*>(out);
   uint16_t* lo = reinterpret_cast<uint16_t*>(out + (size_t)KD * KD * 2);
   for (int nn = 0; nn < KD; ++nn) {
-    const int tp = nn % T;
+    const int tp = tperm[nn % T];
     const bool out_im = nn >= T;
     for (int kk = 0; kk < KD; ++kk) {
-      const int t = kk % T;
+      const int t = tperm[kk % T];
       const bool in_im = kk >= T;
       const double ur = U[2 * ((size_t)tp * T + t)], ui = U[2 * ((size_t)tp * T + t) + 1];
       double w;
@@ -535,6 +668,164 @@ void build_image(int k, const double* U, uint8_t* out) {
   }
 }
 
+// Shuffle-mode tables (see BlockArgs).  Element e of the tile is named by its bit
+// roles: lane bits 0..4 (address bits 0..4), warp bits and register bits.  Returns false
+// (the caller then stages the tile) if a table would not cover every tile bit once.
+bool shuffle_tables(int k, const int* tpos, const int* batch, const int* eidx, int j, BlockArgs& a) {
+  const int T = 1 << k, R = T / 2, ebits = FB_BATCH_BITS + k;
+  constexpr int A_LBO = FB_M * 16;
+  int kt[8];  // kernel target order: positions ascending
+  for (int i = 0; i < k; ++i) kt[i] = tpos[i];
+  std::sort(kt, kt + k);
+  int tE[8];       // e of kernel target bit i
+  int tbit[24];    // kernel target bit of e, or -1
+  bool isb[24];    // e is a group (batch) bit
+  for (int e = 0; e < ebits; ++e) {
+    tbit[e] = -1;
+    isb[e] = false;
+  }
+  for (int i = 0; i < k; ++i) {
+    tE[i] = eidx[kt[i]];
+    tbit[tE[i]] = i;
+  }
+  for (int i = 0; i < FB_BATCH_BITS; ++i) isb[eidx[batch[i]]] = true;
+  for (int tp = 0; tp < T; ++tp) {
+    int t = 0;
+    for (int i = 0; i < k; ++i) {
+      if (!((tp >> i) & 1)) continue;
+      int jj = 0;
+      while (tpos[jj] != kt[i]) ++jj;
+      t |= 1 << (k - 1 - jj);
+    }
+    a.tperm[tp] = (uint8_t)t;
+  }
+  if (j < 1 || j > k - 1) return false;
+  const int s = std::min(j, 3);
+  // Register bits before the load rounds: group bits above address bit 4 in 0..s-1
+  // (they trade places with the first s lane targets), t' bits s..2, then the rest.
+  int hb[16], nhb = 0;
+  for (int e = 5; e < ebits; ++e)
+    if (isb[e]) hb[nhb++] = e;
+  int reg[8], wb[3];
+  bool used[24] = {false};
+  for (int i = 0; i < 3; ++i) {
+    reg[i] = i < s ? hb[i] : tE[i];
+    used[reg[i]] = true;
+  }
+  int rest[24], nr = 0;
+  for (int e = 5; e < ebits; ++e)
+    if (!used[e]) rest[nr++] = e;
+  if (nr != k - 1) return false;
+  for (int i = 3; i < k - 1; ++i) reg[i] = rest[i - 3];
+  for (int i = 0; i < 3; ++i) wb[i] = rest[k - 4 + i];
+  a.nld = s;
+  for (int i = 0; i < 3; ++i) a.ld_lane[i] = i < s ? tE[i] : 0;
+  for (int i = 0; i < 3; ++i) a.ld_warp[i] = 1ull << a.ptile[wb[i]];
+  for (int r = 0; r < 32; ++r) {
+    uint64_t off = 0;
+    for (int i = 0; i < k - 1; ++i)
+      if (r < R && ((r >> i) & 1)) off += 1ull << a.ptile[reg[i]];
+    a.ld_reg[r] = off;
+  }
+  int lane_after[5], reg_after[8];
+  for (int x = 0; x < 5; ++x) lane_after[x] = x;
+  for (int i = 0; i < k - 1; ++i) reg_after[i] = reg[i];
+  for (int i = 0; i < s; ++i) {
+    lane_after[tE[i]] = reg[i];
+    reg_after[i] = tE[i];
+  }
+  // A row order m: row bits 0..2 = the group bits on lane bits 0..2 (distinct 16-byte
+  // slots per quarter warp), then the remaining group bits below address bit 5, then the rest.
+  int mb[FB_BATCH_BITS], nm = 0, mbit[24];
+  bool placed[24] = {false};
+  for (int x = 0; x < 3; ++x) {
+    if (!isb[lane_after[x]]) return false;
+    mb[nm++] = lane_after[x];
+    placed[lane_after[x]] = true;
+  }
+  for (int e = 0; e < 5; ++e)
+    if (isb[e] && !placed[e]) {
+      mb[nm++] = e;
+      placed[e] = true;
+    }
+  for (int e = 5; e < ebits && nm < FB_BATCH_BITS; ++e)
+    if (isb[e] && !placed[e]) {
+      mb[nm++] = e;
+      placed[e] = true;
+    }
+  if (nm != FB_BATCH_BITS) return false;
+  for (int i = 0; i < FB_BATCH_BITS; ++i) mbit[mb[i]] = i;
+  auto contrib_a = [&](int e) -> uint32_t {
+    if (isb[e]) return 16u << mbit[e];
+    return (uint32_t)A_LBO << (tbit[e] - 3);
+  };
+  // Load side: lane_after, warp bits and reg_after bits 3.. must cover every bit once,
+  // with t' bits 0..2 exactly on register bits 0..2.
+  {
+    int cover[24] = {0};
+    for (int x = 0; x < 5; ++x) cover[lane_after[x]]++;
+    for (int i = 0; i < 3; ++i) cover[wb[i]]++;
+    for (int i = 0; i < k - 1; ++i) cover[reg_after[i]]++;
+    for (int e = 0; e < ebits; ++e)
+      if (cover[e] != 1) return false;
+    for (int i = 0; i < 3; ++i)
+      if (tbit[reg_after[i]] != i) return false;
+    for (int x = 0; x < 5; ++x)
+      if (!isb[lane_after[x]] && tbit[lane_after[x]] < 3) return false;
+    for (int i = 0; i < 3; ++i)
+      if (!isb[wb[i]] && tbit[wb[i]] < 3) return false;
+    for (int i = 3; i < k - 1; ++i)
+      if (!isb[reg_after[i]] && tbit[reg_after[i]] < 3) return false;
+  }
+  for (int x = 0; x < 5; ++x) a.a_lw[x] = contrib_a(lane_after[x]);
+  for (int i = 0; i < 3; ++i) a.a_lw[5 + i] = contrib_a(wb[i]);
+  for (int it = 0; it < 4; ++it) {
+    uint32_t off = 0;
+    for (int y = 0; 3 + y < k - 1; ++y)
+      if (it < R / 8 && ((it >> y) & 1)) off += contrib_a(reg_after[3 + y]);
+    a.a_it[it] = off;
+  }
+  // Epilogue: row bits 0..4 on the lanes; the j of them above address bit 4 trade
+  // places with register bits 0..j-1 (t' bits 0..j-1, the targets below bit 5).
+  int es[5], nes = 0;
+  for (int x = 0; x < 5; ++x)
+    if (mb[x] >= 5) es[nes++] = x;
+  if (nes != j) return false;
+  int lane_epi[5], reg_epi[8];
+  for (int x = 0; x < 5; ++x) lane_epi[x] = mb[x];
+  for (int i = 0; i < k - 1; ++i) reg_epi[i] = tE[i];
+  for (int i = 0; i < j; ++i) {
+    lane_epi[es[i]] = tE[i];
+    reg_epi[i] = mb[es[i]];
+  }
+  {
+    int cover[24] = {0};
+    for (int x = 0; x < 5; ++x) {
+      if (lane_epi[x] >= 5) return false;
+      cover[lane_epi[x]]++;
+    }
+    cover[mb[5]]++;
+    cover[mb[6]]++;
+    cover[tE[k - 1]]++;
+    for (int i = 0; i < k - 1; ++i) cover[reg_epi[i]]++;
+    for (int e = 0; e < ebits; ++e)
+      if (cover[e] != 1) return false;
+  }
+  a.nst = j;
+  for (int i = 0; i < 5; ++i) a.st_lane[i] = i < j ? es[i] : 0;
+  for (int x = 0; x < 5; ++x) a.st_lw[x] = 1ull << a.ptile[lane_epi[x]];
+  a.st_lw[5] = 1ull << a.ptile[mb[5]];
+  a.st_lw[6] = 1ull << a.ptile[mb[6]];
+  a.st_lw[7] = 1ull << a.ptile[tE[k - 1]];
+  for (int c = 0; c < 32; ++c) {
+    uint64_t off = 0;
+    for (int i = 0; i < k - 1; ++i)
+      if (c < R && ((c >> i) & 1)) off += 1ull << a.ptile[reg_epi[i]];
+    a.st_reg[c] = off;
+  }
+  return true;
+}
+
 // Tile geometry of a block on target positions tpos[0..k) (tpos[0] = MSB of t):
 // sorted tile positions, the e-index maps of groups and targets, the address table
 // and the staging swizzle (see BlockArgs).
@@ -542,15 +833,17 @@ void tile_geometry(int k, const int* tpos, BlockArgs& a) {
   const int ebits = FB_BATCH_BITS + k;
   uint64_t tmask = 0;
   for (int j = 0; j < k; ++j) tmask |= 1ull << tpos[j];
-  // Direct loads/stores stay coalesced while few targets sit in the 7 lowest bits.
-  // Direct loads/stores stay sector-efficient when the block's targets below bit 7 form
-  // a prefix 0..L-1 of the address and t's lowest bits are exactly those (tpos in
-  // descending bit order): t..t+3 are then adjacent amplitudes (one 32-byte sector).
+  // Lanes of a warp cover address bits 0..4.  With j targets there, direct accesses
+  // stay coalesced only when those targets are the address prefix 0..L-1 with L <= 2
+  // (L == j; t's lowest bits are exactly those, as tpos is in descending bit order, so
+  // t..t+vec-1 are adjacent amplitudes and a warp reads 32 x vec contiguous
+  // amplitudes; a longer prefix spreads the lanes 2^L amplitudes apart).  Otherwise the
+  // shuffle mode handles up to k-1 of them and the staged mode the rest.
   int L = 0;
   while (L < k && tpos[k - 1 - L] == L) ++L;
-  const int low = __builtin_popcountll(tmask & 0x7Full);
+  const int jl = __builtin_popcountll(tmask & 0x1Full);
   a.vec = L >= 2 ? 4 : (L == 1 ? 2 : 1);
-  a.staged = (low > L && low >= 3) ? 1 : 0;
+  a.mode = (jl == L && L <= 2) ? MODE_DIRECT : (jl <= k - 1 ? MODE_SHUF : MODE_STAGED);
   int batch[FB_BATCH_BITS];
   for (int p = 0, nb = 0; nb < FB_BATCH_BITS; ++p)
     if (!((tmask >> p) & 1ull)) batch[nb++] = p;
@@ -615,36 +908,42 @@ void tile_geometry(int k, const int* tpos, BlockArgs& a) {
   }
   for (int y = 0; y < (1 << (ebits - 4)); ++y) {
     int v = 0;
-    for (int j = 0; j < ebits - 4; ++j)
-      if ((y >> j) & 1) v ^= c[4 + j];
+    for (int jj = 0; jj < ebits - 4; ++jj)
+      if ((y >> jj) & 1) v ^= c[4 + jj];
     a.swz[y] = (uint8_t)v;
   }
+  for (int t = 0; t < T; ++t) a.tperm[t] = (uint8_t)t;
+  if (a.mode == MODE_SHUF && !shuffle_tables(k, tpos, batch, eidx, jl, a)) a.mode = MODE_STAGED;
 }
 
-template <int KQ, bool STAGED>
+template <int KQ, int MODE>
 int launch_block_variant(qsv_state* s, const BlockArgs& a) {
   using P = FB<KQ>;
-  constexpr int SMEM = STAGED ? P::SMEM : P::SMEM_DIRECT;
+  constexpr int SMEM = MODE == MODE_STAGED ? P::SMEM : P::SMEM_DIRECT;
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_block_tc<KQ, STAGED>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    cudaError_t e = cudaFuncSetAttribute(k_block_tc<KQ, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
     if (e != cudaSuccess) return set_error(s, QSV_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(e));
     configured = true;
   }
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_block_tc<KQ, STAGED>, FB_THREADS, SMEM);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_block_tc<KQ, MODE>, FB_THREADS, SMEM);
   if (per_sm < 1) per_sm = 1;
   // Bound co-resident CTAs so their TMEM allocations always fit (512 columns per SM).
   per_sm = std::min(per_sm, 512 / P::TMEM_COLS);
   uint64_t grid = (uint64_t)std::max(1, s->sm_count) * per_sm;
   if (grid > a.ntiles) grid = a.ntiles;
-  k_block_tc<KQ, STAGED><<<(unsigned)grid, FB_THREADS, SMEM, s->stream>>>((float2*)s->d_amp, a);
+  k_block_tc<KQ, MODE><<<(unsigned)grid, FB_THREADS, SMEM, s->stream>>>((float2*)s->d_amp, a);
   return check_launch(s, "block_tc");
 }
 
 template <int KQ>
 int launch_block(qsv_state* s, const BlockArgs& a) {
-  return a.staged ? launch_block_variant<KQ, true>(s, a) : launch_block_variant<KQ, false>(s, a);
+  switch (a.mode) {
+    case MODE_STAGED: return launch_block_variant<KQ, MODE_STAGED>(s, a);
+    case MODE_SHUF: return launch_block_variant<KQ, MODE_SHUF>(s, a);
+    default: return launch_block_variant<KQ, MODE_DIRECT>(s, a);
+  }
 }
 
 }  // namespace
@@ -718,7 +1017,7 @@ extern "C" int qsv_plan_create(qsv_state* s, int nblocks, const int* ks, const i
   }
   std::vector<uint8_t> host(total);
   for (int i = 0; i < nblocks; ++i)
-    build_image(ks[i], mats_c128 + mat_offs[(size_t)i], host.data() + img_off[(size_t)i]);
+    build_image(ks[i], mats_c128 + mat_offs[(size_t)i], p->args[(size_t)i].tperm, host.data() + img_off[(size_t)i]);
   if (cudaMalloc(&p->d_images, total) != cudaSuccess) {
     cudaGetLastError();
     delete p;
@@ -803,7 +1102,8 @@ extern "C" int qsv_apply_blocks(qsv_state* s, int nblocks, const int* ks, const 
     s->d_images_bytes = want;
   }
   uint8_t* himg = static_cast<uint8_t*>(s->h_img[slot]);
-  for (int i = 0; i < nblocks; ++i) build_image(ks[i], mats_c128 + mat_offs[(size_t)i], himg + img_off[(size_t)i]);
+  for (int i = 0; i < nblocks; ++i)
+    build_image(ks[i], mats_c128 + mat_offs[(size_t)i], args[(size_t)i].tperm, himg + img_off[(size_t)i]);
   QSV_CUDA(s, cudaMemcpyAsync(s->d_images, himg, total, cudaMemcpyHostToDevice, s->stream));
   QSV_CUDA(s, cudaEventRecord(s->img_ev[slot], s->stream));
   s->img_busy[slot] = true;

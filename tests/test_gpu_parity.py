@@ -260,6 +260,44 @@ def test_tensor_core_block_matches_oracle(k):
         assert infidelity(got, want) < 1e-8
 
 
+BLOCK_PLACEMENTS = [  # target bit positions below bit 7 (the rest sit at the top bits)
+    (6, ()), (6, (5, 6)), (6, (0,)), (6, (0, 1)),  # direct
+    (6, (0, 1, 2, 3, 4, 5)), (6, (0, 1, 2, 3)),  # shuffle (prefix longer than 2)
+    (6, (4,)), (6, (3, 4)), (6, (1, 2)), (6, (0, 2)), (6, (4, 5, 6)), (6, (1, 2, 3, 4)),  # shuffle
+    (6, (0, 1, 4, 5, 6)), (6, (2, 3, 4, 5, 6)), (5, (1, 3)), (5, (0, 2, 3, 4)), (4, (2, 3, 4)),
+    (4, (1, 2, 3, 4)), (4, (0, 2, 3, 4)),  # staged (all four targets below bit 5, not a prefix)
+]
+
+
+@pytest.mark.parametrize("k,low", BLOCK_PLACEMENTS)
+def test_tensor_core_block_modes_match_oracle(k, low):
+    """Each access mode of the tensor-core block kernel (direct, shuffle, staged), with
+    the block's qubits in ascending, descending and shuffled matrix order."""
+    n = 15
+    rng = numpy.random.default_rng(100 * k + len(low))
+    bits = list(low) + [n - 1 - i for i in range(k - len(low))]
+    from qip_gb300.fusion import Block
+
+    for order in ("asc", "desc", "shuffled"):
+        qubits = [n - 1 - b for b in bits]
+        if order == "asc":
+            qubits.sort()
+        elif order == "desc":
+            qubits.sort(reverse=True)
+        else:
+            rng.shuffle(qubits)
+        u = numpy.linalg.qr(rng.standard_normal((2 ** k, 2 ** k)) + 1j * rng.standard_normal((2 ** k, 2 ** k)))[0]
+        v = (rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)) / numpy.sqrt(2 ** (n + 1))
+        st = fresh(n, v, statetype=C64)
+        st.apply_blocks([Block(tuple(qubits), u, 1, 1.0)])
+        got = st.get_state()
+        st.close()
+        want = sv.apply_on(v, n, qubits, u)
+        err = numpy.max(numpy.abs(got - want)) / numpy.max(numpy.abs(want))
+        assert err < 5e-5, (qubits, err)
+        assert infidelity(got, want) < 1e-8
+
+
 def test_fused_brickwork_infidelity_n20():
     n, depth = 20, 12
     gl = circuits.brickwork(n, depth, seed=3)
