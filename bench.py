@@ -717,6 +717,64 @@ def run_block_placements(args):
                       "placements": rows}), flush=True)
 
 
+def run_gate_placements(args):
+    """Per-gate kernels by gate kind and target bit position (complex64 and complex128),
+    CUDA-event timed: algorithmic GB/s = 2 x amplitudes the gate rewrites x amp size."""
+    import torch
+
+    from qip_gb300 import GpuBackend, circuits
+    from qip_gb300.gates import GateOp
+
+    n = args.n
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    peak, _ = read_peaks()
+    rng = numpy.random.default_rng(5)
+    h = numpy.array([[1, 1], [1, -1]]) / numpy.sqrt(2)
+    u4 = numpy.linalg.qr(rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4)))[0]
+    u8 = numpy.linalg.qr(rng.standard_normal((8, 8)) + 1j * rng.standard_normal((8, 8)))[0]
+
+    def q(bit):
+        return n - 1 - bit
+
+    def kinds(p):
+        p2 = p + 1 if p + 1 < n else p - 1
+        p3 = p + 2 if p + 2 < n else p - 2
+        return [
+            ("haar1", GateOp("dense", (q(p),), (), circuits.haar_2x2(rng)), 1.0),
+            ("h1", GateOp("dense", (q(p),), (), h), 1.0),
+            ("phase1", GateOp("diag", (q(p),), (), numpy.array([1, numpy.exp(0.3j)])), 0.5),
+            ("x1", GateOp("mono", (q(p),), (), numpy.array([1, 1]), perm=numpy.array([1, 0])), 1.0),
+            ("cnot", GateOp("mono", (q(p),), (q(p2),), numpy.array([1, 1]), perm=numpy.array([1, 0])), 0.5),
+            ("cz", GateOp("diag", (q(p), q(p2)), (), numpy.array([1, 1, 1, -1])), 0.25),
+            ("dense2", GateOp("dense", (q(p), q(p2)), (), u4), 1.0),
+            ("dense3", GateOp("dense", (q(p), q(p2), q(p3)), (), u8), 1.0),
+            ("swap", GateOp("swap", (q(p),), (), swap_b=(q(p2),)), 0.5),
+        ]
+
+    rows = []
+    for dt, size in ((numpy.complex64, 8), (numpy.complex128, 16)):
+        st = GpuBackend.make_state(n, [], [], statetype=dt, fusion=False)
+        st.set_stream(stream.cuda_stream)
+        for p in (0, 1, 2, 3, 4, 5, 8, 16, n - 1):
+            for name, op, frac in kinds(p):
+                for _ in range(args.warmup):
+                    st.apply_op(op)
+                e0, e1 = _events()
+                e0.record(stream)
+                for _ in range(args.steps):
+                    st.apply_op(op)
+                e1.record(stream)
+                e1.synchronize()
+                ms = e0.elapsed_time(e1) / args.steps
+                gbs = 2 * frac * (2 ** n) * size / (ms * 1e-3) / 1e9
+                rows.append({"dtype": numpy.dtype(dt).name, "kind": name, "bit": p, "ms": round(ms, 4),
+                             "GB_s": round(gbs, 1), "frac": round(gbs / peak, 3)})
+        st.close()
+    print(json.dumps({"metric": "per-gate kernel GB/s by kind and target bit", "unit": "GB/s", "n": n,
+                      "peak": peak, "rows": rows}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -730,7 +788,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--parts", default="fused,plain,e2e,cpu",
                     help="comma list of fused,plain,e2e,cpu (profiling runs use fused only)")
-    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "qft16", "hbm", "batched", "adjoint", "blocks"])
+    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "qft16", "hbm", "batched", "adjoint", "blocks", "gates"])
     ap.add_argument("--hbm-n64", type=int, default=32)
     ap.add_argument("--hbm-n128", type=int, default=31)
     ap.add_argument("--batch-count", type=int, default=4096)
@@ -744,7 +802,7 @@ def main():
         run_ours(args)
     else:
         {"qft16": run_qft16, "hbm": run_hbm, "batched": run_batched, "adjoint": run_adjoint,
-         "blocks": run_block_placements}[args.workload](args)
+         "blocks": run_block_placements, "gates": run_gate_placements}[args.workload](args)
 
 
 if __name__ == "__main__":

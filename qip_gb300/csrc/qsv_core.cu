@@ -12,6 +12,7 @@
 #include <mutex>
 #include <thread>
 #include <new>
+#include <type_traits>
 #include <vector>
 
 #include "qsv_internal.cuh"
@@ -168,7 +169,37 @@ struct DenseArgs {
   CT<R> m[(1 << K) * (1 << K)];  // row-major
 };
 
-template <typename R, int K>
+// Vector loads/stores of 2^VB adjacent amplitudes (complex64; VB = 1: 16 bytes, VB = 2:
+// 32 bytes).  Used when matrix index bits 0..VB-1 are address bits 0..VB-1 (the host
+// orders the targets so), which turns a warp's 8-byte accesses spread over 2^VB times
+// as many cache lines into dense ones.
+template <int VB>
+__device__ __forceinline__ void ld_amps(const float2* p, float2* v) {
+  if constexpr (VB == 2) {
+    float f[8];
+    asm volatile("ld.global.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(f[0]), "=f"(f[1]), "=f"(f[2]), "=f"(f[3]), "=f"(f[4]), "=f"(f[5]), "=f"(f[6]), "=f"(f[7])
+                 : "l"(p));
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = make_float2(f[2 * i], f[2 * i + 1]);
+  } else {
+    const float4 x = *reinterpret_cast<const float4*>(p);
+    v[0] = make_float2(x.x, x.y);
+    v[1] = make_float2(x.z, x.w);
+  }
+}
+template <int VB>
+__device__ __forceinline__ void st_amps(float2* p, const float2* v) {
+  if constexpr (VB == 2) {
+    asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(v[0].x), "f"(v[0].y),
+                 "f"(v[1].x), "f"(v[1].y), "f"(v[2].x), "f"(v[2].y), "f"(v[3].x), "f"(v[3].y)
+                 : "memory");
+  } else {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+  }
+}
+
+template <typename R, int K, int VB>
 __global__ void __launch_bounds__(QSV_THREADS)
     k_dense(CT<R>* __restrict__ psi, const __grid_constant__ DenseArgs<R, K> a) {
   constexpr int D = 1 << K;
@@ -176,8 +207,25 @@ __global__ void __launch_bounds__(QSV_THREADS)
   for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < a.ngroups; g += stride) {
     const uint64_t base = qsv_insert_zeros(g, a.pos, a.npos) | a.ctrl;
     CT<R> v[D];
+    if constexpr (VB > 0) {
+      static_assert(K <= 3 && VB <= K, "vector path covers up to 3 targets");
 #pragma unroll
-    for (int j = 0; j < D; ++j) v[j] = psi[base + a.off[j]];
+      for (int j = 0; j < D; j += 1 << VB) ld_amps<VB>(psi + base + a.off[j], &v[j]);
+      CT<R> o[D];
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        o[r].x = R(0);
+        o[r].y = R(0);
+#pragma unroll
+        for (int c = 0; c < D; ++c) o[r] = qsv_cfma(a.m[r * D + c], v[c], o[r]);
+      }
+#pragma unroll
+      for (int j = 0; j < D; j += 1 << VB) st_amps<VB>(psi + base + a.off[j], &o[j]);
+      continue;
+    } else {
+#pragma unroll
+      for (int j = 0; j < D; ++j) v[j] = psi[base + a.off[j]];
+    }
     if constexpr (K <= 3) {
 #pragma unroll
       for (int r = 0; r < D; ++r) {
@@ -256,12 +304,23 @@ struct DiagArgs {
 template <typename R>
 __global__ void __launch_bounds__(QSV_THREADS)
     k_diag(CT<R>* __restrict__ psi, const __grid_constant__ DiagArgs<R> a) {
+  // Four groups per thread (stride apart, so a warp's accesses stay adjacent), their
+  // loads issued together: one amplitude per thread in flight is too little to keep
+  // HBM busy when a gate touches a single entry.
+  constexpr int U = 4;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < a.ngroups; g += stride) {
-    const uint64_t base = qsv_insert_zeros(g, a.pos, a.npos) | a.ctrl;
+  for (uint64_t g0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g0 < a.ngroups; g0 += U * stride) {
+    uint64_t base[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) base[u] = qsv_insert_zeros(g0 + u * stride, a.pos, a.npos) | a.ctrl;
     for (int e = 0; e < a.nent; ++e) {
-      const uint64_t idx = base + a.off[e];
-      psi[idx] = qsv_cmul(a.ph[e], psi[idx]);
+      CT<R> x[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (g0 + u * stride < a.ngroups) x[u] = psi[base[u] + a.off[e]];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (g0 + u * stride < a.ngroups) psi[base[u] + a.off[e]] = qsv_cmul(a.ph[e], x[u]);
     }
   }
 }
@@ -315,6 +374,41 @@ struct SwapArgs {
   int apos[QSV_MAXQ / 2];  // register a, first = MSB
   int bpos[QSV_MAXQ / 2];
 };
+
+// Single-qubit swap (m = 1): one item per exchanged pair (a = 1, b = 0) <-> (a = 0,
+// b = 1), two items per thread.  pos holds a, b and the controls, ascending.
+struct Swap1Args {
+  uint64_t nitems;  // 2^(n - 2 - ncontrols)
+  uint64_t ctrl;    // controls | bit a
+  uint64_t flip;    // bit a | bit b
+  int npos;
+  int pos[QSV_MAXQ];
+};
+
+template <typename R>
+__global__ void __launch_bounds__(QSV_THREADS)
+    k_swap1(CT<R>* __restrict__ psi, const __grid_constant__ Swap1Args a) {
+  constexpr int U = 2;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t0 < a.nitems; t0 += U * stride) {
+    uint64_t idx[U];
+    CT<R> x[U], y[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      idx[u] = qsv_insert_zeros(t0 + u * stride, a.pos, a.npos) | a.ctrl;
+      if (t0 + u * stride < a.nitems) {
+        x[u] = psi[idx[u]];
+        y[u] = psi[idx[u] ^ a.flip];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (t0 + u * stride < a.nitems) {
+        psi[idx[u]] = y[u];
+        psi[idx[u] ^ a.flip] = x[u];
+      }
+  }
+}
 
 template <typename R>
 __global__ void __launch_bounds__(QSV_THREADS)
@@ -785,9 +879,45 @@ int launch_dense(qsv_state* s, const GateGeom& g, const double* mat) {
   a->ctrl = g.ctrl;
   a->npos = g.npos;
   for (int i = 0; i < g.npos; ++i) a->pos[i] = g.sorted[i];
-  for (int j = 0; j < D; ++j) a->off[j] = target_offset(g, j);
-  for (int j = 0; j < D * D; ++j) a->m[j] = to_ct<R>(mat + 2 * j);
-  k_dense<R, K><<<grid_for(s, ngroups), QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, *a);
+  // complex64 with a target on address bit 0 (and 1): reorder the matrix index so its
+  // lowest bits are those address bits (targets by descending position; new index j'
+  // reads old index perm[j']) and move 2^VB adjacent amplitudes per access.
+  int vb = 0;
+  if (std::is_same<R, float>::value && K <= 3 && K >= 1) {
+    int order[8];
+    for (int b = 0; b < K; ++b) order[b] = b;
+    std::sort(order, order + K, [&](int x, int y) { return g.tpos[x] > g.tpos[y]; });
+    if (g.tpos[order[K - 1]] == 0) vb = (K >= 2 && g.tpos[order[K - 2]] == 1) ? 2 : 1;
+    if (vb) {
+      GateGeom gs = g;
+      for (int b = 0; b < K; ++b) gs.tpos[b] = g.tpos[order[b]];
+      unsigned perm[8];
+      for (unsigned jn = 0; jn < (unsigned)D; ++jn) {
+        unsigned jo = 0;
+        for (int b = 0; b < K; ++b)
+          if ((jn >> (K - 1 - b)) & 1u) jo |= 1u << (K - 1 - order[b]);
+        perm[jn] = jo;
+      }
+      for (int j = 0; j < D; ++j) a->off[j] = target_offset(gs, j);
+      for (int r = 0; r < D; ++r)
+        for (int c = 0; c < D; ++c) a->m[r * D + c] = to_ct<R>(mat + 2 * (perm[r] * D + perm[c]));
+    }
+  }
+  if (!vb) {
+    for (int j = 0; j < D; ++j) a->off[j] = target_offset(g, j);
+    for (int j = 0; j < D * D; ++j) a->m[j] = to_ct<R>(mat + 2 * j);
+  }
+  const unsigned grid = grid_for(s, ngroups);
+  if constexpr (K <= 3 && std::is_same<R, float>::value) {
+    if (vb == 2 && K >= 2)
+      k_dense<R, K, (K >= 2 ? 2 : 1)><<<grid, QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, *a);
+    else if (vb == 1)
+      k_dense<R, K, 1><<<grid, QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, *a);
+    else
+      k_dense<R, K, 0><<<grid, QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, *a);
+  } else {
+    k_dense<R, K, 0><<<grid, QSV_THREADS, 0, s->stream>>>((CT<R>*)s->d_amp, *a);
+  }
   delete a;
   return check_launch(s, "dense");
 }
@@ -1240,6 +1370,26 @@ int qsv_apply_swap(qsv_state* s, int m, const int* a, const int* b, int ncontrol
   if (!rc) rc = to_positions(s, m, b, args.bpos, &seen);
   if (!rc) rc = to_positions(s, ncontrols, controls, args.cpos, &seen);
   if (rc) return rc;
+  if (m == 1) {
+    Swap1Args a1;
+    a1.npos = 2 + ncontrols;
+    a1.pos[0] = args.apos[0];
+    a1.pos[1] = args.bpos[0];
+    a1.ctrl = 1ull << args.apos[0];
+    for (int i = 0; i < ncontrols; ++i) {
+      a1.pos[2 + i] = args.cpos[i];
+      a1.ctrl |= 1ull << args.cpos[i];
+    }
+    std::sort(a1.pos, a1.pos + a1.npos);
+    a1.flip = (1ull << args.apos[0]) | (1ull << args.bpos[0]);
+    a1.nitems = 1ull << (s->n - a1.npos);
+    const unsigned grid1 = grid_for(s, (a1.nitems + 1) / 2);
+    if (is_c64(s))
+      k_swap1<float><<<grid1, QSV_THREADS, 0, s->stream>>>((float2*)s->d_amp, a1);
+    else
+      k_swap1<double><<<grid1, QSV_THREADS, 0, s->stream>>>((double2*)s->d_amp, a1);
+    return check_launch(s, "swap1");
+  }
   args.m = m;
   args.ncp = ncontrols;
   args.ctrl = 0;

@@ -298,6 +298,43 @@ def test_tensor_core_block_modes_match_oracle(k, low):
         assert infidelity(got, want) < 1e-8
 
 
+@pytest.mark.parametrize("statetype,atol", [(C64, 2e-6), (C128, 1e-12)])
+def test_per_gate_low_bit_targets_match_oracle(statetype, atol):
+    """Dense gates whose targets include address bits 0/1 (vector accesses for
+    complex64) in every target order, with and without controls, and single-qubit and
+    register swaps, against the oracle."""
+    from qip_gb300.gates import GateOp
+
+    n = 10
+    rng = numpy.random.default_rng(31)
+    q = lambda bit: n - 1 - bit  # noqa: E731
+    cases = []
+    for bits in ([0], [1], [0, 1], [1, 0], [0, 5], [5, 0], [1, 0, 4], [0, 4, 1], [4, 1, 0], [0, 2], [2, 1, 0]):
+        for ctrl in ([], [7], [3, 8]):
+            k = len(bits)
+            u = numpy.linalg.qr(rng.standard_normal((2 ** k, 2 ** k)) + 1j * rng.standard_normal((2 ** k, 2 ** k)))[0]
+            cases.append(GateOp("dense", tuple(q(b) for b in bits), tuple(q(c) for c in ctrl), u))
+    for a, b, ctrl in ((0, 1, []), (1, 0, []), (0, 6, [2]), (7, 3, [0, 9]), (9, 0, [])):
+        cases.append(GateOp("swap", (q(a),), tuple(q(c) for c in ctrl), swap_b=(q(b),)))
+    cases.append(GateOp("swap", (q(0), q(3)), (q(6),), swap_b=(q(1), q(8))))
+    for bits, ctrl in (([0], []), ([1, 0], [5]), ([4], [0, 1])):
+        d = numpy.exp(1j * rng.uniform(0, 6.28, 2 ** len(bits)))
+        d[0] = 1.0
+        cases.append(GateOp("diag", tuple(q(b) for b in bits), tuple(q(c) for c in ctrl), d))
+    for op in cases:
+        v = (rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)) / numpy.sqrt(2 ** (n + 1))
+        st = fresh(n, v, statetype=statetype, fusion=False)
+        st.apply_op(op)
+        got = st.get_state()
+        st.close()
+        order, m = op.matrix()
+        want = sv.apply_on(v.astype(statetype).astype(complex), n, order, m)
+        if op.kind == "swap":
+            assert numpy.array_equal(got, want.astype(statetype)), op
+        else:
+            numpy.testing.assert_allclose(got, want, rtol=0, atol=atol, err_msg=str(op))
+
+
 def test_fused_brickwork_infidelity_n20():
     n, depth = 20, 12
     gl = circuits.brickwork(n, depth, seed=3)
