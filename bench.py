@@ -210,6 +210,7 @@ def run_ours(args):
     import torch
 
     from qip_gb300 import GpuBackend, _native as nat, circuits, fusion, gates as gmod
+    from qip_gb300.autotune import MODES as MODE_NAMES, default_tuner, placement_class
 
     ws, rank, local = dist_setup(args)
     n, depth = args.n, args.depth
@@ -218,14 +219,25 @@ def run_ours(args):
     gl = circuits.brickwork(n, depth, seed=SEED)
     amp_updates = circuits.gate_amp_updates(gl, n)
     ops = [op for g in gl for op in gmod.decompose(g)]
-    t_plan0 = time.perf_counter()
-    steps = fusion.plan(ops, kmax=args.kmax)
-    t_plan = time.perf_counter() - t_plan0
-    blocks = [s for s in steps if isinstance(s, fusion.Block) and len(s.qubits) >= 4]
     lib = nat.load()
-
     st = GpuBackend.make_state(n, [], [], statetype=numpy.complex64, fusion=True)
     st.set_stream(stream.cuda_stream)
+    t_plan0 = time.perf_counter()
+    tuner = default_tuner()
+    if args.kmax:
+        kmax, width_report = args.kmax, {}
+        steps = fusion.plan(ops, kmax=kmax)
+        tuner.ensure_plan(st.handle, n, steps)
+    else:
+        # Measured fusion width and block access modes (scratch-state timings).
+        kmax, steps, width_report = tuner.choose_width(st.handle, n, ops)
+    t_plan = time.perf_counter() - t_plan0
+    blocks = [s for s in steps if isinstance(s, fusion.Block) and len(s.qubits) >= 4]
+    mode_counts = {}
+    for b in blocks:
+        meas = tuner.measured(n, *placement_class(b.qubits, n))
+        name = MODE_NAMES[meas[1]] if meas else "rule"
+        mode_counts[name] = mode_counts.get(name, 0) + 1
     # Device-resident plan: block images uploaded once; a step launches kernels only.
     ks = nat.int_array([len(b.qubits) for b in blocks])
     tg = nat.int_array([q for b in blocks for q in b.qubits])
@@ -295,7 +307,10 @@ def run_ours(args):
             print(json.dumps({"metric": METRIC, "value": value, "unit": "amp-updates/s", "n_gpus": ws,
                               "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_fused * 1e3,
                               "partial": sorted(parts), "mean_block_ms": mean_block_s * 1e3,
-                              "gpu_launches": int(launches)}), flush=True)
+                              "gpu_launches": int(launches), "fusion_kmax": kmax, "fused_blocks": len(blocks),
+                              "autotune": {"width_predicted_ms": {str(k): round(v, 3)
+                                                                  for k, v in width_report.items()},
+                                           "block_modes": mode_counts, "plan_seconds": t_plan}}), flush=True)
         return
     # Plain complex128 per-gate path (the FP64 baseline of the metric).
     ref = GpuBackend.make_state(n, [], [], statetype=numpy.complex128, fusion=False)
@@ -335,7 +350,7 @@ def run_ours(args):
 
     # e2e through the plugin (StateType calls with host buffers).
     def e2e_step():
-        s2 = GpuBackend.make_state(n, [], [], statetype=numpy.complex64, fusion=True, max_block=args.kmax)
+        s2 = GpuBackend.make_state(n, [], [], statetype=numpy.complex64, fusion=True, max_block=kmax)
         for g in gl:
             s2.kronselect_dot(g)
         out = s2.get_state()
@@ -364,7 +379,9 @@ def run_ours(args):
         "data": "synthetic: seeded Haar-random brickwork, |0...0> input",
         "config": {"workload": f"brickwork n={n} depth {depth} (Haar 2x2 on every qubit, CZ even/odd pairs, "
                                f"C(Swap) every 10 layers)", "n": n, "depth": depth, "gates": len(gl),
-                   "amp_updates_per_step": amp_updates, "fusion_kmax": args.kmax,
+                   "amp_updates_per_step": amp_updates, "fusion_kmax": kmax,
+                   "autotune": {"width_predicted_ms": {str(k): round(v, 3) for k, v in width_report.items()},
+                                "block_modes": mode_counts},
                    "fused_blocks": len(blocks), "standalone_ops": sum(1 for k, _ in seq if k == "op"),
                    "plan_seconds": t_plan, "parallelism": f"replicas x{ws}",
                    "l2": f"state {2 ** n * 8 / 2 ** 30:.0f} GiB > L2; no flush needed"},
@@ -505,6 +522,7 @@ def run_hbm(args):
     import torch
 
     from qip_gb300 import GpuBackend, _native as nat, circuits, fusion, gates as gmod
+    from qip_gb300.autotune import default_tuner
 
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -522,6 +540,7 @@ def run_hbm(args):
         e0, e1 = _events()
         if fusion_on:
             steps = fusion.plan(ops, kmax=6)
+            default_tuner().ensure_plan(st.handle, n, steps)
         else:
             steps = ops
         t_all0, t_all1 = _events()
@@ -685,7 +704,7 @@ def run_block_placements(args):
     st.set_stream(stream.cuda_stream)
     lib = nat.load()
     rng = numpy.random.default_rng(3)
-    k = args.kmax
+    k = args.kmax or 6
     bits_list = [list(range(n - k, n)), list(range(k)), [0, 1] + list(range(n - k + 2, n)),
                  [0, 1, 2, 3] + list(range(n - k + 4, n)), [1, 2, 3] + list(range(n - k + 3, n)),
                  [0, 2, 4, 6, 8, 10][:k], sorted(int(x) for x in rng.choice(n, k, replace=False))]
@@ -783,7 +802,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--depth", type=int, default=DEPTH_DEFAULT)
-    ap.add_argument("--kmax", type=int, default=6)
+    ap.add_argument("--kmax", type=int, default=0, help="fusion width; 0 = measured by the autotuner")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--parts", default="fused,plain,e2e,cpu",

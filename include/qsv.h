@@ -113,6 +113,22 @@ int qsv_plan_create(qsv_state* s, int nblocks, const int* ks, const int* targets
 int qsv_plan_launch(qsv_state* s, const qsv_plan* p, int first, int count);
 int qsv_plan_destroy(qsv_plan* p);
 
+/* Access-mode autotuning of the tensor-core block kernel.  No reference counterpart
+ * (the reference has no GPU path).  A placement class is (k, low_mask): bit p of
+ * low_mask set <-> a target on address bit p, p < 7 (targets on higher bits do not
+ * change how a tile is read).  Modes: 0 direct, 1 staged (shared-memory transpose),
+ * 2 shuffle (warp exchanges; needs 1..k-1 targets on bits 0..4).  Choices are kept per
+ * device for the life of the process and used by qsv_apply_blocks / qsv_plan_create.
+ *
+ * qsv_tune_blocks times every applicable mode of each class (reps launches after one
+ * warm-up) on a zeroed scratch state of min(n, 26) qubits (the caller's state is not
+ * touched), writes out_ms[3*i + mode] (-1 where a mode does not apply) and out_mode[i],
+ * and records the fastest.  Synchronises the handle's stream.
+ * qsv_set_block_mode pins a mode for a class (mode -1 restores the built-in rule). */
+int qsv_tune_blocks(qsv_state* s, int count, const int* ks, const int* low_masks, int reps,
+                    double* out_ms, int* out_mode);
+int qsv_set_block_mode(qsv_state* s, int k, int low_mask, int mode);
+
 /* ---- measurement ---------------------------------------------------------------------
  * Marginal probabilities over m qubits, FP64 compensated sums, out[2^m].
  * Outcome bit j <-> qubits[j] (LSB first), as measure_probabilities

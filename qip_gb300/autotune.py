@@ -1,0 +1,139 @@
+"""Measured choices for the fused-block path: fusion width and tile access mode.
+
+The tensor-core block kernel reads and writes a tile in one of three access modes
+(direct, staged through shared memory, warp shuffles; ``include/qsv.h``).  Which one
+is fastest depends on where the block's targets sit among the low address bits, so it
+is measured: ``qsv_tune_blocks`` times every applicable mode on a scratch state for
+each placement class a plan uses, and the library keeps the fastest per device.
+
+The fusion width (largest block, 4..6 qubits) is chosen per gate list: the planner runs
+at each candidate width and each plan is priced from the measured times.  A tensor-core
+block costs its class's tuned time; any other step costs one per-gate pass weighted by
+the share of amplitudes it rewrites, where one pass is the tuned time of the k=4 block
+with every target on a high bit (one HBM pass with the least arithmetic).  Times are
+measured on min(n, 26) qubits and scaled by 2^(n - that) for an n-qubit state (every
+pass is HBM-bound at those sizes).  The cheapest width wins and is remembered per n.
+
+The caches assume one device per process, the library's own table is per device.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+from typing import Dict, Iterable, List, Optional, Sequence, Tuple
+
+import numpy
+
+from . import _native as nat
+from .fusion import Block, plan
+from .gates import GateOp
+
+SCRATCH_QUBITS = 26  # the library tunes on min(n, 26) qubits
+BATCH_BITS = 7       # a tile's group bits: targets below this change the access pattern
+MODES = ("direct", "staged", "shuffle")
+
+
+def placement_class(qubits: Sequence[int], n: int) -> Tuple[int, int]:
+    """(k, low_mask) of a block on ``qubits`` (qubit q <-> address bit n-1-q)."""
+    low = 0
+    for q in qubits:
+        b = n - 1 - q
+        if b < BATCH_BITS:
+            low |= 1 << b
+    return len(qubits), low
+
+
+def tensor_core_block(step, n: int) -> bool:
+    return isinstance(step, Block) and len(step.qubits) >= 4 and n - len(step.qubits) >= BATCH_BITS
+
+
+class Autotuner:
+    def __init__(self, reps: int = 3):
+        self.reps = int(reps)
+        self._lock = threading.Lock()
+        self._ms: Dict[Tuple[int, int, int], Tuple[List[float], int]] = {}  # (nt, k, low) -> (ms per mode, best)
+        self._width: Dict[int, int] = {}
+
+    # ---- access modes ----------------------------------------------------------------
+    def tune(self, handle, n: int, classes: Iterable[Tuple[int, int]]) -> None:
+        """Measure every class not measured yet (one library call for all of them)."""
+        nt = min(n, SCRATCH_QUBITS)
+        with self._lock:
+            todo = sorted({c for c in classes if (nt,) + tuple(c) not in self._ms})
+            if not todo:
+                return
+            lib = nat.load()
+            ks = nat.int_array([k for k, _ in todo])
+            lows = nat.int_array([low for _, low in todo])
+            ms = numpy.zeros(3 * len(todo), dtype=numpy.float64)
+            best = numpy.zeros(len(todo), dtype=numpy.int32)
+            nat.check(lib.qsv_tune_blocks(handle, len(todo), nat.ip(ks), nat.ip(lows), self.reps, nat.dp(ms),
+                                          best.ctypes.data_as(ctypes.POINTER(ctypes.c_int))),
+                      handle, "tune_blocks")
+            for i, c in enumerate(todo):
+                self._ms[(nt,) + tuple(c)] = ([float(x) for x in ms[3 * i:3 * i + 3]], int(best[i]))
+
+    def measured(self, n: int, k: int, low: int) -> Optional[Tuple[List[float], int]]:
+        return self._ms.get((min(n, SCRATCH_QUBITS), k, low))
+
+    def block_ms(self, n: int, k: int, low: int) -> float:
+        """Tuned time of one block of this class on an n-qubit state (ms)."""
+        times, best = self._ms[(min(n, SCRATCH_QUBITS), k, low)]
+        return times[best] * 2.0 ** (n - min(n, SCRATCH_QUBITS))
+
+    def ensure_plan(self, handle, n: int, steps) -> None:
+        """Tune the placement classes of the tensor-core blocks of a plan."""
+        classes = {placement_class(s.qubits, n) for s in steps if tensor_core_block(s, n)}
+        if classes:
+            self.tune(handle, n, classes)
+
+    # ---- fusion width ----------------------------------------------------------------
+    def predict_ms(self, handle, n: int, steps) -> float:
+        """Predicted device time of a plan from the measured classes."""
+        self.ensure_plan(handle, n, steps)
+        self.tune(handle, n, [(4, 0)])
+        one_pass = self.block_ms(n, 4, 0)
+        total = 0.0
+        for s in steps:
+            if tensor_core_block(s, n):
+                total += self.block_ms(n, *placement_class(s.qubits, n))
+            elif isinstance(s, Block):
+                total += one_pass
+            else:
+                total += one_pass * s.amp_update_weight()
+        return total
+
+    def candidate_widths(self, n: int, max_block: int = 6) -> List[int]:
+        return [w for w in (4, 5, 6) if w <= max_block and n - w >= BATCH_BITS]
+
+    def choose_width(self, handle, n: int, ops: Sequence[GateOp], max_block: int = 6):
+        """Plan ``ops`` at every candidate width; returns (width, steps, {width: predicted ms}).
+        The choice is remembered for n."""
+        widths = self.candidate_widths(n, max_block)
+        if not widths:
+            return 3, plan(ops, kmax=3), {}
+        best = None
+        report = {}
+        for w in widths:
+            steps = plan(ops, kmax=w)
+            ms = self.predict_ms(handle, n, steps)
+            report[w] = ms
+            if best is None or ms < best[0]:
+                best = (ms, w, steps)
+        with self._lock:
+            self._width[n] = best[1]
+        return best[1], best[2], report
+
+    def width_for(self, n: int) -> Optional[int]:
+        return self._width.get(n)
+
+
+_DEFAULT: Optional[Autotuner] = None
+
+
+def default_tuner() -> Autotuner:
+    """The process-wide tuner used by ``GpuBackend``."""
+    global _DEFAULT
+    if _DEFAULT is None:
+        _DEFAULT = Autotuner()
+    return _DEFAULT

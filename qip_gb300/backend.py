@@ -20,6 +20,7 @@ from typing import Callable, List, Mapping, Optional, Sequence, Tuple, Union
 import numpy
 
 from . import _native as nat
+from .autotune import default_tuner
 from .fusion import Block, plan, plan_prefix
 from .gates import GateOp, classify_matrix, decompose
 from .util import InitialState, IndexType, MatrixType
@@ -149,13 +150,18 @@ class GpuBackend(StateType):
     # join are launched while the executor keeps feeding gates.
     PARTIAL_FLUSH = 384
 
-    def __init__(self, n: int, handle: ctypes.c_void_p, statetype, fusion: bool, max_block: int = 6):
+    # Gates needed before the fusion width is measured on them (fewer: the static rule).
+    AUTOTUNE_MIN_GATES = 64
+
+    def __init__(self, n: int, handle: ctypes.c_void_p, statetype, fusion: bool, max_block: int = 6,
+                 autotune: bool = True):
         super().__init__(n, None)
         self._h = handle
         self._lib = nat.load()
         self.statetype = numpy.dtype(statetype)
         self.fusion = bool(fusion)
         self.max_block = int(max_block)
+        self.autotune = bool(autotune)
         self._pending: List[GateOp] = []
         self._next_partial = self.PARTIAL_FLUSH
         self.stats = {"ops": 0, "blocks": 0, "block_gates": 0, "launch_calls": 0}
@@ -166,10 +172,11 @@ class GpuBackend(StateType):
                    inputstartindex: Optional[int] = None, inputendindex: Optional[int] = None,
                    outputstartindex: Optional[int] = None, outputendindex: Optional[int] = None,
                    statetype: type = numpy.complex128, fusion: Optional[bool] = None,
-                   max_block: int = 6) -> "GpuBackend":
+                   max_block: int = 6, autotune: bool = True) -> "GpuBackend":
         """Same contract as ``CythonBackend.make_state`` (``qip/backend.py:73-104``): the
         product of the fed register vectors at their global indices, unfed qubits |0>,
-        |0...0> without feeds, no normalisation."""
+        |0...0> without feeds, no normalisation.  ``autotune`` (fusion only): measure the
+        fusion width and the block kernel's access modes (``qip_gb300.autotune``)."""
         full = 2 ** n
         for lo, hi in ((inputstartindex, inputendindex), (outputstartindex, outputendindex)):
             if (lo not in (None, 0)) or (hi not in (None, full)):
@@ -182,7 +189,7 @@ class GpuBackend(StateType):
         nat.check(lib.qsv_create(int(n), _DTYPES[dt], ctypes.byref(h)), None, "qsv_create")
         if fusion is None:
             fusion = dt == numpy.dtype(numpy.complex64)
-        st = GpuBackend(n, h, dt, fusion, max_block)
+        st = GpuBackend(n, h, dt, fusion, max_block, autotune)
         if len(feed_list) > 0:
             st._set_product(index_groups, feed_list)
         return st
@@ -242,9 +249,24 @@ class GpuBackend(StateType):
                 self.apply_op(op)
 
     def _kmax(self) -> int:
+        if self.autotune:
+            w = default_tuner().width_for(self.n)
+            if w is not None:
+                return min(w, self.max_block)
         return min(self.max_block, max(1, self.n - 7)) if self.n >= 11 else 3
 
+    def _tune_width(self) -> Optional[Tuple[int, list]]:
+        """Measure the fusion width on the queued gates once per n; returns (width, plan
+        of every queued gate at that width) when it measured now."""
+        tuner = default_tuner()
+        if (not self.autotune or tuner.width_for(self.n) is not None or len(self._pending) < self.AUTOTUNE_MIN_GATES
+                or not tuner.candidate_widths(self.n, self.max_block)):
+            return None
+        w, steps, _ = tuner.choose_width(self._h, self.n, self._pending, self.max_block)
+        return w, steps
+
     def _partial_flush(self) -> None:
+        self._tune_width()
         steps, rest = plan_prefix(self._pending, kmax=self._kmax(), nqubits=self.n)
         if steps:
             self._pending = rest
@@ -301,6 +323,8 @@ class GpuBackend(StateType):
 
     def run_plan(self, steps) -> None:
         """Execute a fusion plan: runs of tensor-core blocks go in one call."""
+        if self.autotune:
+            default_tuner().ensure_plan(self._h, self.n, steps)
         batch: List[Block] = []
         for st in steps:
             if isinstance(st, Block) and len(st.qubits) >= 4 and self.n - len(st.qubits) >= 7:
@@ -320,8 +344,9 @@ class GpuBackend(StateType):
         """Fuse and launch every queued gate."""
         if not self._pending:
             return
+        tuned = self._tune_width()
         pending, self._pending = self._pending, []
-        self.run_plan(plan(pending, kmax=self._kmax()))
+        self.run_plan(tuned[1] if tuned else plan(pending, kmax=self._kmax()))
 
     # ---- readout -------------------------------------------------------------------------
     def get_state(self) -> numpy.ndarray:

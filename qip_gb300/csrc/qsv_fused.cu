@@ -28,6 +28,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "qsv_internal.cuh"
@@ -107,7 +109,7 @@ struct BlockArgs {
   uint32_t a_it[4];     // A byte offset of register group it (registers 8*it .. 8*it+7)
   uint64_t st_lw[8];    // address contribution of lane bits 0..4, warp bits 0..1 (row quadrant), warp bit 2
   uint64_t st_reg[32];  // address offset of epilogue register c
-  uint8_t tperm[64];    // kernel target order t' -> block matrix index t (identity unless shuffle)
+  uint8_t tperm[64];    // kernel target order t' -> the caller's block matrix index
   const uint4* wimg;    // hi image then lo image (2 * W_BYTES bytes)
   int* flag;            // status word
 };
@@ -829,8 +831,15 @@ bool shuffle_tables(int k, const int* tpos, const int* batch, const int* eidx, i
 // Tile geometry of a block on target positions tpos[0..k) (tpos[0] = MSB of t):
 // sorted tile positions, the e-index maps of groups and targets, the address table
 // and the staging swizzle (see BlockArgs).
-void tile_geometry(int k, const int* tpos, BlockArgs& a) {
+// user_pos is the caller's target order (user_pos[0] = MSB of the block matrix index).
+// The kernels see the targets in descending bit order (the block matrix is permuted
+// to match through tperm), so an access mode means the same thing for every order of a
+// placement.  forced_mode >= 0 replaces the built-in rule where it applies.
+void tile_geometry(int k, const int* user_pos, BlockArgs& a, int forced_mode) {
   const int ebits = FB_BATCH_BITS + k;
+  int tpos[8];
+  for (int j = 0; j < k; ++j) tpos[j] = user_pos[j];
+  std::sort(tpos, tpos + k, [](int x, int y) { return x > y; });
   uint64_t tmask = 0;
   for (int j = 0; j < k; ++j) tmask |= 1ull << tpos[j];
   // Lanes of a warp cover address bits 0..4.  With j targets there, direct accesses
@@ -843,7 +852,10 @@ void tile_geometry(int k, const int* tpos, BlockArgs& a) {
   while (L < k && tpos[k - 1 - L] == L) ++L;
   const int jl = __builtin_popcountll(tmask & 0x1Full);
   a.vec = L >= 2 ? 4 : (L == 1 ? 2 : 1);
-  a.mode = (jl == L && L <= 2) ? MODE_DIRECT : (jl <= k - 1 ? MODE_SHUF : MODE_STAGED);
+  const int rule = (jl == L && L <= 2) ? MODE_DIRECT : (jl <= k - 1 ? MODE_SHUF : MODE_STAGED);
+  a.mode = rule;
+  if (forced_mode == MODE_DIRECT || forced_mode == MODE_STAGED) a.mode = forced_mode;
+  if (forced_mode == MODE_SHUF && jl >= 1 && jl <= k - 1) a.mode = MODE_SHUF;
   int batch[FB_BATCH_BITS];
   for (int p = 0, nb = 0; nb < FB_BATCH_BITS; ++p)
     if (!((tmask >> p) & 1ull)) batch[nb++] = p;
@@ -912,12 +924,44 @@ void tile_geometry(int k, const int* tpos, BlockArgs& a) {
       if ((y >> jj) & 1) v ^= c[4 + jj];
     a.swz[y] = (uint8_t)v;
   }
-  for (int t = 0; t < T; ++t) a.tperm[t] = (uint8_t)t;
-  if (a.mode == MODE_SHUF && !shuffle_tables(k, tpos, batch, eidx, jl, a)) a.mode = MODE_STAGED;
+  if (a.mode == MODE_SHUF && !shuffle_tables(k, user_pos, batch, eidx, jl, a)) a.mode = MODE_STAGED;
+  if (a.mode != MODE_SHUF) {
+    // Sorted index t (bit k-1-i <-> tpos[i]) -> caller's index (bit k-1-jj <-> user_pos[jj]).
+    for (int t = 0; t < T; ++t) {
+      int u = 0;
+      for (int i = 0; i < k; ++i) {
+        if (!((t >> (k - 1 - i)) & 1)) continue;
+        int jj = 0;
+        while (user_pos[jj] != tpos[i]) ++jj;
+        u |= 1 << (k - 1 - jj);
+      }
+      a.tperm[t] = (uint8_t)u;
+    }
+  }
+}
+
+// ---- measured access modes ---------------------------------------------------------------
+// Per device: the access mode to use for a placement class (k, target bits among address
+// bits 0..6), set by qsv_tune_blocks (fastest measured) or qsv_set_block_mode.
+std::mutex g_mode_mu;
+std::map<long long, int> g_modes;
+
+long long mode_key(int dev, int k, int low) { return ((long long)dev << 16) | ((long long)k << 8) | low; }
+
+int lookup_mode(int dev, int k, int low) {
+  std::lock_guard<std::mutex> lk(g_mode_mu);
+  auto it = g_modes.find(mode_key(dev, k, low));
+  return it == g_modes.end() ? -1 : it->second;
+}
+
+bool mode_applies(int k, int low, int mode) {
+  if (mode == MODE_DIRECT || mode == MODE_STAGED) return true;
+  const int j = __builtin_popcount((unsigned)low & 0x1Fu);
+  return mode == MODE_SHUF && j >= 1 && j <= k - 1;
 }
 
 template <int KQ, int MODE>
-int launch_block_variant(qsv_state* s, const BlockArgs& a) {
+int launch_block_variant(qsv_state* s, const BlockArgs& a, float2* psi) {
   using P = FB<KQ>;
   constexpr int SMEM = MODE == MODE_STAGED ? P::SMEM : P::SMEM_DIRECT;
   static bool configured = false;
@@ -933,16 +977,16 @@ int launch_block_variant(qsv_state* s, const BlockArgs& a) {
   per_sm = std::min(per_sm, 512 / P::TMEM_COLS);
   uint64_t grid = (uint64_t)std::max(1, s->sm_count) * per_sm;
   if (grid > a.ntiles) grid = a.ntiles;
-  k_block_tc<KQ, MODE><<<(unsigned)grid, FB_THREADS, SMEM, s->stream>>>((float2*)s->d_amp, a);
+  k_block_tc<KQ, MODE><<<(unsigned)grid, FB_THREADS, SMEM, s->stream>>>(psi, a);
   return check_launch(s, "block_tc");
 }
 
 template <int KQ>
-int launch_block(qsv_state* s, const BlockArgs& a) {
+int launch_block(qsv_state* s, const BlockArgs& a, float2* psi) {
   switch (a.mode) {
-    case MODE_STAGED: return launch_block_variant<KQ, MODE_STAGED>(s, a);
-    case MODE_SHUF: return launch_block_variant<KQ, MODE_SHUF>(s, a);
-    default: return launch_block_variant<KQ, MODE_DIRECT>(s, a);
+    case MODE_STAGED: return launch_block_variant<KQ, MODE_STAGED>(s, a, psi);
+    case MODE_SHUF: return launch_block_variant<KQ, MODE_SHUF>(s, a, psi);
+    default: return launch_block_variant<KQ, MODE_DIRECT>(s, a, psi);
   }
 }
 
@@ -956,12 +1000,16 @@ struct qsv_plan {
 };
 
 namespace {
-int launch_args(qsv_state* s, const BlockArgs& a) {
+int launch_args_on(qsv_state* s, const BlockArgs& a, float2* psi) {
   switch (a.k) {
-    case 4: return launch_block<4>(s, a);
-    case 5: return launch_block<5>(s, a);
-    default: return launch_block<6>(s, a);
+    case 4: return launch_block<4>(s, a, psi);
+    case 5: return launch_block<5>(s, a, psi);
+    default: return launch_block<6>(s, a, psi);
   }
+}
+
+int launch_args(qsv_state* s, const BlockArgs& a) {
+  return launch_args_on(s, a, (float2*)s->d_amp);
 }
 
 // Validates a block list and fills per-block launch arguments and image offsets.
@@ -987,7 +1035,10 @@ int prepare_blocks(qsv_state* s, int nblocks, const int* ks, const int* targets_
     if (rc) return rc;
     a.k = k;
     a.ntiles = 1ull << (s->n - k - FB_BATCH_BITS);
-    tile_geometry(k, tpos, a);
+    int low = 0;
+    for (int j = 0; j < k; ++j)
+      if (tpos[j] < FB_BATCH_BITS) low |= 1 << tpos[j];
+    tile_geometry(k, tpos, a, lookup_mode(s->device, k, low));
     a.flag = s->d_flag;
     img_off[(size_t)i] = total;
     mat_offs[(size_t)i] = mat_off;
@@ -1114,4 +1165,112 @@ extern "C" int qsv_apply_blocks(qsv_state* s, int nblocks, const int* ks, const 
     if (rc) return rc;
   }
   return QSV_OK;
+}
+
+// ---- access-mode autotuning --------------------------------------------------------------
+extern "C" int qsv_set_block_mode(qsv_state* s, int k, int low_mask, int mode) {
+  QSV_CHECK_HANDLE(s);
+  if (k < 4 || k > 6 || low_mask < 0 || low_mask >= (1 << FB_BATCH_BITS) || __builtin_popcount(low_mask) > k)
+    return set_error(s, QSV_ERR_INVALID, "bad placement class k=%d low_mask=%d", k, low_mask);
+  if (mode < -1 || mode > MODE_SHUF) return set_error(s, QSV_ERR_INVALID, "bad access mode %d", mode);
+  std::lock_guard<std::mutex> lk(g_mode_mu);
+  if (mode < 0) {
+    g_modes.erase(mode_key(s->device, k, low_mask));
+    return QSV_OK;
+  }
+  if (!mode_applies(k, low_mask, mode))
+    return set_error(s, QSV_ERR_INVALID, "mode %d does not apply to k=%d low_mask=%d", mode, k, low_mask);
+  g_modes[mode_key(s->device, k, low_mask)] = mode;
+  return QSV_OK;
+}
+
+extern "C" int qsv_tune_blocks(qsv_state* s, int count, const int* ks, const int* low_masks, int reps,
+                               double* out_ms, int* out_mode) {
+  QSV_CHECK_HANDLE(s);
+  if (count < 0 || (count > 0 && (!ks || !low_masks || !out_ms || !out_mode)) || reps < 1 || reps > 1000)
+    return set_error(s, QSV_ERR_INVALID, "bad tuning request");
+  if (count == 0) return QSV_OK;
+  const int nt = std::min(s->n, 26);
+  for (int i = 0; i < count; ++i) {
+    const int k = ks[i], low = low_masks[i];
+    if (k < 4 || k > 6 || low < 0 || low >= (1 << FB_BATCH_BITS) || __builtin_popcount(low) > k)
+      return set_error(s, QSV_ERR_INVALID, "class %d: bad placement k=%d low_mask=%d", i, k, low);
+    if (nt - (k - __builtin_popcount(low)) < FB_BATCH_BITS || nt - k < FB_BATCH_BITS)
+      return set_error(s, QSV_ERR_UNSUPPORTED, "class %d: n=%d too small to tune k=%d", i, s->n, k);
+  }
+  // Scratch state (zeros) and one identity image per k; the caller's state is untouched.
+  float2* scratch = nullptr;
+  uint8_t* dimg = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = QSV_OK;
+  const size_t sbytes = sizeof(float2) << nt;
+  const size_t ibytes = image_bytes(6);
+  std::vector<uint8_t> himg(ibytes);
+  std::vector<double> ident;
+  if (cudaMalloc(&scratch, sbytes) != cudaSuccess || cudaMalloc(&dimg, 3 * ibytes) != cudaSuccess) {
+    cudaGetLastError();
+    rc = set_error(s, QSV_ERR_OOM, "tuning scratch allocation failed");
+  }
+  if (!rc && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+    rc = set_error(s, QSV_ERR_CUDA, "event creation failed");
+  if (!rc && cudaMemsetAsync(scratch, 0, sbytes, s->stream) != cudaSuccess)
+    rc = set_error(s, QSV_ERR_CUDA, "scratch clear failed");
+  for (int k = 4; k <= 6 && !rc; ++k) {
+    const int T = 1 << k;
+    ident.assign((size_t)2 * T * T, 0.0);
+    for (int t = 0; t < T; ++t) ident[(size_t)2 * (t * T + t)] = 1.0;
+    uint8_t idperm[64];
+    for (int t = 0; t < T; ++t) idperm[t] = (uint8_t)t;
+    build_image(k, ident.data(), idperm, himg.data());
+    if (cudaMemcpy(dimg + (k - 4) * ibytes, himg.data(), image_bytes(k), cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = set_error(s, QSV_ERR_CUDA, "tuning image upload failed");
+  }
+  for (int i = 0; i < count && !rc; ++i) {
+    const int k = ks[i], low = low_masks[i];
+    int tpos[8], nt_pos = 0;
+    for (int p = FB_BATCH_BITS - 1; p >= 0; --p)
+      if ((low >> p) & 1) tpos[nt_pos++] = p;
+    for (int p = nt - 1; nt_pos < k; --p) tpos[nt_pos++] = p;
+    std::sort(tpos, tpos + k, [](int x, int y) { return x > y; });
+    double best = -1.0;
+    int best_mode = -1;
+    for (int mode = 0; mode < 3 && !rc; ++mode) {
+      out_ms[3 * i + mode] = -1.0;
+      if (!mode_applies(k, low, mode)) continue;
+      BlockArgs a{};
+      a.k = k;
+      a.ntiles = 1ull << (nt - k - FB_BATCH_BITS);
+      tile_geometry(k, tpos, a, mode);
+      if (a.mode != mode) continue;
+      a.flag = s->d_flag;
+      a.wimg = reinterpret_cast<const uint4*>(dimg + (k - 4) * ibytes);
+      rc = launch_args_on(s, a, scratch);
+      if (!rc && cudaEventRecord(e0, s->stream) != cudaSuccess) rc = set_error(s, QSV_ERR_CUDA, "event record");
+      for (int r = 0; r < reps && !rc; ++r) rc = launch_args_on(s, a, scratch);
+      if (!rc && cudaEventRecord(e1, s->stream) != cudaSuccess) rc = set_error(s, QSV_ERR_CUDA, "event record");
+      float ms = 0.0f;
+      if (!rc && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+        rc = set_error(s, QSV_ERR_CUDA, "tuning timing failed");
+      if (rc) break;
+      const double per = (double)ms / reps;
+      out_ms[3 * i + mode] = per;
+      if (best < 0.0 || per < best) {
+        best = per;
+        best_mode = mode;
+      }
+    }
+    out_mode[i] = best_mode;
+    if (!rc && best_mode >= 0) {
+      std::lock_guard<std::mutex> lk(g_mode_mu);
+      g_modes[mode_key(s->device, k, low)] = best_mode;
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (scratch || dimg) {
+    cudaStreamSynchronize(s->stream);
+    if (scratch) cudaFree(scratch);
+    if (dimg) cudaFree(dimg);
+  }
+  return rc;
 }

@@ -188,3 +188,37 @@ def test_incremental_plan_equals_full_plan():
             numpy.testing.assert_allclose(a.matrix, b.matrix, atol=1e-13)
         else:
             assert a is b
+
+
+def _synthetic_tuner(cost):
+    from qip_gb300.autotune import Autotuner
+
+    t = Autotuner()
+    for k in (4, 5, 6):
+        for low in range(128):
+            if bin(low).count("1") <= k:
+                ms = cost(k, low)
+                t._ms[(20, k, low)] = ([ms, ms * 1.5, -1.0], 0)
+    return t
+
+
+def test_autotuner_prices_plans_and_picks_the_cheapest_width():
+    from qip_gb300.autotune import placement_class
+
+    n = 20
+    assert placement_class((19, 18, 0), n) == (3, 0b11)
+    assert placement_class((0, 1, 2, 3), n) == (4, 0)
+    ops = [op for g in circuits.brickwork(n, 8, seed=3) for op in gates.decompose(g)]
+    # Every pass costs the same: the widest blocks (fewest passes) win.
+    t = _synthetic_tuner(lambda k, low: 1.0)
+    w, steps, report = t.choose_width(None, n, ops)
+    assert w == 6 and set(report) == {4, 5, 6} and report[6] == min(report.values())
+    assert report[6] == pytest.approx(sum(1.0 if isinstance(s, fusion.Block) else s.amp_update_weight()
+                                          for s in steps))
+    # Wide blocks made expensive: a narrower width wins and is remembered for n.
+    t = _synthetic_tuner(lambda k, low: 1.0 if k == 4 else 50.0)
+    w, _, report = t.choose_width(None, n, ops)
+    assert w == 4 and t.width_for(n) == 4
+    # Times measured on 26 qubits scale to larger states.
+    t._ms[(26, 6, 0)] = ([2.0, 3.0, -1.0], 0)
+    assert t.block_ms(30, 6, 0) == pytest.approx(32.0)
