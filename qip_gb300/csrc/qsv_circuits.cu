@@ -5,8 +5,17 @@
 // first, so the tail of the launch is short.  A circuit of n <= 14 qubits lives entirely
 // in shared memory (2^14 complex64 = 128 KiB): its product-state input is built there
 // from the per-qubit feeds, every gate is applied there, and the final state is
-// written to global memory once.  Larger circuits (n <= 24) are built and updated in
-// their global output slot, one CTA-wide pass per gate.  Each circuit records device
+// written to global memory once.
+//
+// Larger circuits (15 <= n <= 24) are streamed through the same shared buffer by
+// segments.  The host cuts the gate list into maximal runs whose qubits, together with
+// address bits 0..4, fit in 14 bit positions (the segment's local set, completed from
+// the lowest remaining positions) and rewrites those gates' qubits as local indices.
+// For each segment the CTA gathers every chunk of 2^14 amplitudes (fixed values of the
+// other n-14 bits; lanes walk address bits 0..4, so accesses stay coalesced) into
+// shared memory, applies the segment's gates there and scatters the chunk back: one
+// pass over the state per segment instead of one per gate.  The first segment builds
+// its chunks from the feeds instead of reading them.  Each circuit records device
 // timestamps (%globaltimer) when its CTA starts and finishes it.
 //
 // The launch (counter reset + kernel) is captured once into a CUDA graph owned by the
@@ -33,8 +42,19 @@ enum GateKind : int32_t { G_DENSE1 = 0, G_PHASE1 = 1, G_X = 2, G_CX = 3, G_CSWAP
 // Record layouts qsv_gate_rec / qsv_circuit_rec are declared in include/qsv.h
 // (mirrored by qip_gb300/batch.py).
 
+namespace {
+// One segment of a streamed circuit (see above): its gates and its local bit positions.
+struct SegmentRec {
+  int32_t gate_begin, gate_end;  // absolute indices into the gate array
+  int32_t lpos[CB_SMEM_QUBITS];  // ascending; lpos[0..4] = 0..4
+};
+static_assert(sizeof(SegmentRec) == 64, "segment record layout");
+}  // namespace
+
 struct qsv_circuits {
   int ncirc = 0;
+  SegmentRec* d_segs = nullptr;
+  int2* d_segidx = nullptr;  // per circuit: [first, last) segment (streamed circuits only)
   qsv_gate_rec* d_gates = nullptr;
   qsv_circuit_rec* d_circs = nullptr;
   float2* d_feeds = nullptr;
@@ -144,10 +164,64 @@ __device__ __forceinline__ void build_product(float2* v, int n, const float2* fe
   }
 }
 
+// Streams a circuit of n > 14 qubits through the shared buffer segment by segment.
+__device__ void run_segments(float2* sv, float2* out, int n, const qsv_gate_rec* gates, const SegmentRec* segs,
+                             int2 range, const float2* feed) {
+  __shared__ uint64_t dlo[128], dhi[128];  // address offset of chunk element bits 0..6 / 7..13
+  constexpr int CHUNK = 1 << CB_SMEM_QUBITS;
+  const uint64_t nchunks = 1ull << (n - CB_SMEM_QUBITS);
+  for (int si = range.x; si < range.y; ++si) {
+    const SegmentRec sg = segs[si];
+    if (threadIdx.x < 128) {
+      uint64_t lo = 0, hi = 0;
+      for (int b = 0; b < 7; ++b)
+        if ((threadIdx.x >> b) & 1) {
+          lo |= 1ull << sg.lpos[b];
+          hi |= 1ull << sg.lpos[7 + b];
+        }
+      dlo[threadIdx.x] = lo;
+      dhi[threadIdx.x] = hi;
+    }
+    __syncthreads();
+    for (uint64_t ch = 0; ch < nchunks; ++ch) {
+      const uint64_t base = qsv_insert_zeros(ch, sg.lpos, CB_SMEM_QUBITS);
+      if (si == range.x) {
+        for (int e = threadIdx.x; e < CHUNK; e += blockDim.x) {
+          const uint64_t i = base + dlo[e & 127] + dhi[e >> 7];
+          float2 acc = make_float2(1.f, 0.f);
+          for (int q = 0; q < n; ++q) acc = qsv_cmul(acc, feed[2 * q + ((i >> (n - 1 - q)) & 1ull)]);
+          sv[e] = acc;
+        }
+      } else {
+        // All of a thread's loads issued before the first shared store (the gather is
+        // latency-bound: one chunk in flight per SM).
+        constexpr int PER = CHUNK / CB_THREADS;
+        float2 t[PER];
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+          const int e = threadIdx.x + j * CB_THREADS;
+          t[j] = out[base + dlo[e & 127] + dhi[e >> 7]];
+        }
+#pragma unroll
+        for (int j = 0; j < PER; ++j) sv[threadIdx.x + j * CB_THREADS] = t[j];
+      }
+      __syncthreads();
+      for (int k = sg.gate_begin; k < sg.gate_end; ++k) {
+        const qsv_gate_rec g = gates[k];
+        apply_gate(sv, CB_SMEM_QUBITS, g);
+        __syncthreads();
+      }
+#pragma unroll 8
+      for (int e = threadIdx.x; e < CHUNK; e += blockDim.x) out[base + dlo[e & 127] + dhi[e >> 7]] = sv[e];
+      __syncthreads();
+    }
+  }
+}
+
 __global__ void __launch_bounds__(CB_THREADS, 1)
     k_circuits(const qsv_gate_rec* __restrict__ gates, const qsv_circuit_rec* __restrict__ circs, int ncirc,
                float2* __restrict__ states, const float2* __restrict__ feeds, unsigned long long* __restrict__ times,
-               int* __restrict__ counter) {
+               int* __restrict__ counter, const SegmentRec* __restrict__ segs, const int2* __restrict__ segidx) {
   extern __shared__ float2 sv[];
   __shared__ int cur;
   for (;;) {
@@ -160,18 +234,18 @@ __global__ void __launch_bounds__(CB_THREADS, 1)
     if (threadIdx.x == 0) times[2 * (size_t)c] = gtimer();
     const qsv_gate_rec* gl = gates + cr.gate_offset;
     float2* out = states + cr.state_offset;
-    const bool local = cr.n <= CB_SMEM_QUBITS;
-    float2* v = local ? sv : out;
-    build_product(v, cr.n, feeds + cr.feed_offset);
-    __syncthreads();
-    for (int k = 0; k < cr.ngates; ++k) {
-      const qsv_gate_rec g = gl[k];
-      apply_gate(v, cr.n, g);
+    if (cr.n <= CB_SMEM_QUBITS) {
+      build_product(sv, cr.n, feeds + cr.feed_offset);
       __syncthreads();
-    }
-    if (local) {
+      for (int k = 0; k < cr.ngates; ++k) {
+        const qsv_gate_rec g = gl[k];
+        apply_gate(sv, cr.n, g);
+        __syncthreads();
+      }
       const uint64_t total = 1ull << cr.n;
       for (uint64_t i = threadIdx.x; i < total; i += blockDim.x) out[i] = sv[i];
+    } else {
+      run_segments(sv, out, cr.n, gates, segs, segidx[c], feeds + cr.feed_offset);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -191,7 +265,7 @@ int capture(qsv_circuits* b, cudaStream_t stream) {
   cudaMemsetAsync(b->d_counter, 0, sizeof(int), stream);
   const int grid = std::min(b->ncirc, std::max(1, b->sm_count));
   k_circuits<<<grid, CB_THREADS, smem, stream>>>(b->d_gates, b->d_circs, b->ncirc, b->d_states, b->d_feeds,
-                                                 b->d_times, b->d_counter);
+                                                 b->d_times, b->d_counter, b->d_segs, b->d_segidx);
   cudaError_t le = cudaGetLastError();
   e = cudaStreamEndCapture(stream, &g);
   if (le != cudaSuccess || e != cudaSuccess) {
@@ -238,6 +312,49 @@ int qsv_circuits_create(const void* gates, int64_t ngates, const void* circuits,
             return set_error(nullptr, QSV_ERR_INVALID, "circuit %d gate %lld: repeated qubit", c, (long long)k);
     }
   }
+  // Segments of the streamed circuits; their gates are rewritten to local indices.
+  std::vector<qsv_gate_rec> gv(gr, gr + ngates);
+  std::vector<SegmentRec> segs;
+  std::vector<int2> segidx((size_t)ncirc, make_int2(0, 0));
+  for (int c = 0; c < ncirc; ++c) {
+    const qsv_circuit_rec& r = cr[c];
+    if (r.n <= CB_SMEM_QUBITS) continue;
+    segidx[(size_t)c].x = (int)segs.size();
+    int64_t i = r.gate_offset;
+    const int64_t end = r.gate_offset + r.ngates;
+    do {
+      uint32_t set = 0x1Fu;  // address bits 0..4 stay local (coalesced chunk accesses)
+      int64_t j = i;
+      for (; j < end; ++j) {
+        const qsv_gate_rec& g = gv[(size_t)j];
+        const int need = g.kind == G_CX ? 2 : (g.kind == G_CSWAP ? 3 : 1);
+        const int qs[3] = {g.q0, g.q1, g.q2};
+        uint32_t gm = 0;
+        for (int t = 0; t < need; ++t) gm |= 1u << (r.n - 1 - qs[t]);
+        if (__builtin_popcount(set | gm) > CB_SMEM_QUBITS) break;
+        set |= gm;
+      }
+      for (int p = 0; p < r.n && __builtin_popcount(set) < CB_SMEM_QUBITS; ++p) set |= 1u << p;
+      SegmentRec sg;
+      sg.gate_begin = (int32_t)i;
+      sg.gate_end = (int32_t)j;
+      int local_of[32];
+      for (int p = 0, li = 0; p < r.n; ++p)
+        if ((set >> p) & 1u) {
+          sg.lpos[li] = p;
+          local_of[p] = li++;
+        }
+      for (int64_t k = i; k < j; ++k) {
+        qsv_gate_rec& g = gv[(size_t)k];
+        const int need = g.kind == G_CX ? 2 : (g.kind == G_CSWAP ? 3 : 1);
+        int* qs[3] = {&g.q0, &g.q1, &g.q2};
+        for (int t = 0; t < need; ++t) *qs[t] = CB_SMEM_QUBITS - 1 - local_of[r.n - 1 - *qs[t]];
+      }
+      segs.push_back(sg);
+      i = j;
+    } while (i < end);
+    segidx[(size_t)c].y = (int)segs.size();
+  }
   auto* b = new (std::nothrow) qsv_circuits();
   if (!b) return set_error(nullptr, QSV_ERR_OOM, "host allocation failed");
   b->ncirc = ncirc;
@@ -251,9 +368,15 @@ int qsv_circuits_create(const void* gates, int64_t ngates, const void* circuits,
             cudaMalloc(&b->d_feeds, std::max<int64_t>(1, nfeeds) * sizeof(float2)) == cudaSuccess &&
             cudaMalloc(&b->d_states, amps * sizeof(float2)) == cudaSuccess &&
             cudaMalloc(&b->d_times, 2 * (size_t)ncirc * sizeof(unsigned long long)) == cudaSuccess &&
-            cudaMalloc(&b->d_counter, sizeof(int)) == cudaSuccess;
+            cudaMalloc(&b->d_counter, sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&b->d_segs, std::max<size_t>(1, segs.size()) * sizeof(SegmentRec)) == cudaSuccess &&
+            cudaMalloc(&b->d_segidx, (size_t)ncirc * sizeof(int2)) == cudaSuccess;
   if (ok)
-    ok = cudaMemcpy(b->d_gates, gates, ngates * sizeof(qsv_gate_rec), cudaMemcpyHostToDevice) == cudaSuccess &&
+    ok = cudaMemcpy(b->d_gates, gv.data(), ngates * sizeof(qsv_gate_rec), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(b->d_segidx, segidx.data(), (size_t)ncirc * sizeof(int2), cudaMemcpyHostToDevice) ==
+             cudaSuccess &&
+         (segs.empty() || cudaMemcpy(b->d_segs, segs.data(), segs.size() * sizeof(SegmentRec),
+                                     cudaMemcpyHostToDevice) == cudaSuccess) &&
          cudaMemcpy(b->d_circs, circuits, ncirc * sizeof(qsv_circuit_rec), cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(b->d_feeds, feeds, nfeeds * sizeof(float2), cudaMemcpyHostToDevice) == cudaSuccess;
   if (!ok) {
@@ -308,6 +431,8 @@ int qsv_circuits_destroy(qsv_circuits* b) {
   cudaFree(b->d_states);
   cudaFree(b->d_times);
   cudaFree(b->d_counter);
+  cudaFree(b->d_segs);
+  cudaFree(b->d_segidx);
   delete b;
   return QSV_OK;
 }

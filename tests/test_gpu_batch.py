@@ -30,3 +30,31 @@ def test_batched_circuits_match_oracle():
         assert numpy.all(lat > 0)
     finally:
         b.close()
+
+
+def test_streamed_circuits_many_segments_match_oracle():
+    """Circuits of 17..20 qubits (streamed through shared memory in segments of 14
+    local bits, up to 64 chunks per segment), one without gates, mixed with small ones."""
+    import torch
+
+    from qip_gb300.circuits import random_circuit, random_product_feed
+
+    rng = numpy.random.default_rng(77)
+    circs, feeds, sizes = [], [], []
+    for n, depth in ((20, 100), (19, 80), (17, 60), (18, 0), (9, 40), (14, 50)):
+        circs.append(random_circuit(rng, n, depth))
+        feeds.append(random_product_feed(rng, n))
+        sizes.append(n)
+    b = batch.CircuitBatch(circs, feeds, sizes)
+    stream = torch.cuda.Stream()
+    try:
+        b.run(stream.cuda_stream)
+        stream.synchronize()
+        for i, (gl, f, n) in enumerate(zip(circs, feeds, sizes)):
+            want = sv.make_state(n, [[q] for q in range(n)], f)
+            for g in gl:
+                want = sv.kronselect_dot(g, want, n)
+            err = numpy.max(numpy.abs(b.state(i) - want))
+            assert err < 2e-5, (i, n, err)
+    finally:
+        b.close()
