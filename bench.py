@@ -515,6 +515,24 @@ def run_qft16(args):
     print(json.dumps(res), flush=True)
 
 
+def op_touched(op, n: int) -> float:
+    """Amplitudes a per-gate pass rewrites: its control-satisfied subspace, restricted to
+    the entries that are not the identity (diagonal: entries != 1; monomial: rows that
+    move or change phase; swap: the a != b half, 1 - 2^-m of the subspace)."""
+    sub = 2.0 ** (n - len(op.controls))
+    k = len(op.targets)
+    if op.kind == "diag":
+        d = numpy.asarray(op.mat)
+        return sub * numpy.count_nonzero(d != 1) / d.size
+    if op.kind == "mono":
+        perm, ph = numpy.asarray(op.perm), numpy.asarray(op.mat)
+        moved = numpy.count_nonzero((perm != numpy.arange(perm.size)) | (ph != 1))
+        return sub * moved / perm.size
+    if op.kind == "swap":
+        return sub * (1.0 - 2.0 ** (-k))
+    return sub
+
+
 def run_hbm(args):
     """QFT + 8 amplitude-amplification iterations at n=32 complex64 (fused) and n=31
     complex128 (per-gate); all single-qubit marginals; per-pass achieved GB/s.  Checked
@@ -558,7 +576,7 @@ def run_hbm(args):
             else:
                 st.apply_op(stp)
                 kind = f"{stp.kind}{len(stp.targets)}c{len(stp.controls)}"
-                touched = 2 ** (n - len(stp.controls)) if stp.kind != "diag" else 2 ** (n - len(stp.controls) - len(stp.targets))
+                touched = op_touched(stp, n)
             b.record(stream)
             per_kind.setdefault(kind, []).append((a, b, touched))
         t_all1.record(stream)
@@ -803,6 +821,8 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--depth", type=int, default=DEPTH_DEFAULT)
     ap.add_argument("--kmax", type=int, default=0, help="fusion width; 0 = measured by the autotuner")
+    ap.add_argument("--tune-cache", default=None,
+                    help="JSON file of autotuner decisions: loaded if present, written after tuning")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--parts", default="fused,plain,e2e,cpu",
@@ -815,6 +835,8 @@ def main():
     ap.add_argument("--adj-layers", type=int, default=20)
     ap.add_argument("--adj-batch", type=int, default=64)
     args = ap.parse_args()
+    if args.tune_cache:
+        os.environ["QSV_TUNE_CACHE"] = args.tune_cache
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "brickwork":

@@ -15,10 +15,18 @@ measured on min(n, 26) qubits and scaled by 2^(n - that) for an n-qubit state (e
 pass is HBM-bound at those sizes).  The cheapest width wins and is remembered per n.
 
 The caches assume one device per process, the library's own table is per device.
+Decisions can be kept in a JSON file (``Autotuner(cache_path=...)``, or the
+``QSV_TUNE_CACHE`` environment variable for the process-wide tuner): a tuner that loads
+one pins the stored modes in the library before its first launch and reuses the stored
+widths, so later processes run exactly the same kernels without measuring again (also
+under a profiler, whose per-launch overhead would distort new measurements).  A cache
+file belongs to one GPU model.
 """
 from __future__ import annotations
 
 import ctypes
+import json
+import os
 import threading
 from typing import Dict, Iterable, List, Optional, Sequence, Tuple
 
@@ -48,17 +56,54 @@ def tensor_core_block(step, n: int) -> bool:
 
 
 class Autotuner:
-    def __init__(self, reps: int = 3):
+    def __init__(self, reps: int = 3, cache_path: Optional[str] = None):
         self.reps = int(reps)
-        self._lock = threading.Lock()
+        self.cache_path = cache_path
+        self._lock = threading.RLock()
         self._ms: Dict[Tuple[int, int, int], Tuple[List[float], int]] = {}  # (nt, k, low) -> (ms per mode, best)
         self._width: Dict[int, int] = {}
+        self._reports: Dict[int, Dict[int, float]] = {}
+        self._unpinned: List[Tuple[int, int, int]] = []  # loaded (k, low, mode) not yet set in the library
+        if cache_path and os.path.exists(cache_path):
+            self._load(cache_path)
+
+    # ---- persistence -----------------------------------------------------------------
+    def _load(self, path: str) -> None:
+        with open(path) as f:
+            d = json.load(f)
+        for nt, k, low, m0, m1, m2, best in d.get("classes", []):
+            self._ms[(int(nt), int(k), int(low))] = ([float(m0), float(m1), float(m2)], int(best))
+            self._unpinned.append((int(k), int(low), int(best)))
+        self._width = {int(n): int(w) for n, w in d.get("widths", {}).items()}
+        self._reports = {int(n): {int(w): float(ms) for w, ms in r.items()} for n, r in d.get("reports", {}).items()}
+
+    def _save(self) -> None:
+        if not self.cache_path:
+            return
+        d = {"classes": [[nt, k, low] + times + [best] for (nt, k, low), (times, best) in sorted(self._ms.items())],
+             "widths": {str(n): w for n, w in self._width.items()},
+             "reports": {str(n): {str(w): ms for w, ms in r.items()} for n, r in self._reports.items()}}
+        tmp = self.cache_path + ".tmp"
+        os.makedirs(os.path.dirname(os.path.abspath(self.cache_path)), exist_ok=True)
+        with open(tmp, "w") as f:
+            json.dump(d, f)
+        os.replace(tmp, self.cache_path)
+
+    def _pin_loaded(self, handle) -> None:
+        """Set the modes read from the cache in the library (once)."""
+        if not self._unpinned:
+            return
+        lib = nat.load()
+        for k, low, mode in self._unpinned:
+            nat.check(lib.qsv_set_block_mode(handle, k, low, mode), handle, "set_block_mode")
+        self._unpinned = []
 
     # ---- access modes ----------------------------------------------------------------
     def tune(self, handle, n: int, classes: Iterable[Tuple[int, int]]) -> None:
         """Measure every class not measured yet (one library call for all of them)."""
         nt = min(n, SCRATCH_QUBITS)
         with self._lock:
+            self._pin_loaded(handle)
             todo = sorted({c for c in classes if (nt,) + tuple(c) not in self._ms})
             if not todo:
                 return
@@ -72,6 +117,7 @@ class Autotuner:
                       handle, "tune_blocks")
             for i, c in enumerate(todo):
                 self._ms[(nt,) + tuple(c)] = ([float(x) for x in ms[3 * i:3 * i + 3]], int(best[i]))
+            self._save()
 
     def measured(self, n: int, k: int, low: int) -> Optional[Tuple[List[float], int]]:
         return self._ms.get((min(n, SCRATCH_QUBITS), k, low))
@@ -112,6 +158,12 @@ class Autotuner:
         widths = self.candidate_widths(n, max_block)
         if not widths:
             return 3, plan(ops, kmax=3), {}
+        if self._width.get(n) in widths and n in self._reports:
+            # Decided before (this process or a loaded cache): reuse it.
+            w = self._width[n]
+            steps = plan(ops, kmax=w)
+            self.ensure_plan(handle, n, steps)
+            return w, steps, dict(self._reports[n])
         best = None
         report = {}
         for w in widths:
@@ -122,6 +174,8 @@ class Autotuner:
                 best = (ms, w, steps)
         with self._lock:
             self._width[n] = best[1]
+            self._reports[n] = dict(report)
+            self._save()
         return best[1], best[2], report
 
     def width_for(self, n: int) -> Optional[int]:
@@ -135,5 +189,5 @@ def default_tuner() -> Autotuner:
     """The process-wide tuner used by ``GpuBackend``."""
     global _DEFAULT
     if _DEFAULT is None:
-        _DEFAULT = Autotuner()
+        _DEFAULT = Autotuner(cache_path=os.environ.get("QSV_TUNE_CACHE") or None)
     return _DEFAULT

@@ -56,7 +56,8 @@ struct FB {
   static constexpr int W_LBO = KD * 16;
   static constexpr int VEC = TILE / 2 / FB_THREADS;             // float4 (2 amplitudes) per thread
   static constexpr int ITEMS = (FB_M * (T / 8)) / FB_THREADS;  // (b, 8 targets) per thread
-  static constexpr int TMEM_COLS = KD < 32 ? 32 : KD;
+  static constexpr int TMEM_COLS = KD < 32 ? 32 : KD;       // one accumulator
+  static constexpr int TMEM_COLS2 = 2 * KD < 32 ? 32 : 2 * KD;  // two (shuffle mode)
   static constexpr int COLS_PER_WARP = T / 2;  // output targets handled per warp
   // Tables: eb[128] u16, et[T] u16, swz[TILE/16] u8, dephi[T] u64; then the mbarrier.
   static constexpr int TAB_BYTES = FB_M * 2 + T * 2 + TILE / 16 + T * 8;
@@ -289,9 +290,11 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   uint16_t* et = eb + FB_M;
   uint8_t* swz = reinterpret_cast<uint8_t*>(et + P::T);
   uint64_t* dephi = reinterpret_cast<uint64_t*>(swz + P::TILE / 16);
+  // Tail: two mbarriers (one per accumulator), the TMEM address, the abort flag.
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + SMEM_USED - 64);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 2);
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+  constexpr int TCOLS = SHUF ? P::TMEM_COLS2 : P::TMEM_COLS;
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
@@ -312,12 +315,13 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   for (int i = tid; i < P::TILE / 16; i += FB_THREADS) swz[i] = a.swz[i];
   if (tid == 0) {
     mbar_init(smem_u32(mbar), 1);
+    mbar_init(smem_u32(mbar + 1), 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"((uint32_t)P::TMEM_COLS)
+                 "r"((uint32_t)TCOLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -326,9 +330,8 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t bar = smem_u32(mbar);
+  auto bar_of = [&](int s) -> uint32_t { return smem_u32(mbar + s); };
   constexpr uint32_t idesc = make_idesc(FB_M, P::KD);
-  uint32_t phase = 0;
 
   auto slot = [&](int e) -> int { return e ^ ((int)swz[e >> 4] << 1); };
   auto dep = [&](int e) -> uint64_t { return (uint64_t)(e & (FB_M - 1)) + dephi[e >> FB_BATCH_BITS]; };
@@ -407,216 +410,292 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
     }
   };
 
-  uint64_t tile = blockIdx.x;
-  uint64_t base = 0;
-  if (tile < a.ntiles) {
-    base = qsv_insert_zeros(tile, a.ptile, P::EBITS);
-    load_tile(base);
-  }
-  for (; tile < a.ntiles; tile += gridDim.x) {
-    // 1. Stage the tile in address order.
-    if constexpr (STAGED) {
-#pragma unroll
-      for (int u = 0; u < P::VEC; ++u) {
-        const int e = 2 * (u * FB_THREADS + tid);
-        raw4[slot(e) >> 1] = buf[u];
+  // Tile i of this CTA accumulates in TMEM columns [acc(i), acc(i) + KD).  The shuffle
+  // mode alternates two accumulators: the products of tile i run while the epilogue of
+  // tile i-1 drains the other one, and the only wait per tile is for the products of
+  // tile i-1 (issued a whole iteration earlier) before A is rewritten; that hides the
+  // products behind its heavier epilogue.  The direct and staged modes keep one
+  // accumulator and wait for the products right after prefetching the next tile: the
+  // wait gives those loads a head start, which matters more to them (measured: the
+  // direct mode is bound by loads in flight, not by the serial chain), and the staged
+  // mode shares its staging buffer between the operand and the epilogue.
+  auto write_a = [&]() {
+      // 1. Stage the tile in address order.
+      if constexpr (STAGED) {
+  #pragma unroll
+        for (int u = 0; u < P::VEC; ++u) {
+          const int e = 2 * (u * FB_THREADS + tid);
+          raw4[slot(e) >> 1] = buf[u];
+        }
+        __syncthreads();
       }
-      __syncthreads();
-    }
-    // 2. Transpose into the A operand: row b, K = [Re t | Im t], bf16 hi/lo split.
-    if constexpr (SHUF) {
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        if (i < a.nld) {
-          const int lb = a.ld_lane[i];
-          const bool up = (lane >> lb) & 1;
-#pragma unroll
-          for (int r = 0; r < R; ++r) {
-            if (r & (1 << i)) continue;
-            const int r1 = r | (1 << i);
-            const float2 send = up ? v[r] : v[r1];
-            float2 got;
-            got.x = __shfl_xor_sync(0xffffffffu, send.x, 1 << lb);
-            got.y = __shfl_xor_sync(0xffffffffu, send.y, 1 << lb);
-            if (up)
-              v[r] = got;
-            else
-              v[r1] = got;
+      // 2. Transpose into the A operand: row b, K = [Re t | Im t], bf16 hi/lo split.
+      if constexpr (SHUF) {
+  #pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          if (i < a.nld) {
+            const int lb = a.ld_lane[i];
+            const bool up = (lane >> lb) & 1;
+  #pragma unroll
+            for (int r = 0; r < R; ++r) {
+              if (r & (1 << i)) continue;
+              const int r1 = r | (1 << i);
+              const float2 send = up ? v[r] : v[r1];
+              float2 got;
+              got.x = __shfl_xor_sync(0xffffffffu, send.x, 1 << lb);
+              got.y = __shfl_xor_sync(0xffffffffu, send.y, 1 << lb);
+              if (up)
+                v[r] = got;
+              else
+                v[r1] = got;
+            }
           }
         }
+  #pragma unroll
+        for (int it = 0; it < R / 8; ++it) {
+          float re[8], im[8];
+  #pragma unroll
+          for (int g = 0; g < 8; ++g) {
+            re[g] = v[8 * it + g].x;
+            im[g] = v[8 * it + g].y;
+          }
+          uint4 rh, rl, ih, il;
+          split8(re, rh, rl);
+          split8(im, ih, il);
+          const uint32_t off_re = a_lw + a.a_it[it];
+          const uint32_t off_im = off_re + (P::T / 8) * P::A_LBO;
+          *reinterpret_cast<uint4*>(sA_hi + off_re) = rh;
+          *reinterpret_cast<uint4*>(sA_lo + off_re) = rl;
+          *reinterpret_cast<uint4*>(sA_hi + off_im) = ih;
+          *reinterpret_cast<uint4*>(sA_lo + off_im) = il;
+        }
       }
-#pragma unroll
-      for (int it = 0; it < R / 8; ++it) {
+  #pragma unroll
+      for (int it = 0; it < (SHUF ? 0 : P::ITEMS); ++it) {
+        const int item = it * FB_THREADS + tid;
+        const int b = item & (FB_M - 1);
+        const int tg = item >> FB_BATCH_BITS;
+        const int eb_ = eb[b];
         float re[8], im[8];
-#pragma unroll
-        for (int g = 0; g < 8; ++g) {
-          re[g] = v[8 * it + g].x;
-          im[g] = v[8 * it + g].y;
+  #pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const float2 v = STAGED ? raw[slot(eb_ | et[tg * 8 + j])] : buf2[it][j];
+          re[j] = v.x;
+          im[j] = v.y;
         }
         uint4 rh, rl, ih, il;
         split8(re, rh, rl);
         split8(im, ih, il);
-        const uint32_t off_re = a_lw + a.a_it[it];
-        const uint32_t off_im = off_re + (P::T / 8) * P::A_LBO;
+        const int off_re = tg * P::A_LBO + b * 16;
+        const int off_im = (P::T / 8 + tg) * P::A_LBO + b * 16;
         *reinterpret_cast<uint4*>(sA_hi + off_re) = rh;
         *reinterpret_cast<uint4*>(sA_lo + off_re) = rl;
         *reinterpret_cast<uint4*>(sA_hi + off_im) = ih;
         *reinterpret_cast<uint4*>(sA_lo + off_im) = il;
       }
-    }
-#pragma unroll
-    for (int it = 0; it < (SHUF ? 0 : P::ITEMS); ++it) {
-      const int item = it * FB_THREADS + tid;
-      const int b = item & (FB_M - 1);
-      const int tg = item >> FB_BATCH_BITS;
-      const int eb_ = eb[b];
-      float re[8], im[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const float2 v = STAGED ? raw[slot(eb_ | et[tg * 8 + j])] : buf2[it][j];
-        re[j] = v.x;
-        im[j] = v.y;
-      }
-      uint4 rh, rl, ih, il;
-      split8(re, rh, rl);
-      split8(im, ih, il);
-      const int off_re = tg * P::A_LBO + b * 16;
-      const int off_im = (P::T / 8 + tg) * P::A_LBO + b * 16;
-      *reinterpret_cast<uint4*>(sA_hi + off_re) = rh;
-      *reinterpret_cast<uint4*>(sA_lo + off_re) = rl;
-      *reinterpret_cast<uint4*>(sA_hi + off_im) = ih;
-      *reinterpret_cast<uint4*>(sA_lo + off_im) = il;
-    }
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    // 3. Three split-bf16 products into TMEM.
+  };
+  auto issue_mma = [&](uint32_t acc, uint32_t barrier) {
     if (tid == 0) {
       const uint32_t a_hi = smem_u32(sA_hi), a_lo = smem_u32(sA_lo);
       const uint32_t w_hi = smem_u32(sW_hi), w_lo = smem_u32(sW_lo);
       constexpr int KSTEPS = P::KD / 16;
 #pragma unroll
       for (int s = 0; s < KSTEPS; ++s)
-        tc_mma(tmem, make_smem_desc(a_hi + s * 2 * P::A_LBO, P::A_LBO, 128),
+        tc_mma(acc, make_smem_desc(a_hi + s * 2 * P::A_LBO, P::A_LBO, 128),
                make_smem_desc(w_hi + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, s > 0 ? 1u : 0u);
 #pragma unroll
       for (int s = 0; s < KSTEPS; ++s)
-        tc_mma(tmem, make_smem_desc(a_hi + s * 2 * P::A_LBO, P::A_LBO, 128),
+        tc_mma(acc, make_smem_desc(a_hi + s * 2 * P::A_LBO, P::A_LBO, 128),
                make_smem_desc(w_lo + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, 1u);
 #pragma unroll
       for (int s = 0; s < KSTEPS; ++s)
-        tc_mma(tmem, make_smem_desc(a_lo + s * 2 * P::A_LBO, P::A_LBO, 128),
+        tc_mma(acc, make_smem_desc(a_lo + s * 2 * P::A_LBO, P::A_LBO, 128),
                make_smem_desc(w_hi + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, 1u);
-      tc_commit(bar);
+      tc_commit(barrier);
     }
-    // 4. Prefetch the next tile while the tensor cores work.
-    const uint64_t next = tile + gridDim.x;
-    uint64_t next_base = 0;
-    if (next < a.ntiles) {
-      next_base = qsv_insert_zeros(next, a.ptile, P::EBITS);
-      load_tile(next_base);
-    }
-    if (!mbar_wait_bounded(bar, phase)) atomicExch(abort_flag, 1);
-    phase ^= 1u;
-    tc_fence_after();
-    __syncthreads();
-    if (*abort_flag) break;
-    // 5. Epilogue: TMEM lane b -> the staging buffer.  Warp w reads lanes 32*(w%4)..
-    //    and output targets [h*T/2, (h+1)*T/2) with h = w/4.
-    if constexpr (SHUF) {
-      constexpr int CHS = P::COLS_PER_WARP;
-      const int q = warp & 3;
-      const int h = warp >> 2;
-      const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
-      float re[CHS], im[CHS];
-      tmem_ld<CHS>(lane_addr + (uint32_t)(h * CHS), re);
-      tmem_ld<CHS>(lane_addr + (uint32_t)(P::T + h * CHS), im);
-      tmem_ld_wait();
-#pragma unroll
-      for (int i = 0; i < 5; ++i) {
-        if (i < KQ - 1 && i < a.nst) {
-          const int lb = a.st_lane[i];
-          const bool up = (lane >> lb) & 1;
-#pragma unroll
-          for (int c = 0; c < CHS; ++c) {
-            if (c & (1 << i)) continue;
-            const int c1 = c | (1 << i);
-            const float sr = up ? re[c] : re[c1];
-            const float si = up ? im[c] : im[c1];
-            const float gr = __shfl_xor_sync(0xffffffffu, sr, 1 << lb);
-            const float gi = __shfl_xor_sync(0xffffffffu, si, 1 << lb);
-            if (up) {
-              re[c] = gr;
-              im[c] = gi;
-            } else {
-              re[c1] = gr;
-              im[c1] = gi;
+  };
+  auto epilogue = [&](uint64_t tbase, uint32_t acc) {
+      // 5. Epilogue: TMEM lane b -> the staging buffer.  Warp w reads lanes 32*(w%4)..
+      //    and output targets [h*T/2, (h+1)*T/2) with h = w/4.
+      if constexpr (SHUF) {
+        constexpr int CHS = P::COLS_PER_WARP;
+        const int q = warp & 3;
+        const int h = warp >> 2;
+        const uint32_t lane_addr = acc + ((uint32_t)(q * 32) << 16);
+        float re[CHS], im[CHS];
+        tmem_ld<CHS>(lane_addr + (uint32_t)(h * CHS), re);
+        tmem_ld<CHS>(lane_addr + (uint32_t)(P::T + h * CHS), im);
+        tmem_ld_wait();
+  #pragma unroll
+        for (int i = 0; i < 5; ++i) {
+          if (i < KQ - 1 && i < a.nst) {
+            const int lb = a.st_lane[i];
+            const bool up = (lane >> lb) & 1;
+  #pragma unroll
+            for (int c = 0; c < CHS; ++c) {
+              if (c & (1 << i)) continue;
+              const int c1 = c | (1 << i);
+              const float sr = up ? re[c] : re[c1];
+              const float si = up ? im[c] : im[c1];
+              const float gr = __shfl_xor_sync(0xffffffffu, sr, 1 << lb);
+              const float gi = __shfl_xor_sync(0xffffffffu, si, 1 << lb);
+              if (up) {
+                re[c] = gr;
+                im[c] = gi;
+              } else {
+                re[c1] = gr;
+                im[c1] = gi;
+              }
             }
           }
         }
-      }
-      float2* dst = psi + base + st_lw;
-#pragma unroll
-      for (int c = 0; c < CHS; ++c) __stcs(dst + a.st_reg[c], make_float2(re[c], im[c]));
-    } else {
-      const int q = warp & 3;
-      const int h = warp >> 2;
-      const int b = q * 32 + lane;
-      const int eb_ = eb[b];
-      const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
-      constexpr int CH = P::COLS_PER_WARP < 32 ? P::COLS_PER_WARP : 32;
-#pragma unroll
-      for (int c0 = 0; c0 < P::COLS_PER_WARP; c0 += CH) {
-        float re[CH], im[CH];
-        const int t0 = h * P::COLS_PER_WARP + c0;
-        tmem_ld<CH>(lane_addr + (uint32_t)t0, re);
-        tmem_ld<CH>(lane_addr + (uint32_t)(P::T + t0), im);
-        tmem_ld_wait();
-        if constexpr (STAGED) {
-#pragma unroll
-          for (int j = 0; j < CH; ++j) raw[slot(eb_ | et[t0 + j])] = make_float2(re[j], im[j]);
-        } else if (a.vec == 4 && CH % 4 == 0) {
-          const uint64_t rb = base + dep(eb_);
-#pragma unroll
-          for (int j = 0; j < CH; j += 4) st_v8(psi + rb + dep(et[t0 + j]), &re[j], &im[j]);
-        } else if (a.vec >= 2) {
-          const uint64_t rb = base + dep(eb_);
-#pragma unroll
-          for (int j = 0; j < CH; j += 2)
-            __stcs(reinterpret_cast<float4*>(psi + rb + dep(et[t0 + j])),
-                   make_float4(re[j], im[j], re[j + 1], im[j + 1]));
-        } else {
-          const uint64_t rb = base + dep(eb_);
-#pragma unroll
-          for (int j = 0; j < CH; ++j) __stcs(&psi[rb + dep(et[t0 + j])], make_float2(re[j], im[j]));
+        float2* dst = psi + tbase + st_lw;
+  #pragma unroll
+        for (int c = 0; c < CHS; ++c) __stcs(dst + a.st_reg[c], make_float2(re[c], im[c]));
+      } else {
+        const int q = warp & 3;
+        const int h = warp >> 2;
+        const int b = q * 32 + lane;
+        const int eb_ = eb[b];
+        const uint32_t lane_addr = acc + ((uint32_t)(q * 32) << 16);
+        constexpr int CH = P::COLS_PER_WARP < 32 ? P::COLS_PER_WARP : 32;
+  #pragma unroll
+        for (int c0 = 0; c0 < P::COLS_PER_WARP; c0 += CH) {
+          float re[CH], im[CH];
+          const int t0 = h * P::COLS_PER_WARP + c0;
+          tmem_ld<CH>(lane_addr + (uint32_t)t0, re);
+          tmem_ld<CH>(lane_addr + (uint32_t)(P::T + t0), im);
+          tmem_ld_wait();
+          if constexpr (STAGED) {
+  #pragma unroll
+            for (int j = 0; j < CH; ++j) raw[slot(eb_ | et[t0 + j])] = make_float2(re[j], im[j]);
+          } else if (a.vec == 4 && CH % 4 == 0) {
+            const uint64_t rb = tbase + dep(eb_);
+  #pragma unroll
+            for (int j = 0; j < CH; j += 4) st_v8(psi + rb + dep(et[t0 + j]), &re[j], &im[j]);
+          } else if (a.vec >= 2) {
+            const uint64_t rb = tbase + dep(eb_);
+  #pragma unroll
+            for (int j = 0; j < CH; j += 2)
+              __stcs(reinterpret_cast<float4*>(psi + rb + dep(et[t0 + j])),
+                     make_float4(re[j], im[j], re[j + 1], im[j + 1]));
+          } else {
+            const uint64_t rb = tbase + dep(eb_);
+  #pragma unroll
+            for (int j = 0; j < CH; ++j) __stcs(&psi[rb + dep(et[t0 + j])], make_float2(re[j], im[j]));
+          }
         }
       }
-    }
+  };
+  auto operand_ready = [&]() {
+    fence_async_smem();
     tc_fence_before();
     __syncthreads();
-    if constexpr (STAGED) {
-      // 6. Write the tile back in address order.
+    tc_fence_after();
+  };
+
+  uint32_t ph[2] = {0u, 0u};
+  bool pending[2] = {false, false};
+  uint64_t tile = blockIdx.x;
+  uint64_t base = 0;
+  if (tile < a.ntiles) {
+    base = qsv_insert_zeros(tile, a.ptile, P::EBITS);
+    load_tile(base);
+  }
+  if constexpr (!SHUF) {
+    for (; tile < a.ntiles; tile += gridDim.x) {
+      write_a();
+      operand_ready();
+      issue_mma(tmem, bar_of(0));
+      pending[0] = true;
+      // Prefetch the next tile while the tensor cores work.
+      const uint64_t next = tile + gridDim.x;
+      uint64_t next_base = 0;
+      if (next < a.ntiles) {
+        next_base = qsv_insert_zeros(next, a.ptile, P::EBITS);
+        load_tile(next_base);
+      }
+      if (mbar_wait_bounded(bar_of(0), ph[0])) {
+        ph[0] ^= 1u;
+        pending[0] = false;
+      } else {
+        atomicExch(abort_flag, 1);
+      }
+      tc_fence_after();
+      __syncthreads();
+      if (*abort_flag) break;
+      epilogue(base, tmem);
+      tc_fence_before();
+      __syncthreads();
+      if constexpr (STAGED) {
+        // Write the tile back in address order.
 #pragma unroll
-      for (int u = 0; u < P::VEC; ++u) {
-        const int e = 2 * (u * FB_THREADS + tid);
-        __stcs(reinterpret_cast<float4*>(psi + base + dep(e)), raw4[slot(e) >> 1]);
+        for (int u = 0; u < P::VEC; ++u) {
+          const int e = 2 * (u * FB_THREADS + tid);
+          __stcs(reinterpret_cast<float4*>(psi + base + dep(e)), raw4[slot(e) >> 1]);
+        }
+        __syncthreads();
+      }
+      tc_fence_after();
+      base = next_base;
+    }
+  } else {
+    uint64_t prev_base = 0;
+    int it = 0;
+    for (; tile < a.ntiles; tile += gridDim.x, ++it) {
+      const int s = it & 1;
+      if (it > 0) {
+        // Products of the previous tile: A is free again and accumulator s^1 is ready.
+        if (mbar_wait_bounded(bar_of(s ^ 1), ph[s ^ 1])) {
+          ph[s ^ 1] ^= 1u;
+          pending[s ^ 1] = false;
+        } else {
+          atomicExch(abort_flag, 1);
+        }
+        tc_fence_after();
       }
       __syncthreads();
+      if (*abort_flag) break;
+      write_a();
+      operand_ready();
+      issue_mma(tmem + (uint32_t)(s * P::KD), bar_of(s));
+      pending[s] = true;
+      const uint64_t next = tile + gridDim.x;
+      uint64_t next_base = 0;
+      if (next < a.ntiles) {
+        next_base = qsv_insert_zeros(next, a.ptile, P::EBITS);
+        load_tile(next_base);
+      }
+      if (it > 0) epilogue(prev_base, tmem + (uint32_t)((s ^ 1) * P::KD));
+      tc_fence_before();
+      prev_base = base;
+      base = next_base;
     }
-    tc_fence_after();
-    base = next_base;
+    if (it > 0 && !*abort_flag) {
+      const int s = (it - 1) & 1;
+      if (mbar_wait_bounded(bar_of(s), ph[s])) {
+        ph[s] ^= 1u;
+        pending[s] = false;
+      } else {
+        atomicExch(abort_flag, 1);
+      }
+      tc_fence_after();
+      __syncthreads();
+      if (!*abort_flag) epilogue(prev_base, tmem + (uint32_t)(s * P::KD));
+    }
   }
+  __syncthreads();
   if (*abort_flag) {
-    // Give the tensor cores a last bounded chance to finish before freeing TMEM.
-    mbar_wait_bounded(bar, phase);
+    // Products still in flight get a last bounded wait before TMEM is freed.
+    for (int s = 0; s < 2; ++s)
+      if (pending[s]) mbar_wait_bounded(bar_of(s), ph[s]);
     if (tid == 0) atomicExch(a.flag, 1);
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)P::TMEM_COLS)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)TCOLS)
                  : "memory");
   }
 }
@@ -974,7 +1053,7 @@ int launch_block_variant(qsv_state* s, const BlockArgs& a, float2* psi) {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_block_tc<KQ, MODE>, FB_THREADS, SMEM);
   if (per_sm < 1) per_sm = 1;
   // Bound co-resident CTAs so their TMEM allocations always fit (512 columns per SM).
-  per_sm = std::min(per_sm, 512 / P::TMEM_COLS);
+  per_sm = std::min(per_sm, 512 / (MODE == MODE_SHUF ? P::TMEM_COLS2 : P::TMEM_COLS));
   uint64_t grid = (uint64_t)std::max(1, s->sm_count) * per_sm;
   if (grid > a.ntiles) grid = a.ntiles;
   k_block_tc<KQ, MODE><<<(unsigned)grid, FB_THREADS, SMEM, s->stream>>>(psi, a);

@@ -222,3 +222,21 @@ def test_autotuner_prices_plans_and_picks_the_cheapest_width():
     # Times measured on 26 qubits scale to larger states.
     t._ms[(26, 6, 0)] = ([2.0, 3.0, -1.0], 0)
     assert t.block_ms(30, 6, 0) == pytest.approx(32.0)
+
+
+def test_autotuner_cache_round_trip(tmp_path):
+    from qip_gb300.autotune import Autotuner
+
+    path = str(tmp_path / "tune.json")
+    n = 20
+    ops = [op for g in circuits.brickwork(n, 6, seed=4) for op in gates.decompose(g)]
+    t = _synthetic_tuner(lambda k, low: 1.0 + 0.1 * bin(low).count("1"))
+    t.cache_path = path
+    w, steps, report = t.choose_width(None, n, ops)
+    t2 = Autotuner(cache_path=path)
+    assert t2.width_for(n) == w and t2._ms == t._ms
+    assert sorted(t2._unpinned) == sorted((k, low, best) for (_, k, low), (_, best) in t._ms.items())
+    # A loaded decision is reused without pricing the other widths again.
+    t2._unpinned = []
+    w2, steps2, report2 = t2.choose_width(None, n, ops)
+    assert w2 == w and report2 == report and len(steps2) == len(steps)
