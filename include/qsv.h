@@ -75,6 +75,11 @@ int qsv_add_range(qsv_state* s, const void* host, uint64_t start, uint64_t count
 /* Copy amplitudes [start, start+count) to host memory of the handle's dtype.  Blocks.
  * Replaces CythonBackend.get_state / get_relative_range (qip/backend.py:106-107,168-169). */
 int qsv_read_range(qsv_state* s, void* host, uint64_t start, uint64_t count);
+/* Page-locked host buffers (cudaHostAlloc / cudaFreeHost).  A read into one is a
+ * single DMA with no staging copy and no page faults.  No reference counterpart: the
+ * reference's state already lives in host memory. */
+int qsv_host_alloc(uint64_t bytes, void** out);
+int qsv_host_free(void* p);
 
 /* ---- gates (kronselect_dot) ---------------------------------------------------------
  * The reference applies every gate through cdot_loop (qip/ext/kronprod.pyx:41-200) via

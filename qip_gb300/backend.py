@@ -20,6 +20,7 @@ from typing import Callable, List, Mapping, Optional, Sequence, Tuple, Union
 import numpy
 
 from . import _native as nat
+from . import hostbuf
 from .autotune import default_tuner
 from .fusion import Block, plan, plan_prefix
 from .gates import GateOp, classify_matrix, decompose
@@ -350,8 +351,11 @@ class GpuBackend(StateType):
 
     # ---- readout -------------------------------------------------------------------------
     def get_state(self) -> numpy.ndarray:
+        """The state in host memory: a page-locked array from a reuse pool (one DMA, no
+        page faults; ``qip_gb300.hostbuf``), owned by the caller like the reference's
+        returned state array."""
         self.flush()
-        out = numpy.empty(2 ** self.n, dtype=self.statetype)
+        out = hostbuf.empty(2 ** self.n, self.statetype)
         self._check(self._lib.qsv_read_range(self._h, out.ctypes.data_as(ctypes.c_void_p), 0, out.shape[0]),
                     "get_state")
         return out

@@ -1271,6 +1271,34 @@ int qsv_add_range(qsv_state* s, const void* host, uint64_t start, uint64_t count
   return check_launch(s, "add_range");
 }
 
+namespace {
+bool is_pinned(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+}  // namespace
+
+int qsv_host_alloc(uint64_t bytes, void** out) {
+  if (!out || bytes == 0) return set_error(nullptr, QSV_ERR_INVALID, "bad host allocation request");
+  *out = nullptr;
+  if (cudaHostAlloc(out, bytes, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    return set_error(nullptr, QSV_ERR_OOM, "page-locked host allocation of %llu bytes failed",
+                     (unsigned long long)bytes);
+  }
+  return QSV_OK;
+}
+
+int qsv_host_free(void* p) {
+  if (p && cudaFreeHost(p) != cudaSuccess) return set_error(nullptr, QSV_ERR_CUDA, "cudaFreeHost failed");
+  return QSV_OK;
+}
+
 int qsv_read_range(qsv_state* s, void* host, uint64_t start, uint64_t count) {
   QSV_CHECK_HANDLE(s);
   if (start + count > (1ull << s->n) || (count && !host))
@@ -1278,7 +1306,8 @@ int qsv_read_range(qsv_state* s, void* host, uint64_t start, uint64_t count) {
   if (!count) return QSV_OK;
   const size_t bytes = count * s->amp_bytes;
   const char* src = (const char*)s->d_amp + start * s->amp_bytes;
-  if (bytes < kStageMinBytes) {
+  if (bytes < kStageMinBytes || is_pinned(host)) {
+    // Small reads, and page-locked destinations (qsv_host_alloc): one direct DMA.
     QSV_CUDA(s, cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, s->stream));
     QSV_CUDA(s, cudaStreamSynchronize(s->stream));
     return QSV_OK;

@@ -1,0 +1,39 @@
+"""Page-locked readback arrays: correct values, never reused while an array still
+refers to them, reused once released, and the opt-out."""
+import numpy
+import pytest
+
+import statevector as sv
+from qip_gb300 import GpuBackend, hostbuf
+
+pytestmark = pytest.mark.gpu
+
+
+def addr(a):
+    return a.__array_interface__["data"][0]
+
+
+def test_readback_arrays_are_owned_by_the_caller(monkeypatch):
+    n = 20
+    rng = numpy.random.default_rng(6)
+    v = (rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)).astype(numpy.complex64)
+    st = GpuBackend.make_state(n, [list(range(n))], [v], statetype=numpy.complex64, fusion=False)
+    a = st.get_state()
+    assert isinstance(a.base, hostbuf._PinnedOwner)
+    assert numpy.array_equal(a, v)
+    h = numpy.array([[1, 1], [1, -1]]) / numpy.sqrt(2)
+    st.kronselect_dot({3: h})
+    b = st.get_state()
+    assert addr(a) != addr(b)             # a is still alive: b got another buffer
+    assert numpy.array_equal(a, v)        # ... and a was not overwritten
+    numpy.testing.assert_allclose(b, sv.kronselect_dot({3: h}, v.astype(complex), n), atol=1e-6)
+    old = addr(a)
+    del a
+    c = st.get_state()                    # the released buffer comes back from the pool
+    assert addr(c) == old
+    assert numpy.array_equal(c, b)
+    monkeypatch.setenv("QSV_PINNED_READBACK", "0")
+    d = st.get_state()
+    assert not isinstance(d.base, hostbuf._PinnedOwner)
+    assert numpy.array_equal(d, b)
+    st.close()
