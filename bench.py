@@ -36,6 +36,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_DEFAULT, DEPTH_DEFAULT, SEED = 28, 40, 1234
+# DRAM bytes (read + write) of one fused-block launch on a 2^25 complex64 state, from an
+# ncu capture (dram__bytes_read.sum 268.57 MB + dram__bytes_write.sum 207.09 MB); the
+# traffic of a launch grows with the state, so it is scaled by 2^(n-25).
+NCU_BLOCK_TRAFFIC_N25 = 268.574464e6 + 207.090944e6
 METRIC = "amp-updates/s (brickwork circuit, fused FP32 tensor-core blocks vs plain FP64 per-gate)"
 THROTTLE_REASONS = {
     0x1: "gpu_idle", 0x2: "applications_clocks_setting", 0x4: "sw_power_cap", 0x8: "hw_slowdown",
@@ -372,6 +376,7 @@ def run_ours(args):
     peak, peak_src = read_peaks()
     alg_bytes = 2 * (2 ** n) * 8
     achieved = alg_bytes / mean_block_s / 1e9
+    traffic = NCU_BLOCK_TRAFFIC_N25 * 2.0 ** (n - 25)
     result = {
         "metric": METRIC, "value": value, "unit": "amp-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_fused * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -390,7 +395,9 @@ def run_ours(args):
         "speedup_fused_vs_plain_fp64": t_plain / t_fused,
         "infidelity_vs_fp64": infid,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "k_block_tc (fused block, k<=6)",
+                     "traffic": traffic, "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum "
+                     "of one k_block_tc launch at n=25, scaled by 2^(n-25)",
+                     "kernel": "k_block_tc (fused block, k<=6)",
                      "per_launch_bytes": alg_bytes, "mean_launch_ms": mean_block_s * 1e3,
                      "peak_source": f"{peak_src} hbm_gbs"},
         "e2e": {"value": ws * amp_updates / t_e2e, "unit": "amp-updates/s", "h2d_bytes_per_step": int(h2d),
