@@ -201,6 +201,26 @@ int qsv_batch_adjoint_step(void* psi, void* lam, int nsets, int n, int dtype, in
                            int grad_stride, double* scratch, size_t scratch_doubles,
                            void* stream);
 
+/* Segmented batch execution (cache blocking; no reference counterpart).  A segment is a
+ * run of single-qubit gates (optionally controlled) whose qubits lie in lb local bit
+ * positions lpos[0..lb) (ascending; complex64 lb <= 13, complex128 lb <= 12).  For every
+ * chunk of 2^lb amplitudes (fixed values of the other bits) of every set the chunk is
+ * brought into shared memory once and all the segment's gates are applied there.
+ * gates_dev: device array of ngates records {int32 local target bit, int32 local control
+ * bit or -1, int32 gate index g, int32 (generator << 24) | parameter index}; the 2x2
+ * matrix of gate g for set s is at mats[(g * nsets + s) * 4], row-major, the state's
+ * dtype.  At most 512 gates and 256 generator gates per segment.
+ * forward: psi <- (gates in order) psi.
+ * adjoint: for the gates in reverse order: generator 1 (Y) / 2 (Z): grads[s * grad_stride
+ * + parameter] += Im <lambda| P |psi>; then psi, lambda <- M psi, M lambda with M the
+ * supplied matrix (U^+).  grads accumulate (FP64 atomics), so zero them first. */
+int qsv_batch_segment_forward(void* psi, int nsets, int n, int dtype, int lb, const int* lpos,
+                              int ngates, const void* gates_dev, const void* mats, void* stream);
+int qsv_batch_segment_adjoint(void* psi, void* lam, int nsets, int n, int dtype, int lb,
+                              const int* lpos, int ngates, const void* gates_dev,
+                              const void* mats_dagger, double* grads, int grad_stride,
+                              void* stream);
+
 /* ---- many small circuits in one persistent launch --------------------------------------
  * No reference counterpart (the reference runs one circuit per run() call).  A batch
  * object holds a gate table, a circuit table, per-qubit product-state feeds and the

@@ -4,11 +4,16 @@ Workload: the hardware-efficient ansatz of ``circuits.ansatz_layers`` — per la
 on every qubit, RZ(phi) on every qubit, then a CNOT ring (i, i+1 mod n) — on |0...0>,
 objective E = <psi| sum_i Z_i |psi>, for a batch of parameter sets at once.
 
-Forward: every gate is one batched launch (all parameter sets, each with its own 2x2
-matrix built on the device from its angle); then lambda = (sum Z) psi and E in FP64.
-Backward (adjoint method, no checkpoints): walk the gates in reverse; at a rotation,
-dE/dtheta = Im <lambda| P |psi> (P = Y or Z) is reduced per set, then psi and lambda
-are un-computed by U^+ in the same pass.  Two state vectors per set (psi, lambda).
+Forward: the gates (each set with its own 2x2 matrix built on the device from its
+angle) run in segments: runs of gates whose qubits fit, with address bits 0..4, in 13
+local bits (12 for complex128), reordered only past gates on other qubits (the fusion
+planner's blocked-qubit rule).  One launch per segment brings every 2^13-amplitude
+chunk of every set into shared memory once and applies all the segment's gates there.
+Then lambda = (sum Z) psi and E in FP64.  Backward (adjoint method, no checkpoints):
+the segments in reverse, each chunk's psi and lambda in shared memory; for each gate
+from last to first, at a rotation dE/dtheta = Im <lambda| P |psi> (P = Y or Z) is
+accumulated per set, then psi and lambda are un-computed by U^+.  Two state vectors
+per set (psi, lambda).  ``segmented=False`` runs the same algorithm one launch per gate.
 
 There is no reference counterpart (the reference has no gradients); results are checked
 against central finite differences and the parameter-shift rule on the FP64 oracle and
@@ -107,6 +112,105 @@ def forward_states(ansatz: Ansatz, U: torch.Tensor, cdtype, qdtype) -> torch.Ten
     return psi
 
 
+SEG_FIXED_BITS = 5        # address bits 0..4 are always local (coalesced chunk accesses)
+SEG_MAX_GATES = 512
+SEG_MAX_PARAMS = 256
+
+
+def local_bits(statetype) -> int:
+    return 13 if statetype in (torch.complex64, numpy.complex64) else 12
+
+
+def plan_segments(ansatz: Ansatz, lb: int) -> List[Tuple[Tuple[int, ...], List[int]]]:
+    """[(local bit positions ascending, gate indices in execution order)] covering every
+    gate once.  A gate joins the segment when its bits fit in lb local bits and none of
+    them is blocked by an earlier gate left out (so it commutes with every gate it
+    passes); left-out gates block their bits."""
+    gates = ansatz.gates()
+    n = ansatz.n
+    lb = min(lb, n)
+    fixed = set(range(min(SEG_FIXED_BITS, lb)))
+    remaining = list(range(len(gates)))
+    segs = []
+    while remaining:
+        S = set(fixed)
+        chosen, rest, blocked = [], [], set()
+        nparams = 0
+        for gi in remaining:
+            kind, t, c, _ = gates[gi]
+            bits = {n - 1 - t} | ({n - 1 - c} if c >= 0 else set())
+            gen = 1 if kind in (RY, RZ) else 0
+            merged = S | bits
+            if not (bits & blocked) and len(merged) <= lb and len(chosen) < SEG_MAX_GATES and \
+                    nparams + gen <= SEG_MAX_PARAMS:
+                S = merged
+                chosen.append(gi)
+                nparams += gen
+            else:
+                blocked |= bits
+                rest.append(gi)
+        p = 0
+        while len(S) < lb:
+            S.add(p) if p not in S else None
+            p += 1
+        segs.append((tuple(sorted(S)), chosen))
+        remaining = rest
+    return segs
+
+
+_SEG_CACHE = {}
+
+
+def segment_tables(ansatz: Ansatz, lb: int, device):
+    """Planned segments with their device gate tables (int32 [ngates, 4]), cached."""
+    key = (ansatz.n, ansatz.layers, min(lb, ansatz.n), str(device))
+    if key not in _SEG_CACHE:
+        gates = ansatz.gates()
+        n = ansatz.n
+        out = []
+        for lpos, gl in plan_segments(ansatz, lb):
+            local = {b: i for i, b in enumerate(lpos)}
+            rows = []
+            for gi in gl:
+                kind, t, c, pi = gates[gi]
+                gen = {RY: 1, RZ: 2}.get(kind, 0)
+                rows.append([local[n - 1 - t], local[n - 1 - c] if c >= 0 else -1, gi,
+                             (gen << 24) | (pi if gen else 0)])
+            tab = torch.tensor(rows, dtype=torch.int32, device=device)
+            out.append((nat.int_array(lpos), len(lpos), len(gl), tab))
+        _SEG_CACHE[key] = out
+    return _SEG_CACHE[key]
+
+
+def forward_states_segmented(ansatz: Ansatz, U: torch.Tensor, cdtype, qdtype, lb: int) -> torch.Tensor:
+    lib = nat.load()
+    B = U.shape[1]
+    n = ansatz.n
+    psi = torch.empty((B, 2 ** n), dtype=cdtype, device=U.device)
+    st = ctypes.c_void_p(_stream_ptr())
+    _check(lib.qsv_batch_reset(ctypes.c_void_p(psi.data_ptr()), B, n, qdtype, st), "batch_reset")
+    for lpos, nl, ng, tab in segment_tables(ansatz, lb, U.device):
+        _check(lib.qsv_batch_segment_forward(ctypes.c_void_p(psi.data_ptr()), B, n, qdtype, nl, nat.ip(lpos), ng,
+                                             ctypes.c_void_p(tab.data_ptr()), ctypes.c_void_p(U.data_ptr()), st),
+               "segment_forward")
+    return psi
+
+
+def adjoint_sweep_segmented(ansatz: Ansatz, psi, lam, Ud, qdtype, lb: int) -> torch.Tensor:
+    """Reverse sweep by segments; consumes psi and lambda.  Returns dE/dtheta [B, P]."""
+    lib = nat.load()
+    B = psi.shape[0]
+    P = ansatz.nparams
+    grads = torch.zeros((B, P), dtype=torch.float64, device=psi.device)
+    st = ctypes.c_void_p(_stream_ptr())
+    for lpos, nl, ng, tab in reversed(segment_tables(ansatz, lb, psi.device)):
+        _check(lib.qsv_batch_segment_adjoint(ctypes.c_void_p(psi.data_ptr()), ctypes.c_void_p(lam.data_ptr()), B,
+                                             ansatz.n, qdtype, nl, nat.ip(lpos), ng, ctypes.c_void_p(tab.data_ptr()),
+                                             ctypes.c_void_p(Ud.data_ptr()), ctypes.c_void_p(grads.data_ptr()), P, st),
+               "segment_adjoint")
+    return grads
+
+
 def _scratch(B: int, device) -> torch.Tensor:
     return torch.empty(B * 4096, dtype=torch.float64, device=device)
 
@@ -115,12 +219,14 @@ class SumZExpectation(torch.autograd.Function):
     """E[b] = <psi(thetas[b])| sum_i Z_i |psi(thetas[b])> with adjoint gradients."""
 
     @staticmethod
-    def forward(ctx, thetas: torch.Tensor, ansatz: Ansatz, statetype=torch.complex64):
+    def forward(ctx, thetas: torch.Tensor, ansatz: Ansatz, statetype=torch.complex64, segmented: bool = True):
         if not thetas.is_cuda:
             raise ValueError("thetas must live on the CUDA device")
         cdtype, qdtype = _dtype(statetype)
         U, Ud = gate_matrices(ansatz, thetas.detach(), cdtype)
-        psi = forward_states(ansatz, U, cdtype, qdtype)
+        lb = local_bits(cdtype)
+        psi = forward_states_segmented(ansatz, U, cdtype, qdtype, lb) if segmented else \
+            forward_states(ansatz, U, cdtype, qdtype)
         lam = torch.empty_like(psi)
         B = thetas.shape[0]
         energies = torch.empty(B, dtype=torch.float64, device=thetas.device)
@@ -133,14 +239,18 @@ class SumZExpectation(torch.autograd.Function):
         ctx.ansatz, ctx.qdtype = ansatz, qdtype
         ctx.buffers = (psi, lam, Ud, scratch)
         ctx.tdtype = thetas.dtype
+        ctx.segmented, ctx.lb = segmented, lb
         return energies.to(thetas.dtype)
 
     @staticmethod
     def backward(ctx, grad_e: torch.Tensor):
         psi, lam, Ud, scratch = ctx.buffers
         ctx.buffers = None
-        grads = adjoint_sweep(ctx.ansatz, psi, lam, Ud, scratch, ctx.qdtype)
-        return (grad_e.to(torch.float64)[:, None] * grads).to(ctx.tdtype), None, None
+        if ctx.segmented:
+            grads = adjoint_sweep_segmented(ctx.ansatz, psi, lam, Ud, ctx.qdtype, ctx.lb)
+        else:
+            grads = adjoint_sweep(ctx.ansatz, psi, lam, Ud, scratch, ctx.qdtype)
+        return (grad_e.to(torch.float64)[:, None] * grads).to(ctx.tdtype), None, None, None
 
 
 def adjoint_sweep(ansatz: Ansatz, psi, lam, Ud, scratch, qdtype) -> torch.Tensor:
@@ -164,9 +274,9 @@ def adjoint_sweep(ansatz: Ansatz, psi, lam, Ud, scratch, qdtype) -> torch.Tensor
     return grads
 
 
-def energy_and_grad(thetas: torch.Tensor, ansatz: Ansatz, statetype=torch.complex64):
+def energy_and_grad(thetas: torch.Tensor, ansatz: Ansatz, statetype=torch.complex64, segmented: bool = True):
     """Convenience: (E [B], dE/dtheta [B, P]) through the autograd Function."""
     th = thetas.detach().clone().requires_grad_(True)
-    e = SumZExpectation.apply(th, ansatz, statetype)
+    e = SumZExpectation.apply(th, ansatz, statetype, segmented)
     e.sum().backward()
     return e.detach(), th.grad

@@ -210,6 +210,230 @@ __global__ void k_batch_zero(CT<R>* psi, int n, int nsets) {
   }
 }
 
+// ---- segmented execution -----------------------------------------------------------
+// A segment is a run of gates whose qubits lie in a set of LB bit positions (the
+// segment's local bits, ascending in lpos, always containing the lowest address bits so
+// a warp's accesses stay coalesced).  Each CTA takes chunks of one parameter set: a
+// chunk is the 2^LB amplitudes with fixed values of the other n-LB bits, gathered into
+// shared memory, and every gate of the segment is applied there before the chunk is
+// scattered back: one pass over the state per segment instead of one per gate.
+// Gate descriptors (SegGate) name local bits; matrices are looked up per set.
+struct SegGate {
+  int32_t tbit;   // local target bit
+  int32_t cbit;   // local control bit, -1 if none
+  int32_t g;      // gate index: matrices at mats[(g * nsets + s) * 4 ...]
+  int32_t gp;     // (generator << 24) | parameter index; generator 0 none, 1 Y, 2 Z
+};
+constexpr int SEG_THREADS = 512;
+constexpr int SEG_MAX_GATES = 512;
+constexpr int SEG_MAX_PARAMS = 256;
+
+struct SegArgs {
+  int n, nsets, lb, ngates;
+  int lpos[16];
+  uint64_t nchunks;
+};
+
+// Applies gate m (2x2, per set) to the pairs of local bit t (with local control c >= 0).
+template <typename R>
+__device__ __forceinline__ void seg_apply(CT<R>* v, int lb, int t, int c, const CT<R> m[4]) {
+  const int npairs = 1 << (lb - 1 - (c >= 0 ? 1 : 0));
+  const int lo = c >= 0 ? min(t, c) : t, hi = c >= 0 ? max(t, c) : t;
+  for (int k = threadIdx.x; k < npairs; k += blockDim.x) {
+    int i0 = ((k >> lo) << (lo + 1)) | (k & ((1 << lo) - 1));
+    if (c >= 0) {
+      i0 = ((i0 >> hi) << (hi + 1)) | (i0 & ((1 << hi) - 1));
+      i0 |= 1 << c;
+    }
+    const int i1 = i0 | (1 << t);
+    const CT<R> x = v[i0], y = v[i1];
+    CT<R> o0, o1;
+    o0.x = R(0); o0.y = R(0); o1 = o0;
+    o0 = qsv_cfma(m[0], x, o0);
+    o0 = qsv_cfma(m[1], y, o0);
+    o1 = qsv_cfma(m[2], x, o1);
+    o1 = qsv_cfma(m[3], y, o1);
+    v[i0] = o0;
+    v[i1] = o1;
+  }
+}
+
+// Gathers a chunk (and optionally a second state's) into shared memory with GB loads per
+// thread issued before the first shared store (the gather is latency-bound otherwise).
+template <typename R, bool TWO>
+__device__ __forceinline__ void seg_gather(const CT<R>* src, const CT<R>* src2, CT<R>* v, CT<R>* v2, int chunk,
+                                           uint64_t base, const uint64_t* dlo, const uint64_t* dhi) {
+  constexpr int GB = sizeof(R) == 4 ? 16 : 8;
+  for (int e0 = threadIdx.x; e0 < chunk; e0 += GB * blockDim.x) {
+    CT<R> t[GB], t2[TWO ? GB : 1];
+#pragma unroll
+    for (int j = 0; j < GB; ++j) {
+      const int e = e0 + j * blockDim.x;
+      if (e < chunk) {
+        const uint64_t ad = base + dlo[e & 127] + dhi[e >> 7];
+        t[j] = src[ad];
+        if constexpr (TWO) t2[j] = src2[ad];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < GB; ++j) {
+      const int e = e0 + j * blockDim.x;
+      if (e < chunk) {
+        v[e] = t[j];
+        if constexpr (TWO) v2[e] = t2[j];
+      }
+    }
+  }
+}
+
+// The segment's gate records and this set's matrices, staged in shared memory once per
+// CTA (otherwise every gate starts with two dependent global loads).
+template <typename R>
+__device__ __forceinline__ void seg_stage(const SegGate* gates, const CT<R>* mats, const SegArgs& a, int s,
+                                          SegGate* gsh, CT<R>* msh) {
+  for (int k = threadIdx.x; k < a.ngates; k += blockDim.x) {
+    const SegGate g = gates[k];
+    gsh[k] = g;
+    const CT<R>* mp = mats + ((uint64_t)g.g * a.nsets + s) * 4;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) msh[4 * k + i] = mp[i];
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void seg_tables(const SegArgs& a, uint64_t* dlo, uint64_t* dhi) {
+  for (int i = threadIdx.x; i < 128; i += blockDim.x) {
+    uint64_t lo = 0, hi = 0;
+    for (int b = 0; b < 7; ++b)
+      if ((i >> b) & 1) {
+        if (b < a.lb) lo |= 1ull << a.lpos[b];
+        if (7 + b < a.lb) hi |= 1ull << a.lpos[7 + b];
+      }
+    dlo[i] = lo;
+    dhi[i] = hi;
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(SEG_THREADS, 2)
+    k_seg_forward(CT<R>* __restrict__ psi, const CT<R>* __restrict__ mats, const SegGate* __restrict__ gates,
+                  const __grid_constant__ SegArgs a) {
+  extern __shared__ __align__(16) uint8_t seg_smem[];
+  const int chunk = 1 << a.lb;
+  CT<R>* v = reinterpret_cast<CT<R>*>(seg_smem);
+  CT<R>* msh = v + chunk;                                   // [ngates][4] this set's matrices
+  SegGate* gsh = reinterpret_cast<SegGate*>(msh + 4 * a.ngates);
+  __shared__ uint64_t dlo[128], dhi[128];
+  const int s = blockIdx.y;
+  CT<R>* st = psi + ((uint64_t)s << a.n);
+  seg_tables<R>(a, dlo, dhi);
+  seg_stage<R>(gates, mats, a, s, gsh, msh);
+  __syncthreads();
+  for (uint64_t ch = blockIdx.x; ch < a.nchunks; ch += gridDim.x) {
+    const uint64_t base = qsv_insert_zeros(ch, a.lpos, a.lb);
+    seg_gather<R, false>(st, nullptr, v, nullptr, chunk, base, dlo, dhi);
+    __syncthreads();
+    for (int k = 0; k < a.ngates; ++k) {
+      const SegGate g = gsh[k];
+      const CT<R> m[4] = {msh[4 * k], msh[4 * k + 1], msh[4 * k + 2], msh[4 * k + 3]};
+      seg_apply<R>(v, a.lb, g.tbit, g.cbit, m);
+      __syncthreads();
+    }
+    for (int e = threadIdx.x; e < chunk; e += blockDim.x) st[base + dlo[e & 127] + dhi[e >> 7]] = v[e];
+    __syncthreads();
+  }
+}
+
+// Reverse sweep over one segment: for k = last .. first: [generator: accumulate
+// Im<lambda| P |psi> over the chunk]; psi, lambda <- M psi, M lambda (M = U^+).  Per
+// warp FP64 accumulators in shared memory, one atomicAdd per parameter per CTA.
+template <typename R>
+__global__ void __launch_bounds__(SEG_THREADS)
+    k_seg_adjoint(CT<R>* __restrict__ psi, CT<R>* __restrict__ lam, const CT<R>* __restrict__ mats_dagger,
+                  const SegGate* __restrict__ gates, const __grid_constant__ SegArgs a, double* __restrict__ grads,
+                  int grad_stride) {
+  extern __shared__ __align__(16) uint8_t seg_smem[];
+  const int chunk = 1 << a.lb;
+  CT<R>* v = reinterpret_cast<CT<R>*>(seg_smem);
+  CT<R>* l = v + chunk;
+  double* accw = reinterpret_cast<double*>(l + chunk);  // [SEG_MAX_PARAMS][16 warps]
+  CT<R>* msh = reinterpret_cast<CT<R>*>(accw + SEG_MAX_PARAMS * 16);  // [ngates][4]
+  SegGate* gsh = reinterpret_cast<SegGate*>(msh + 4 * a.ngates);
+  __shared__ uint64_t dlo[128], dhi[128];
+  __shared__ int slot_of[SEG_MAX_GATES];
+  const int s = blockIdx.y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  CT<R>* sp = psi + ((uint64_t)s << a.n);
+  CT<R>* sl = lam + ((uint64_t)s << a.n);
+  seg_tables<R>(a, dlo, dhi);
+  seg_stage<R>(gates, mats_dagger, a, s, gsh, msh);
+  if (threadIdx.x == 0) {
+    int np = 0;
+    for (int k = 0; k < a.ngates; ++k) slot_of[k] = ((gates[k].gp >> 24) && np < SEG_MAX_PARAMS) ? np++ : -1;
+  }
+  for (int i = threadIdx.x; i < SEG_MAX_PARAMS * 16; i += blockDim.x) accw[i] = 0.0;
+  __syncthreads();
+  for (uint64_t ch = blockIdx.x; ch < a.nchunks; ch += gridDim.x) {
+    const uint64_t base = qsv_insert_zeros(ch, a.lpos, a.lb);
+    seg_gather<R, true>(sp, sl, v, l, chunk, base, dlo, dhi);
+    __syncthreads();
+    for (int k = a.ngates - 1; k >= 0; --k) {
+      const SegGate g = gsh[k];
+      const int gen = g.gp >> 24;
+      const CT<R> m00 = msh[4 * k], m01 = msh[4 * k + 1], m10 = msh[4 * k + 2], m11 = msh[4 * k + 3];
+      // One pass over the pairs of the target (with the control set): the generator
+      // term Im<lambda| P |psi> from the current pair, then U^+ on psi and lambda.
+      const int t = g.tbit, c = g.cbit;
+      const int npairs = chunk >> (c >= 0 ? 2 : 1);
+      const int lo = c >= 0 ? min(t, c) : t, hi = c >= 0 ? max(t, c) : t;
+      R part = R(0);
+      for (int kk = threadIdx.x; kk < npairs; kk += blockDim.x) {
+        int i0 = ((kk >> lo) << (lo + 1)) | (kk & ((1 << lo) - 1));
+        if (c >= 0) i0 = (((i0 >> hi) << (hi + 1)) | (i0 & ((1 << hi) - 1))) | (1 << c);
+        const int i1 = i0 | (1 << t);
+        const CT<R> x = v[i0], y = v[i1], l0 = l[i0], l1 = l[i1];
+        if (gen == 2)
+          part += (l0.x * x.y - l0.y * x.x) - (l1.x * y.y - l1.y * y.x);
+        else if (gen == 1)
+          part += (l1.x * x.x + l1.y * x.y) - (l0.x * y.x + l0.y * y.y);
+        CT<R> o0, o1, q0, q1;
+        o0.x = R(0); o0.y = R(0); o1 = o0; q0 = o0; q1 = o0;
+        o0 = qsv_cfma(m00, x, o0);
+        o0 = qsv_cfma(m01, y, o0);
+        o1 = qsv_cfma(m10, x, o1);
+        o1 = qsv_cfma(m11, y, o1);
+        q0 = qsv_cfma(m00, l0, q0);
+        q0 = qsv_cfma(m01, l1, q0);
+        q1 = qsv_cfma(m10, l0, q1);
+        q1 = qsv_cfma(m11, l1, q1);
+        v[i0] = o0;
+        v[i1] = o1;
+        l[i0] = q0;
+        l[i1] = q1;
+      }
+      if (gen) {
+        const double w = warp_sum_d((double)part);
+        if (lane == 0 && slot_of[k] >= 0) accw[slot_of[k] * 16 + warp] += w;
+      }
+      __syncthreads();
+    }
+    for (int e = threadIdx.x; e < chunk; e += blockDim.x) {
+      const uint64_t ad = base + dlo[e & 127] + dhi[e >> 7];
+      sp[ad] = v[e];
+      sl[ad] = l[e];
+    }
+    __syncthreads();
+  }
+  for (int k = threadIdx.x; k < a.ngates; k += blockDim.x) {
+    const int slot = slot_of[k];
+    if (slot < 0) continue;
+    double sum = 0.0;
+    for (int w = 0; w < nwarps; ++w) sum += accw[slot * 16 + w];
+    atomicAdd(&grads[(uint64_t)s * grad_stride + (gates[k].gp & 0xFFFFFF)], sum);
+  }
+}
+
 int g_sms = 0;
 int sms() {
   if (!g_sms) {
@@ -343,6 +567,93 @@ int qsv_batch_adjoint_step(void* psi, void* lam, int nsets, int n, int dtype, in
   if (rc || !generator) return rc;
   k_batch_finish<<<(nsets + 127) / 128, 128, 0, st>>>(scratch, (int)nb, nsets, grads, grad_stride);
   return launch_check("batch_finish");
+}
+
+}  // extern "C"
+
+// ---- segmented execution ------------------------------------------------------------
+namespace {
+int seg_args(int n, int nsets, int dtype, int lb, const int* lpos, int ngates, bool two, SegArgs& a, size_t& smem) {
+  if (n < 1 || n > QSV_MAXN || nsets < 1 || nsets > 65535 || !lpos || ngates < 0 || ngates > SEG_MAX_GATES)
+    return set_error(nullptr, QSV_ERR_INVALID, "bad segment (n=%d nsets=%d ngates=%d)", n, nsets, ngates);
+  if (dtype != QSV_C64 && dtype != QSV_C128) return set_error(nullptr, QSV_ERR_INVALID, "unknown dtype %d", dtype);
+  const size_t amp = dtype == QSV_C64 ? 8 : 16;
+  const int lbmax = dtype == QSV_C64 ? 13 : 12;
+  if (lb < 1 || lb > n || lb > lbmax) return set_error(nullptr, QSV_ERR_INVALID, "local bits %d outside [1, %d]", lb, lbmax);
+  for (int i = 0; i < lb; ++i) {
+    if (lpos[i] < 0 || lpos[i] >= n || (i > 0 && lpos[i] <= lpos[i - 1]))
+      return set_error(nullptr, QSV_ERR_INVALID, "local bit positions must ascend within [0, n)");
+    a.lpos[i] = lpos[i];
+  }
+  a.n = n;
+  a.nsets = nsets;
+  a.lb = lb;
+  a.ngates = ngates;
+  a.nchunks = 1ull << (n - lb);
+  smem = ((size_t)1 << lb) * amp * (two ? 2 : 1) + (two ? (size_t)SEG_MAX_PARAMS * 16 * sizeof(double) : 0) +
+         (size_t)ngates * (4 * amp + sizeof(SegGate));
+  return QSV_OK;
+}
+
+template <typename K>
+int seg_config(K kernel, size_t smem, const char* what) {
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return set_error(nullptr, QSV_ERR_CUDA, "%s smem attribute: %s", what, cudaGetErrorString(e));
+  return QSV_OK;
+}
+
+dim3 seg_grid(uint64_t nchunks, int nsets, int per_sm) {
+  uint64_t want = ((uint64_t)sms() * per_sm * 4 + nsets - 1) / nsets;
+  if (want < 1) want = 1;
+  return dim3((unsigned)std::min<uint64_t>(want, nchunks), (unsigned)nsets);
+}
+}  // namespace
+
+extern "C" {
+
+int qsv_batch_segment_forward(void* psi, int nsets, int n, int dtype, int lb, const int* lpos, int ngates,
+                              const void* gates_dev, const void* mats, void* stream) {
+  if (!psi || !mats || (ngates > 0 && !gates_dev)) return set_error(nullptr, QSV_ERR_INVALID, "null pointer");
+  SegArgs a;
+  size_t smem = 0;
+  int rc = seg_args(n, nsets, dtype, lb, lpos, ngates, false, a, smem);
+  if (rc || ngates == 0) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const dim3 grid = seg_grid(a.nchunks, nsets, 2);
+  if (dtype == QSV_C64) {
+    if ((rc = seg_config(k_seg_forward<float>, smem, "segment_forward"))) return rc;
+    k_seg_forward<float><<<grid, SEG_THREADS, smem, st>>>((float2*)psi, (const float2*)mats,
+                                                          (const SegGate*)gates_dev, a);
+  } else {
+    if ((rc = seg_config(k_seg_forward<double>, smem, "segment_forward"))) return rc;
+    k_seg_forward<double><<<grid, SEG_THREADS, smem, st>>>((double2*)psi, (const double2*)mats,
+                                                           (const SegGate*)gates_dev, a);
+  }
+  return launch_check("segment_forward");
+}
+
+int qsv_batch_segment_adjoint(void* psi, void* lam, int nsets, int n, int dtype, int lb, const int* lpos, int ngates,
+                              const void* gates_dev, const void* mats_dagger, double* grads, int grad_stride,
+                              void* stream) {
+  if (!psi || !lam || !mats_dagger || !grads || (ngates > 0 && !gates_dev))
+    return set_error(nullptr, QSV_ERR_INVALID, "null pointer");
+  SegArgs a;
+  size_t smem = 0;
+  int rc = seg_args(n, nsets, dtype, lb, lpos, ngates, true, a, smem);
+  if (rc || ngates == 0) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const dim3 grid = seg_grid(a.nchunks, nsets, 1);
+  if (dtype == QSV_C64) {
+    if ((rc = seg_config(k_seg_adjoint<float>, smem, "segment_adjoint"))) return rc;
+    k_seg_adjoint<float><<<grid, SEG_THREADS, smem, st>>>((float2*)psi, (float2*)lam, (const float2*)mats_dagger,
+                                                          (const SegGate*)gates_dev, a, grads, grad_stride);
+  } else {
+    if ((rc = seg_config(k_seg_adjoint<double>, smem, "segment_adjoint"))) return rc;
+    k_seg_adjoint<double><<<grid, SEG_THREADS, smem, st>>>((double2*)psi, (double2*)lam,
+                                                           (const double2*)mats_dagger, (const SegGate*)gates_dev, a,
+                                                           grads, grad_stride);
+  }
+  return launch_check("segment_adjoint");
 }
 
 }  // extern "C"

@@ -50,3 +50,32 @@ def test_ansatz_gate_list_matches_circuit_generator():
             assert key == (tgt,)
             numpy.testing.assert_allclose(m, m2, atol=1e-15)
         numpy.testing.assert_allclose(Ud[g, 0].numpy().reshape(2, 2), m2.conj().T, atol=1e-15)
+
+
+def test_segment_plan_is_the_same_circuit():
+    """Segments (gates reordered only past gates on other qubits) reproduce the circuit;
+    every segment's gates act on its local bits, which include address bits 0..4."""
+    n, layers = 10, 3
+    a = adjoint.Ansatz(n, layers)
+    rng = numpy.random.default_rng(3)
+    th = rng.uniform(0, 2 * numpy.pi, a.nparams)
+    mats = circuits.ansatz_layers(n, layers, th)
+    # ansatz_layers gives one dictionary per gate in ansatz.gates() order.
+    assert len(mats) == len(a.gates())
+    v0 = (rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n))
+    want = v0.copy()
+    for g in mats:
+        want = sv.kronselect_dot(g, want, n)
+    for lb in (7, 8, 10):
+        segs = adjoint.plan_segments(a, lb)
+        assert sorted(gi for _, gl in segs for gi in gl) == list(range(len(mats)))
+        got = v0.copy()
+        for lpos, gl in segs:
+            assert len(lpos) == min(lb, n) and set(range(5)) <= set(lpos)
+            for gi in gl:
+                kind, t, c, _ = a.gates()[gi]
+                assert n - 1 - t in lpos and (c < 0 or n - 1 - c in lpos)
+                got = sv.kronselect_dot(mats[gi], got, n)
+        numpy.testing.assert_allclose(got, want, atol=1e-12)
+        if lb < n:
+            assert len(segs) > 1
