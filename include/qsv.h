@@ -206,20 +206,26 @@ int qsv_batch_adjoint_step(void* psi, void* lam, int nsets, int n, int dtype, in
  * positions lpos[0..lb) (ascending; complex64 lb <= 13, complex128 lb <= 12).  For every
  * chunk of 2^lb amplitudes (fixed values of the other bits) of every set the chunk is
  * brought into shared memory once and all the segment's gates are applied there.
- * gates_dev: device array of ngates records {int32 local target bit, int32 local control
- * bit or -1, int32 gate index g, int32 (generator << 24) | parameter index}; the 2x2
- * matrix of gate g for set s is at mats[(g * nsets + s) * 4], row-major, the state's
- * dtype.  At most 512 gates and 256 generator gates per segment.
+ * Gates come in groups of at most 3 local bits and 8 gates, each applied in registers
+ * to items of 2^nb amplitudes (one shared-memory pass per group).
+ * groups_dev: device array of ngroups records {int32 nb (1..3), int32 local bit
+ * positions packed 8 bits each (ascending), int32 first gate, int32 gate count}.
+ * gates_dev: device array of ngates records {int32 target index among its group's bits,
+ * int32 control index or -1, int32 gate index g, int32 (generator << 24) | parameter};
+ * the 2x2 matrix of gate g for set s is at mats[(g * nsets + s) * 4], row-major, the
+ * state's dtype.  At most 512 gates and 256 generator gates per segment.
  * forward: psi <- (gates in order) psi.
- * adjoint: for the gates in reverse order: generator 1 (Y) / 2 (Z): grads[s * grad_stride
- * + parameter] += Im <lambda| P |psi>; then psi, lambda <- M psi, M lambda with M the
- * supplied matrix (U^+).  grads accumulate (FP64 atomics), so zero them first. */
+ * adjoint: groups and their gates in reverse order: generator 1 (Y) / 2 (Z):
+ * grads[s * grad_stride + parameter] += Im <lambda| P |psi>; then psi, lambda <- M psi,
+ * M lambda with M the supplied matrix (U^+).  grads accumulate (FP64 atomics), so zero
+ * them first. */
 int qsv_batch_segment_forward(void* psi, int nsets, int n, int dtype, int lb, const int* lpos,
-                              int ngates, const void* gates_dev, const void* mats, void* stream);
+                              int ngroups, const void* groups_dev, int ngates, const void* gates_dev,
+                              const void* mats, void* stream);
 int qsv_batch_segment_adjoint(void* psi, void* lam, int nsets, int n, int dtype, int lb,
-                              const int* lpos, int ngates, const void* gates_dev,
-                              const void* mats_dagger, double* grads, int grad_stride,
-                              void* stream);
+                              const int* lpos, int ngroups, const void* groups_dev, int ngates,
+                              const void* gates_dev, const void* mats_dagger, double* grads,
+                              int grad_stride, void* stream);
 
 /* ---- many small circuits in one persistent launch --------------------------------------
  * No reference counterpart (the reference runs one circuit per run() call).  A batch

@@ -52,11 +52,12 @@ SIGNATURES = {
     "qsv_host_alloc": (ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]),
     "qsv_host_free": (ctypes.c_int, [ctypes.c_void_p]),
     "qsv_batch_segment_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                                  _c_int_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
-                                                  ctypes.c_void_p]),
+                                                  _c_int_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_void_p]),
     "qsv_batch_segment_adjoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                                  ctypes.c_int, _c_int_p, ctypes.c_int, ctypes.c_void_p,
-                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+                                                  ctypes.c_int, _c_int_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                                  ctypes.c_void_p]),
     "qsv_tune_blocks": (ctypes.c_int, [_handle, ctypes.c_int, _c_int_p, _c_int_p, ctypes.c_int, _c_double_p, _c_int_p]),
     "qsv_set_block_mode": (ctypes.c_int, [_handle, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "qsv_apply_blocks": (ctypes.c_int, [_handle, ctypes.c_int, _c_int_p, _c_int_p, _c_double_p]),

@@ -12,7 +12,9 @@ chunk of every set into shared memory once and applies all the segment's gates t
 Then lambda = (sum Z) psi and E in FP64.  Backward (adjoint method, no checkpoints):
 the segments in reverse, each chunk's psi and lambda in shared memory; for each gate
 from last to first, at a rotation dE/dtheta = Im <lambda| P |psi> (P = Y or Z) is
-accumulated per set, then psi and lambda are un-computed by U^+.  Two state vectors
+accumulated per set, then psi and lambda are un-computed by U^+.  Inside a segment
+gates are grouped by at most 3 local bits and applied in registers to 8-amplitude
+items, one shared-memory pass per group.  Two state vectors
 per set (psi, lambda).  ``segmented=False`` runs the same algorithm one launch per gate.
 
 There is no reference counterpart (the reference has no gradients); results are checked
@@ -117,8 +119,12 @@ SEG_MAX_GATES = 512
 SEG_MAX_PARAMS = 256
 
 
-def local_bits(statetype) -> int:
-    return 13 if statetype in (torch.complex64, numpy.complex64) else 12
+def local_bits(statetype, backward: bool = False) -> int:
+    """Local bits of a segment: 2^lb amplitudes per chunk in shared memory.  The reverse
+    sweep holds psi and lambda chunks, so it uses one bit less (two CTAs per SM); any
+    segmentation is an equivalent order of the same circuit, so the two may differ."""
+    lb = 13 if statetype in (torch.complex64, numpy.complex64) else 12
+    return lb - 1 if backward else lb
 
 
 def plan_segments(ansatz: Ansatz, lb: int) -> List[Tuple[Tuple[int, ...], List[int]]]:
@@ -158,11 +164,39 @@ def plan_segments(ansatz: Ansatz, lb: int) -> List[Tuple[Tuple[int, ...], List[i
     return segs
 
 
+GROUP_BITS = 3    # local bits of a register group (2^3 amplitudes per item)
+GROUP_GATES = 8   # gates per group
+
+
+def plan_groups(bits_of: List[Tuple[int, ...]], max_bits: int = GROUP_BITS,
+                max_gates: int = GROUP_GATES) -> List[Tuple[Tuple[int, ...], List[int]]]:
+    """Split a segment's gate sequence (bits_of[i] = local bits of gate i) into groups of
+    at most max_bits bits and max_gates gates, with the blocked-bit rule (a gate moves
+    ahead only past gates on other bits).  Returns [(bits ascending, gate positions)]."""
+    remaining = list(range(len(bits_of)))
+    groups = []
+    while remaining:
+        B, chosen, blocked, rest = set(), [], set(), []
+        for i in remaining:
+            bits = set(bits_of[i])
+            if not (bits & blocked) and len(chosen) < max_gates and len(B | bits) <= max_bits:
+                B |= bits
+                chosen.append(i)
+            else:
+                blocked |= bits
+                rest.append(i)
+        groups.append((tuple(sorted(B)), chosen))
+        remaining = rest
+    return groups
+
+
 _SEG_CACHE = {}
 
 
 def segment_tables(ansatz: Ansatz, lb: int, device):
-    """Planned segments with their device gate tables (int32 [ngates, 4]), cached."""
+    """Planned segments with their device tables, cached: per segment (local bits,
+    lb, groups int32 [ngroups, 4], gates int32 [ngates, 4]); gates are stored in group
+    order, targets/controls as indices among their group's bits."""
     key = (ansatz.n, ansatz.layers, min(lb, ansatz.n), str(device))
     if key not in _SEG_CACHE:
         gates = ansatz.gates()
@@ -170,14 +204,23 @@ def segment_tables(ansatz: Ansatz, lb: int, device):
         out = []
         for lpos, gl in plan_segments(ansatz, lb):
             local = {b: i for i, b in enumerate(lpos)}
-            rows = []
+            lbits = []
             for gi in gl:
-                kind, t, c, pi = gates[gi]
-                gen = {RY: 1, RZ: 2}.get(kind, 0)
-                rows.append([local[n - 1 - t], local[n - 1 - c] if c >= 0 else -1, gi,
-                             (gen << 24) | (pi if gen else 0)])
+                kind, t, c, _ = gates[gi]
+                lbits.append((local[n - 1 - t],) + ((local[n - 1 - c],) if c >= 0 else ()))
+            grows, rows = [], []
+            for gbits, members in plan_groups(lbits):
+                idx = {b: j for j, b in enumerate(gbits)}
+                packed = sum(b << (8 * j) for j, b in enumerate(gbits))
+                grows.append([len(gbits), packed, len(rows), len(members)])
+                for m in members:
+                    kind, t, c, pi = gates[gl[m]]
+                    gen = {RY: 1, RZ: 2}.get(kind, 0)
+                    rows.append([idx[local[n - 1 - t]], idx[local[n - 1 - c]] if c >= 0 else -1, gl[m],
+                                 (gen << 24) | (pi if gen else 0)])
+            gtab = torch.tensor(grows, dtype=torch.int32, device=device)
             tab = torch.tensor(rows, dtype=torch.int32, device=device)
-            out.append((nat.int_array(lpos), len(lpos), len(gl), tab))
+            out.append((nat.int_array(lpos), len(lpos), len(grows), gtab, len(rows), tab))
         _SEG_CACHE[key] = out
     return _SEG_CACHE[key]
 
@@ -189,9 +232,10 @@ def forward_states_segmented(ansatz: Ansatz, U: torch.Tensor, cdtype, qdtype, lb
     psi = torch.empty((B, 2 ** n), dtype=cdtype, device=U.device)
     st = ctypes.c_void_p(_stream_ptr())
     _check(lib.qsv_batch_reset(ctypes.c_void_p(psi.data_ptr()), B, n, qdtype, st), "batch_reset")
-    for lpos, nl, ng, tab in segment_tables(ansatz, lb, U.device):
-        _check(lib.qsv_batch_segment_forward(ctypes.c_void_p(psi.data_ptr()), B, n, qdtype, nl, nat.ip(lpos), ng,
-                                             ctypes.c_void_p(tab.data_ptr()), ctypes.c_void_p(U.data_ptr()), st),
+    for lpos, nl, ngr, gtab, ng, tab in segment_tables(ansatz, lb, U.device):
+        _check(lib.qsv_batch_segment_forward(ctypes.c_void_p(psi.data_ptr()), B, n, qdtype, nl, nat.ip(lpos), ngr,
+                                             ctypes.c_void_p(gtab.data_ptr()), ng, ctypes.c_void_p(tab.data_ptr()),
+                                             ctypes.c_void_p(U.data_ptr()), st),
                "segment_forward")
     return psi
 
@@ -203,10 +247,11 @@ def adjoint_sweep_segmented(ansatz: Ansatz, psi, lam, Ud, qdtype, lb: int) -> to
     P = ansatz.nparams
     grads = torch.zeros((B, P), dtype=torch.float64, device=psi.device)
     st = ctypes.c_void_p(_stream_ptr())
-    for lpos, nl, ng, tab in reversed(segment_tables(ansatz, lb, psi.device)):
+    for lpos, nl, ngr, gtab, ng, tab in reversed(segment_tables(ansatz, lb, psi.device)):
         _check(lib.qsv_batch_segment_adjoint(ctypes.c_void_p(psi.data_ptr()), ctypes.c_void_p(lam.data_ptr()), B,
-                                             ansatz.n, qdtype, nl, nat.ip(lpos), ng, ctypes.c_void_p(tab.data_ptr()),
-                                             ctypes.c_void_p(Ud.data_ptr()), ctypes.c_void_p(grads.data_ptr()), P, st),
+                                             ansatz.n, qdtype, nl, nat.ip(lpos), ngr, ctypes.c_void_p(gtab.data_ptr()),
+                                             ng, ctypes.c_void_p(tab.data_ptr()), ctypes.c_void_p(Ud.data_ptr()),
+                                             ctypes.c_void_p(grads.data_ptr()), P, st),
                "segment_adjoint")
     return grads
 
@@ -239,7 +284,7 @@ class SumZExpectation(torch.autograd.Function):
         ctx.ansatz, ctx.qdtype = ansatz, qdtype
         ctx.buffers = (psi, lam, Ud, scratch)
         ctx.tdtype = thetas.dtype
-        ctx.segmented, ctx.lb = segmented, lb
+        ctx.segmented, ctx.lb = segmented, local_bits(cdtype, backward=True)
         return energies.to(thetas.dtype)
 
     @staticmethod

@@ -217,44 +217,170 @@ __global__ void k_batch_zero(CT<R>* psi, int n, int nsets) {
 // chunk is the 2^LB amplitudes with fixed values of the other n-LB bits, gathered into
 // shared memory, and every gate of the segment is applied there before the chunk is
 // scattered back: one pass over the state per segment instead of one per gate.
-// Gate descriptors (SegGate) name local bits; matrices are looked up per set.
+//
+// Inside a segment the gates come in groups whose local bits number at most 3: a
+// thread loads an item of 2^nb amplitudes (one value of the chunk's other bits), applies
+// all the group's gates to it in registers, and stores it back — one shared-memory pass
+// per group rather than per gate.
 struct SegGate {
-  int32_t tbit;   // local target bit
-  int32_t cbit;   // local control bit, -1 if none
+  int32_t tbit;   // target: index (0..nb-1) among its group's bits
+  int32_t cbit;   // control: index among the group's bits, -1 if none
   int32_t g;      // gate index: matrices at mats[(g * nsets + s) * 4 ...]
   int32_t gp;     // (generator << 24) | parameter index; generator 0 none, 1 Y, 2 Z
+};
+struct SegGroup {
+  int32_t nb;     // local bits of the group (1..3)
+  int32_t bits;   // the bits (local positions), ascending, 8 bits each
+  int32_t first;  // first gate of the group in the segment's gate table
+  int32_t count;  // gates in the group (<= SEG_GROUP_GATES)
 };
 constexpr int SEG_THREADS = 512;
 constexpr int SEG_MAX_GATES = 512;
 constexpr int SEG_MAX_PARAMS = 256;
+constexpr int SEG_GROUP_GATES = 8;
 
 struct SegArgs {
-  int n, nsets, lb, ngates;
+  int n, nsets, lb, ngates, ngroups;
   int lpos[16];
   uint64_t nchunks;
 };
 
-// Applies gate m (2x2, per set) to the pairs of local bit t (with local control c >= 0).
-template <typename R>
-__device__ __forceinline__ void seg_apply(CT<R>* v, int lb, int t, int c, const CT<R> m[4]) {
-  const int npairs = 1 << (lb - 1 - (c >= 0 ? 1 : 0));
-  const int lo = c >= 0 ? min(t, c) : t, hi = c >= 0 ? max(t, c) : t;
-  for (int k = threadIdx.x; k < npairs; k += blockDim.x) {
-    int i0 = ((k >> lo) << (lo + 1)) | (k & ((1 << lo) - 1));
-    if (c >= 0) {
-      i0 = ((i0 >> hi) << (hi + 1)) | (i0 & ((1 << hi) - 1));
-      i0 |= 1 << c;
-    }
-    const int i1 = i0 | (1 << t);
-    const CT<R> x = v[i0], y = v[i1];
+// Shared-memory position of chunk element e: one padding amplitude every 16, so items
+// whose group owns the lowest bits (lanes 8 or more amplitudes apart) spread over the
+// banks instead of hitting two of them.
+__device__ __forceinline__ int phys(int e) { return e + (e >> 4); }
+
+// 2x2 matrix m on register bit J of an item (pairs with control bit c set, c >= 0).
+template <typename R, int NB, int J>
+__device__ __forceinline__ void reg_apply(CT<R>* a, int c, const CT<R> m[4]) {
+#pragma unroll
+  for (int i0 = 0; i0 < (1 << NB); ++i0) {
+    if ((i0 >> J) & 1) continue;
+    if (c >= 0 && !((i0 >> c) & 1)) continue;
+    const int i1 = i0 | (1 << J);
+    const CT<R> x = a[i0], y = a[i1];
     CT<R> o0, o1;
     o0.x = R(0); o0.y = R(0); o1 = o0;
     o0 = qsv_cfma(m[0], x, o0);
     o0 = qsv_cfma(m[1], y, o0);
     o1 = qsv_cfma(m[2], x, o1);
     o1 = qsv_cfma(m[3], y, o1);
-    v[i0] = o0;
-    v[i1] = o1;
+    a[i0] = o0;
+    a[i1] = o1;
+  }
+}
+
+template <typename R, int NB>
+__device__ __forceinline__ void reg_gate(CT<R>* a, int j, int c, const CT<R> m[4]) {
+  if (j == 0) reg_apply<R, NB, 0>(a, c, m);
+  if constexpr (NB > 1) if (j == 1) reg_apply<R, NB, 1>(a, c, m);
+  if constexpr (NB > 2) if (j == 2) reg_apply<R, NB, 2>(a, c, m);
+}
+
+// Im <lambda| P |psi> over the pairs of register bit J (P = Z: gen 2, Y: gen 1).
+template <typename R, int NB, int J>
+__device__ __forceinline__ R reg_gen(const CT<R>* x, const CT<R>* l, int gen) {
+  R part = R(0);
+#pragma unroll
+  for (int i0 = 0; i0 < (1 << NB); ++i0) {
+    if ((i0 >> J) & 1) continue;
+    const int i1 = i0 | (1 << J);
+    const CT<R> x0 = x[i0], y0 = x[i1], l0 = l[i0], l1 = l[i1];
+    if (gen == 2)
+      part += (l0.x * x0.y - l0.y * x0.x) - (l1.x * y0.y - l1.y * y0.x);
+    else
+      part += (l1.x * x0.x + l1.y * x0.y) - (l0.x * y0.x + l0.y * y0.y);
+  }
+  return part;
+}
+
+template <typename R, int NB>
+__device__ __forceinline__ R reg_gen_any(const CT<R>* x, const CT<R>* l, int j, int gen) {
+  if (j == 0) return reg_gen<R, NB, 0>(x, l, gen);
+  if constexpr (NB > 1) if (j == 1) return reg_gen<R, NB, 1>(x, l, gen);
+  if constexpr (NB > 2) if (j == 2) return reg_gen<R, NB, 2>(x, l, gen);
+  return R(0);
+}
+
+// Shared-memory offsets of an item's 2^NB amplitudes: item it -> zeros inserted at the
+// group's bits; amplitude i adds the bits of i.
+template <int NB>
+__device__ __forceinline__ int item_base(int it, const int* gb) {
+  int x = it;
+#pragma unroll
+  for (int j = 0; j < NB; ++j) x = ((x >> gb[j]) << (gb[j] + 1)) | (x & ((1 << gb[j]) - 1));
+  return x;
+}
+
+template <typename R, int NB>
+__device__ __forceinline__ void group_forward(CT<R>* v, int chunk, const int* gb, const SegGate* gsh,
+                                              const CT<R>* msh, int first, int count) {
+  constexpr int D = 1 << NB;
+  int mb[NB];
+#pragma unroll
+  for (int j = 0; j < NB; ++j) mb[j] = 1 << gb[j];
+  auto off = [&](int i) {
+    int o = 0;
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+      if ((i >> j) & 1) o |= mb[j];
+    return o;
+  };
+  for (int it = threadIdx.x; it < (chunk >> NB); it += blockDim.x) {
+    const int b = item_base<NB>(it, gb);
+    CT<R> a[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) a[i] = v[phys(b + off(i))];
+    for (int k = first; k < first + count; ++k) {
+      const SegGate g = gsh[k];
+      const CT<R> m[4] = {msh[4 * k], msh[4 * k + 1], msh[4 * k + 2], msh[4 * k + 3]};
+      reg_gate<R, NB>(a, g.tbit, g.cbit, m);
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i) v[phys(b + off(i))] = a[i];
+  }
+}
+
+// Reverse over a group's gates on each item of psi and lambda; part[k - first] collects
+// this thread's generator terms.
+template <typename R, int NB>
+__device__ __forceinline__ void group_adjoint(CT<R>* v, CT<R>* l, int chunk, const int* gb, const SegGate* gsh,
+                                              const CT<R>* msh, int first, int count, R* part) {
+  constexpr int D = 1 << NB;
+  int mb[NB];
+#pragma unroll
+  for (int j = 0; j < NB; ++j) mb[j] = 1 << gb[j];
+  auto off = [&](int i) {
+    int o = 0;
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+      if ((i >> j) & 1) o |= mb[j];
+    return o;
+  };
+  for (int it = threadIdx.x; it < (chunk >> NB); it += blockDim.x) {
+    const int b = item_base<NB>(it, gb);
+    CT<R> a[D], la[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      a[i] = v[phys(b + off(i))];
+      la[i] = l[phys(b + off(i))];
+    }
+#pragma unroll
+    for (int q = SEG_GROUP_GATES - 1; q >= 0; --q) {
+      if (q >= count) continue;
+      const int k = first + q;
+      const SegGate g = gsh[k];
+      const int gen = (g.gp >> 24) & 3;
+      if (gen) part[q] += reg_gen_any<R, NB>(a, la, g.tbit, gen);
+      const CT<R> m[4] = {msh[4 * k], msh[4 * k + 1], msh[4 * k + 2], msh[4 * k + 3]};
+      reg_gate<R, NB>(a, g.tbit, g.cbit, m);
+      reg_gate<R, NB>(la, g.tbit, g.cbit, m);
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      v[phys(b + off(i))] = a[i];
+      l[phys(b + off(i))] = la[i];
+    }
   }
 }
 
@@ -263,7 +389,7 @@ __device__ __forceinline__ void seg_apply(CT<R>* v, int lb, int t, int c, const 
 template <typename R, bool TWO>
 __device__ __forceinline__ void seg_gather(const CT<R>* src, const CT<R>* src2, CT<R>* v, CT<R>* v2, int chunk,
                                            uint64_t base, const uint64_t* dlo, const uint64_t* dhi) {
-  constexpr int GB = sizeof(R) == 4 ? 16 : 8;
+  constexpr int GB = TWO ? (sizeof(R) == 4 ? 8 : 4) : (sizeof(R) == 4 ? 16 : 8);
   for (int e0 = threadIdx.x; e0 < chunk; e0 += GB * blockDim.x) {
     CT<R> t[GB], t2[TWO ? GB : 1];
 #pragma unroll
@@ -279,18 +405,18 @@ __device__ __forceinline__ void seg_gather(const CT<R>* src, const CT<R>* src2, 
     for (int j = 0; j < GB; ++j) {
       const int e = e0 + j * blockDim.x;
       if (e < chunk) {
-        v[e] = t[j];
-        if constexpr (TWO) v2[e] = t2[j];
+        v[phys(e)] = t[j];
+        if constexpr (TWO) v2[phys(e)] = t2[j];
       }
     }
   }
 }
 
-// The segment's gate records and this set's matrices, staged in shared memory once per
-// CTA (otherwise every gate starts with two dependent global loads).
+// The segment's gate records, groups and this set's matrices, staged in shared memory
+// once per CTA (otherwise every gate starts with two dependent global loads).
 template <typename R>
-__device__ __forceinline__ void seg_stage(const SegGate* gates, const CT<R>* mats, const SegArgs& a, int s,
-                                          SegGate* gsh, CT<R>* msh) {
+__device__ __forceinline__ void seg_stage(const SegGate* gates, const SegGroup* groups, const CT<R>* mats,
+                                          const SegArgs& a, int s, SegGate* gsh, SegGroup* grsh, CT<R>* msh) {
   for (int k = threadIdx.x; k < a.ngates; k += blockDim.x) {
     const SegGate g = gates[k];
     gsh[k] = g;
@@ -298,6 +424,7 @@ __device__ __forceinline__ void seg_stage(const SegGate* gates, const CT<R>* mat
 #pragma unroll
     for (int i = 0; i < 4; ++i) msh[4 * k + i] = mp[i];
   }
+  for (int k = threadIdx.x; k < a.ngroups; k += blockDim.x) grsh[k] = groups[k];
 }
 
 template <typename R>
@@ -314,51 +441,67 @@ __device__ __forceinline__ void seg_tables(const SegArgs& a, uint64_t* dlo, uint
   }
 }
 
+__device__ __forceinline__ void group_bits(const SegGroup& G, int* gb) {
+  gb[0] = G.bits & 0xFF;
+  gb[1] = (G.bits >> 8) & 0xFF;
+  gb[2] = (G.bits >> 16) & 0xFF;
+}
+
 template <typename R>
 __global__ void __launch_bounds__(SEG_THREADS, 2)
     k_seg_forward(CT<R>* __restrict__ psi, const CT<R>* __restrict__ mats, const SegGate* __restrict__ gates,
-                  const __grid_constant__ SegArgs a) {
+                  const SegGroup* __restrict__ groups, const __grid_constant__ SegArgs a) {
   extern __shared__ __align__(16) uint8_t seg_smem[];
   const int chunk = 1 << a.lb;
   CT<R>* v = reinterpret_cast<CT<R>*>(seg_smem);
-  CT<R>* msh = v + chunk;                                   // [ngates][4] this set's matrices
+  CT<R>* msh = v + phys(chunk);                             // [ngates][4] this set's matrices
   SegGate* gsh = reinterpret_cast<SegGate*>(msh + 4 * a.ngates);
+  SegGroup* grsh = reinterpret_cast<SegGroup*>(gsh + a.ngates);
   __shared__ uint64_t dlo[128], dhi[128];
   const int s = blockIdx.y;
   CT<R>* st = psi + ((uint64_t)s << a.n);
   seg_tables<R>(a, dlo, dhi);
-  seg_stage<R>(gates, mats, a, s, gsh, msh);
+  seg_stage<R>(gates, groups, mats, a, s, gsh, grsh, msh);
   __syncthreads();
   for (uint64_t ch = blockIdx.x; ch < a.nchunks; ch += gridDim.x) {
     const uint64_t base = qsv_insert_zeros(ch, a.lpos, a.lb);
     seg_gather<R, false>(st, nullptr, v, nullptr, chunk, base, dlo, dhi);
     __syncthreads();
-    for (int k = 0; k < a.ngates; ++k) {
-      const SegGate g = gsh[k];
-      const CT<R> m[4] = {msh[4 * k], msh[4 * k + 1], msh[4 * k + 2], msh[4 * k + 3]};
-      seg_apply<R>(v, a.lb, g.tbit, g.cbit, m);
+    for (int q = 0; q < a.ngroups; ++q) {
+      const SegGroup G = grsh[q];
+      int gb[3];
+      group_bits(G, gb);
+      if (G.nb == 1)
+        group_forward<R, 1>(v, chunk, gb, gsh, msh, G.first, G.count);
+      else if (G.nb == 2)
+        group_forward<R, 2>(v, chunk, gb, gsh, msh, G.first, G.count);
+      else
+        group_forward<R, 3>(v, chunk, gb, gsh, msh, G.first, G.count);
       __syncthreads();
     }
-    for (int e = threadIdx.x; e < chunk; e += blockDim.x) st[base + dlo[e & 127] + dhi[e >> 7]] = v[e];
+    for (int e = threadIdx.x; e < chunk; e += blockDim.x) st[base + dlo[e & 127] + dhi[e >> 7]] = v[phys(e)];
     __syncthreads();
   }
 }
 
-// Reverse sweep over one segment: for k = last .. first: [generator: accumulate
-// Im<lambda| P |psi> over the chunk]; psi, lambda <- M psi, M lambda (M = U^+).  Per
+// Reverse sweep over one segment: groups last to first, each group's gates last to
+// first: [generator: Im<lambda| P |psi>]; psi, lambda <- M psi, M lambda (M = U^+).  Per
 // warp FP64 accumulators in shared memory, one atomicAdd per parameter per CTA.
+// Two CTAs per SM for complex64 (registers capped at 64); complex128 items need more.
 template <typename R>
-__global__ void __launch_bounds__(SEG_THREADS)
+__global__ void __launch_bounds__(SEG_THREADS, sizeof(R) == 4 ? 2 : 1)
     k_seg_adjoint(CT<R>* __restrict__ psi, CT<R>* __restrict__ lam, const CT<R>* __restrict__ mats_dagger,
-                  const SegGate* __restrict__ gates, const __grid_constant__ SegArgs a, double* __restrict__ grads,
-                  int grad_stride) {
+                  const SegGate* __restrict__ gates, const SegGroup* __restrict__ groups,
+                  const __grid_constant__ SegArgs a, double* __restrict__ grads, int grad_stride) {
   extern __shared__ __align__(16) uint8_t seg_smem[];
   const int chunk = 1 << a.lb;
   CT<R>* v = reinterpret_cast<CT<R>*>(seg_smem);
-  CT<R>* l = v + chunk;
-  double* accw = reinterpret_cast<double*>(l + chunk);  // [SEG_MAX_PARAMS][16 warps]
-  CT<R>* msh = reinterpret_cast<CT<R>*>(accw + SEG_MAX_PARAMS * 16);  // [ngates][4]
+  CT<R>* l = v + phys(chunk);
+  const int nrows = min(a.ngates, SEG_MAX_PARAMS);  // generator slots (<= gates)
+  double* accw = reinterpret_cast<double*>(l + phys(chunk));  // [nrows][16 warps]
+  CT<R>* msh = reinterpret_cast<CT<R>*>(accw + nrows * 16);  // [ngates][4]
   SegGate* gsh = reinterpret_cast<SegGate*>(msh + 4 * a.ngates);
+  SegGroup* grsh = reinterpret_cast<SegGroup*>(gsh + a.ngates);
   __shared__ uint64_t dlo[128], dhi[128];
   __shared__ int slot_of[SEG_MAX_GATES];
   const int s = blockIdx.y;
@@ -367,61 +510,44 @@ __global__ void __launch_bounds__(SEG_THREADS)
   CT<R>* sp = psi + ((uint64_t)s << a.n);
   CT<R>* sl = lam + ((uint64_t)s << a.n);
   seg_tables<R>(a, dlo, dhi);
-  seg_stage<R>(gates, mats_dagger, a, s, gsh, msh);
+  seg_stage<R>(gates, groups, mats_dagger, a, s, gsh, grsh, msh);
   if (threadIdx.x == 0) {
     int np = 0;
-    for (int k = 0; k < a.ngates; ++k) slot_of[k] = ((gates[k].gp >> 24) && np < SEG_MAX_PARAMS) ? np++ : -1;
+    for (int k = 0; k < a.ngates; ++k) slot_of[k] = (((gates[k].gp >> 24) & 3) && np < nrows) ? np++ : -1;
   }
-  for (int i = threadIdx.x; i < SEG_MAX_PARAMS * 16; i += blockDim.x) accw[i] = 0.0;
+  for (int i = threadIdx.x; i < nrows * 16; i += blockDim.x) accw[i] = 0.0;
   __syncthreads();
   for (uint64_t ch = blockIdx.x; ch < a.nchunks; ch += gridDim.x) {
     const uint64_t base = qsv_insert_zeros(ch, a.lpos, a.lb);
     seg_gather<R, true>(sp, sl, v, l, chunk, base, dlo, dhi);
     __syncthreads();
-    for (int k = a.ngates - 1; k >= 0; --k) {
-      const SegGate g = gsh[k];
-      const int gen = g.gp >> 24;
-      const CT<R> m00 = msh[4 * k], m01 = msh[4 * k + 1], m10 = msh[4 * k + 2], m11 = msh[4 * k + 3];
-      // One pass over the pairs of the target (with the control set): the generator
-      // term Im<lambda| P |psi> from the current pair, then U^+ on psi and lambda.
-      const int t = g.tbit, c = g.cbit;
-      const int npairs = chunk >> (c >= 0 ? 2 : 1);
-      const int lo = c >= 0 ? min(t, c) : t, hi = c >= 0 ? max(t, c) : t;
-      R part = R(0);
-      for (int kk = threadIdx.x; kk < npairs; kk += blockDim.x) {
-        int i0 = ((kk >> lo) << (lo + 1)) | (kk & ((1 << lo) - 1));
-        if (c >= 0) i0 = (((i0 >> hi) << (hi + 1)) | (i0 & ((1 << hi) - 1))) | (1 << c);
-        const int i1 = i0 | (1 << t);
-        const CT<R> x = v[i0], y = v[i1], l0 = l[i0], l1 = l[i1];
-        if (gen == 2)
-          part += (l0.x * x.y - l0.y * x.x) - (l1.x * y.y - l1.y * y.x);
-        else if (gen == 1)
-          part += (l1.x * x.x + l1.y * x.y) - (l0.x * y.x + l0.y * y.y);
-        CT<R> o0, o1, q0, q1;
-        o0.x = R(0); o0.y = R(0); o1 = o0; q0 = o0; q1 = o0;
-        o0 = qsv_cfma(m00, x, o0);
-        o0 = qsv_cfma(m01, y, o0);
-        o1 = qsv_cfma(m10, x, o1);
-        o1 = qsv_cfma(m11, y, o1);
-        q0 = qsv_cfma(m00, l0, q0);
-        q0 = qsv_cfma(m01, l1, q0);
-        q1 = qsv_cfma(m10, l0, q1);
-        q1 = qsv_cfma(m11, l1, q1);
-        v[i0] = o0;
-        v[i1] = o1;
-        l[i0] = q0;
-        l[i1] = q1;
-      }
-      if (gen) {
-        const double w = warp_sum_d((double)part);
+    for (int q = a.ngroups - 1; q >= 0; --q) {
+      const SegGroup G = grsh[q];
+      int gb[3];
+      group_bits(G, gb);
+      R part[SEG_GROUP_GATES];
+#pragma unroll
+      for (int i = 0; i < SEG_GROUP_GATES; ++i) part[i] = R(0);
+      if (G.nb == 1)
+        group_adjoint<R, 1>(v, l, chunk, gb, gsh, msh, G.first, G.count, part);
+      else if (G.nb == 2)
+        group_adjoint<R, 2>(v, l, chunk, gb, gsh, msh, G.first, G.count, part);
+      else
+        group_adjoint<R, 3>(v, l, chunk, gb, gsh, msh, G.first, G.count, part);
+#pragma unroll
+      for (int i = 0; i < SEG_GROUP_GATES; ++i) {
+        if (i >= G.count) continue;
+        const int k = G.first + i;
+        if (!((gsh[k].gp >> 24) & 3)) continue;
+        const double w = warp_sum_d((double)part[i]);
         if (lane == 0 && slot_of[k] >= 0) accw[slot_of[k] * 16 + warp] += w;
       }
       __syncthreads();
     }
     for (int e = threadIdx.x; e < chunk; e += blockDim.x) {
       const uint64_t ad = base + dlo[e & 127] + dhi[e >> 7];
-      sp[ad] = v[e];
-      sl[ad] = l[e];
+      sp[ad] = v[phys(e)];
+      sl[ad] = l[phys(e)];
     }
     __syncthreads();
   }
@@ -573,9 +699,12 @@ int qsv_batch_adjoint_step(void* psi, void* lam, int nsets, int n, int dtype, in
 
 // ---- segmented execution ------------------------------------------------------------
 namespace {
-int seg_args(int n, int nsets, int dtype, int lb, const int* lpos, int ngates, bool two, SegArgs& a, size_t& smem) {
-  if (n < 1 || n > QSV_MAXN || nsets < 1 || nsets > 65535 || !lpos || ngates < 0 || ngates > SEG_MAX_GATES)
-    return set_error(nullptr, QSV_ERR_INVALID, "bad segment (n=%d nsets=%d ngates=%d)", n, nsets, ngates);
+int seg_args(int n, int nsets, int dtype, int lb, const int* lpos, int ngroups, int ngates, bool two, SegArgs& a,
+             size_t& smem) {
+  if (n < 1 || n > QSV_MAXN || nsets < 1 || nsets > 65535 || !lpos || ngates < 0 || ngates > SEG_MAX_GATES ||
+      ngroups < 0 || ngroups > ngates)
+    return set_error(nullptr, QSV_ERR_INVALID, "bad segment (n=%d nsets=%d groups=%d gates=%d)", n, nsets, ngroups,
+                     ngates);
   if (dtype != QSV_C64 && dtype != QSV_C128) return set_error(nullptr, QSV_ERR_INVALID, "unknown dtype %d", dtype);
   const size_t amp = dtype == QSV_C64 ? 8 : 16;
   const int lbmax = dtype == QSV_C64 ? 13 : 12;
@@ -589,9 +718,12 @@ int seg_args(int n, int nsets, int dtype, int lb, const int* lpos, int ngates, b
   a.nsets = nsets;
   a.lb = lb;
   a.ngates = ngates;
+  a.ngroups = ngroups;
   a.nchunks = 1ull << (n - lb);
-  smem = ((size_t)1 << lb) * amp * (two ? 2 : 1) + (two ? (size_t)SEG_MAX_PARAMS * 16 * sizeof(double) : 0) +
-         (size_t)ngates * (4 * amp + sizeof(SegGate));
+  const size_t padded = ((size_t)1 << lb) + ((size_t)1 << lb) / 16;  // one padding amplitude per 16
+  smem = padded * amp * (two ? 2 : 1) +
+         (two ? (size_t)std::min(ngates, SEG_MAX_PARAMS) * 16 * sizeof(double) : 0) +
+         (size_t)ngates * (4 * amp + sizeof(SegGate) + sizeof(SegGroup));
   return QSV_OK;
 }
 
@@ -611,47 +743,50 @@ dim3 seg_grid(uint64_t nchunks, int nsets, int per_sm) {
 
 extern "C" {
 
-int qsv_batch_segment_forward(void* psi, int nsets, int n, int dtype, int lb, const int* lpos, int ngates,
-                              const void* gates_dev, const void* mats, void* stream) {
-  if (!psi || !mats || (ngates > 0 && !gates_dev)) return set_error(nullptr, QSV_ERR_INVALID, "null pointer");
+int qsv_batch_segment_forward(void* psi, int nsets, int n, int dtype, int lb, const int* lpos, int ngroups,
+                              const void* groups_dev, int ngates, const void* gates_dev, const void* mats,
+                              void* stream) {
+  if (!psi || !mats || (ngates > 0 && (!gates_dev || !groups_dev)))
+    return set_error(nullptr, QSV_ERR_INVALID, "null pointer");
   SegArgs a;
   size_t smem = 0;
-  int rc = seg_args(n, nsets, dtype, lb, lpos, ngates, false, a, smem);
+  int rc = seg_args(n, nsets, dtype, lb, lpos, ngroups, ngates, false, a, smem);
   if (rc || ngates == 0) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   const dim3 grid = seg_grid(a.nchunks, nsets, 2);
   if (dtype == QSV_C64) {
     if ((rc = seg_config(k_seg_forward<float>, smem, "segment_forward"))) return rc;
     k_seg_forward<float><<<grid, SEG_THREADS, smem, st>>>((float2*)psi, (const float2*)mats,
-                                                          (const SegGate*)gates_dev, a);
+                                                          (const SegGate*)gates_dev, (const SegGroup*)groups_dev, a);
   } else {
     if ((rc = seg_config(k_seg_forward<double>, smem, "segment_forward"))) return rc;
     k_seg_forward<double><<<grid, SEG_THREADS, smem, st>>>((double2*)psi, (const double2*)mats,
-                                                           (const SegGate*)gates_dev, a);
+                                                           (const SegGate*)gates_dev, (const SegGroup*)groups_dev, a);
   }
   return launch_check("segment_forward");
 }
 
-int qsv_batch_segment_adjoint(void* psi, void* lam, int nsets, int n, int dtype, int lb, const int* lpos, int ngates,
-                              const void* gates_dev, const void* mats_dagger, double* grads, int grad_stride,
-                              void* stream) {
-  if (!psi || !lam || !mats_dagger || !grads || (ngates > 0 && !gates_dev))
+int qsv_batch_segment_adjoint(void* psi, void* lam, int nsets, int n, int dtype, int lb, const int* lpos, int ngroups,
+                              const void* groups_dev, int ngates, const void* gates_dev, const void* mats_dagger,
+                              double* grads, int grad_stride, void* stream) {
+  if (!psi || !lam || !mats_dagger || !grads || (ngates > 0 && (!gates_dev || !groups_dev)))
     return set_error(nullptr, QSV_ERR_INVALID, "null pointer");
   SegArgs a;
   size_t smem = 0;
-  int rc = seg_args(n, nsets, dtype, lb, lpos, ngates, true, a, smem);
+  int rc = seg_args(n, nsets, dtype, lb, lpos, ngroups, ngates, true, a, smem);
   if (rc || ngates == 0) return rc;
   cudaStream_t st = (cudaStream_t)stream;
-  const dim3 grid = seg_grid(a.nchunks, nsets, 1);
+  const dim3 grid = seg_grid(a.nchunks, nsets, 2);
   if (dtype == QSV_C64) {
     if ((rc = seg_config(k_seg_adjoint<float>, smem, "segment_adjoint"))) return rc;
     k_seg_adjoint<float><<<grid, SEG_THREADS, smem, st>>>((float2*)psi, (float2*)lam, (const float2*)mats_dagger,
-                                                          (const SegGate*)gates_dev, a, grads, grad_stride);
+                                                          (const SegGate*)gates_dev, (const SegGroup*)groups_dev, a,
+                                                          grads, grad_stride);
   } else {
     if ((rc = seg_config(k_seg_adjoint<double>, smem, "segment_adjoint"))) return rc;
     k_seg_adjoint<double><<<grid, SEG_THREADS, smem, st>>>((double2*)psi, (double2*)lam,
-                                                           (const double2*)mats_dagger, (const SegGate*)gates_dev, a,
-                                                           grads, grad_stride);
+                                                           (const double2*)mats_dagger, (const SegGate*)gates_dev,
+                                                           (const SegGroup*)groups_dev, a, grads, grad_stride);
   }
   return launch_check("segment_adjoint");
 }

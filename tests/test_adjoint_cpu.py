@@ -79,3 +79,35 @@ def test_segment_plan_is_the_same_circuit():
         numpy.testing.assert_allclose(got, want, atol=1e-12)
         if lb < n:
             assert len(segs) > 1
+
+
+def test_segment_device_tables_decode_to_the_circuit():
+    """The group / gate records the kernels read (decoded back to global qubits through
+    each segment's local bits and each group's bits) replay the circuit exactly."""
+    n, layers = 10, 3
+    a = adjoint.Ansatz(n, layers)
+    rng = numpy.random.default_rng(8)
+    th = rng.uniform(0, 2 * numpy.pi, a.nparams)
+    mats = circuits.ansatz_layers(n, layers, th)
+    v0 = rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)
+    want = v0.copy()
+    for g in mats:
+        want = sv.kronselect_dot(g, want, n)
+    for lb in (7, 9):
+        got = v0.copy()
+        seen = []
+        for lpos, nl, ngr, gtab, ng, tab in adjoint.segment_tables(a, lb, "cpu"):
+            lpos = list(lpos)
+            for nb, packed, first, count in gtab.tolist():
+                gbits = [(packed >> (8 * j)) & 0xFF for j in range(nb)]
+                assert 1 <= nb <= 3 and gbits == sorted(gbits) and count <= adjoint.GROUP_GATES
+                for tb, cb, gi, gp in tab[first:first + count].tolist():
+                    kind, t, c, pi = a.gates()[gi]
+                    assert n - 1 - lpos[gbits[tb]] == t
+                    assert (cb < 0 and c < 0) or n - 1 - lpos[gbits[cb]] == c
+                    assert (gp >> 24) & 3 == {adjoint.RY: 1, adjoint.RZ: 2}.get(kind, 0)
+                    assert (gp >> 24) & 3 == 0 or (gp & 0xFFFFFF) == pi
+                    seen.append(gi)
+                    got = sv.kronselect_dot(mats[gi], got, n)
+        assert sorted(seen) == list(range(len(mats)))
+        numpy.testing.assert_allclose(got, want, atol=1e-12)
