@@ -78,26 +78,31 @@ def plan(gates: Sequence[GateOp], kmax: int = 6, lookahead: int = LOOKAHEAD) -> 
     return steps
 
 
-def _grow(remaining: Sequence[GateOp], start: int, kmax: int):
-    """Candidate block starting at remaining[start]: (chosen, rest, qubits, blocked)."""
-    S: set = set()
-    chosen: List[GateOp] = []
-    blocked: set = set()
-    rest: List[GateOp] = []
+def _grow(remaining: Sequence[GateOp], start: int, kmax: int, full_at: int):
+    """Candidate block starting at remaining[start].  Returns (chosen positions, qubit
+    mask, blocked mask, final): the scan stops early once the block is final (full_at
+    qubits and every one of them blocked: no later gate can join)."""
+    S = 0
+    nS = 0
+    blocked = 0
+    chosen: List[int] = []
     for i, g in enumerate(remaining):
-        q = g.qubits
+        q = g.qmask
         if i < start or (q & blocked) or g.width > kmax:
             blocked |= q
-            rest.append(g)
+            if nS >= full_at and (S & ~blocked) == 0:
+                return chosen, S, blocked, True
             continue
         merged = S | q
-        if len(merged) <= kmax:
-            S = merged
-            chosen.append(g)
+        nm = bin(merged).count("1")
+        if nm <= kmax:
+            S, nS = merged, nm
+            chosen.append(i)
         else:
             blocked |= q
-            rest.append(g)
-    return chosen, rest, S, blocked
+            if nS >= full_at and (S & ~blocked) == 0:
+                return chosen, S, blocked, True
+    return chosen, S, blocked, nS >= full_at and (S & ~blocked) == 0
 
 
 def plan_prefix(gates: Sequence[GateOp], kmax: int = 6, nqubits=None,
@@ -119,17 +124,17 @@ def plan_prefix(gates: Sequence[GateOp], kmax: int = 6, nqubits=None,
             remaining = remaining[1:]
             continue
         best = None
+        full_at = kmax if nqubits is None else min(kmax, nqubits)
         for start in range(min(lookahead, len(remaining))):
             if remaining[start].width > kmax:
                 continue
-            chosen, rest, S, blocked = _grow(remaining, start, kmax)
-            if nqubits is not None:
-                full = len(S) == kmax or len(S) == nqubits
-                if not (full and S <= blocked):
-                    return steps, remaining
-            work = sum(g.amp_update_weight() for g in chosen)
+            chosen, S, blocked, final = _grow(remaining, start, kmax, full_at)
+            if nqubits is not None and not final:
+                return steps, remaining
+            work = sum(remaining[i].amp_update_weight() for i in chosen)
             if best is None or work > best[0]:
-                best = (work, chosen, rest)
-        remaining = best[2]
-        steps.append(_emit(best[1]))
+                best = (work, chosen)
+        picked = set(best[1])
+        steps.append(_emit([remaining[i] for i in best[1]]))
+        remaining = [g for i, g in enumerate(remaining) if i not in picked]
     return steps, []

@@ -47,9 +47,14 @@ class GateOp:
     perm: Any = None
     swap_b: Tuple[int, ...] = ()
     qubits: frozenset = field(default_factory=frozenset)
+    qmask: int = 0  # the qubits as a bit mask (bit q <-> qubit q), for the planner
 
     def __post_init__(self):
         self.qubits = frozenset(self.targets) | frozenset(self.controls) | frozenset(self.swap_b)
+        m = 0
+        for q in self.qubits:
+            m |= 1 << int(q)
+        self.qmask = m
 
     @property
     def width(self) -> int:
