@@ -118,6 +118,33 @@ int qsv_plan_create(qsv_state* s, int nblocks, const int* ks, const int* targets
 int qsv_plan_launch(qsv_state* s, const qsv_plan* p, int first, int count);
 int qsv_plan_destroy(qsv_plan* p);
 
+/* Fusion planning on the host (no reference counterpart).  Gates are given as qubit bit
+ * masks (bit q <-> qubit q) and amp-update weights.  Each round grows up to lookahead
+ * candidate blocks (candidate s leaves the first s pending gates out, then takes every
+ * later gate whose qubits fit in kmax and are not blocked by a gate left out before it;
+ * a left-out gate blocks its qubits) and keeps the one with the most weight; a gate
+ * wider than kmax at the front is its own step.  nqubits < 0: plan every gate.
+ * nqubits >= 0 (prefix mode): stop at the first round later gates could change (a
+ * candidate is final once it holds min(kmax, nqubits) qubits, all blocked; strict: all
+ * candidates must be final, else the best one), except that a round is decided on the
+ * pending gates anyway while more than min_pending (> 0) are pending: the block is just
+ * as valid, it may only be smaller than later gates would have allowed.  Output: the
+ * planned gates in step
+ * order (order_out, ngates entries of room), step s = order_out[step_start_out[s] ..
+ * step_start_out[s+1]) (ngates + 1 entries of room), nsteps, number of planned gates. */
+int qsv_fusion_plan(int ngates, const uint64_t* qmask, const double* weight, int kmax,
+                    int lookahead, int nqubits, int strict, int min_pending, int* order_out,
+                    int* step_start_out, int* nsteps_out, int* nplanned_out);
+/* Dense matrices of fused blocks (host, threads across blocks; no reference
+ * counterpart).  Block b has block_k[b] qubits (block_qubits, ascending: the first is
+ * the MSB of the block index) and block_ngates[b] gates; gate g acts on gate_nq[g]
+ * qubits (gate_qubits, its first the MSB of its index) with the row-major complex
+ * matrix gate_mats (2^q x 2^q, interleaved re/im).  out: block b's 2^k x 2^k complex
+ * matrix = product of its gates in order (later gates on the left). */
+int qsv_block_matrices(int nblocks, const int* block_k, const int* block_qubits,
+                       const int* block_ngates, const int* gate_nq, const int* gate_qubits,
+                       const double* gate_mats, double* out);
+
 /* Access-mode autotuning of the tensor-core block kernel.  No reference counterpart
  * (the reference has no GPU path).  A placement class is (k, low_mask): bit p of
  * low_mask set <-> a target on address bit p, p < 7 (targets on higher bits do not

@@ -147,8 +147,9 @@ class GpuBackend(StateType):
     """
 
     FLUSH_LIMIT = 8192
-    # Queued gates beyond this are planned incrementally: blocks that no later gate can
-    # join are launched while the executor keeps feeding gates.
+    # Queued gates beyond this are planned incrementally and launched while the executor
+    # keeps feeding gates: rounds whose best block no later gate can join, and any round
+    # while more than this many gates are queued.
     PARTIAL_FLUSH = 384
 
     # Gates needed before the fusion width is measured on them (fewer: the static rule).
@@ -268,7 +269,8 @@ class GpuBackend(StateType):
 
     def _partial_flush(self) -> None:
         self._tune_width()
-        steps, rest = plan_prefix(self._pending, kmax=self._kmax(), nqubits=self.n)
+        steps, rest = plan_prefix(self._pending, kmax=self._kmax(), nqubits=self.n, strict=False,
+                                  min_pending=self.PARTIAL_FLUSH)
         if steps:
             self._pending = rest
             self.run_plan(steps)

@@ -1,0 +1,231 @@
+// Host-side fusion planning and block-matrix construction (no device code).
+//
+// qsv_fusion_plan is the planner of qip_gb300/fusion.py in native code: each round
+// grows up to `lookahead` candidate blocks — candidate s leaves the first s pending
+// gates out and then scans in program order; a gate joins when its qubits fit (at most
+// kmax) and none of them is blocked by a gate left out earlier; a left-out gate blocks
+// its qubits — and keeps the candidate with the most work (sum of amp-update
+// weights, first on ties).  A candidate is final once it is full and all its qubits
+// are blocked; prefix mode (nqubits >= 0) stops at the first round that later gates
+// could still change (strict: some candidate is not final; relaxed: the best is not),
+// unless more than min_pending gates are pending (then the round is decided anyway).
+//
+// qsv_block_matrices multiplies each block's gates into its 2^k x 2^k matrix, blocks
+// spread over host threads.
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "qsv_internal.cuh"
+
+using namespace qsv;
+
+namespace {
+
+struct Cand {
+  std::vector<int> chosen;  // positions in the pending list
+  double work = 0.0;
+  bool final = false;
+};
+
+void grow(const std::vector<int>& rem, int start, const uint64_t* qmask, const int* width, const double* weight,
+          int kmax, int full_at, Cand& c) {
+  uint64_t S = 0, blocked = 0;
+  int nS = 0;
+  c.chosen.clear();
+  c.work = 0.0;
+  c.final = false;
+  const int m = (int)rem.size();
+  for (int i = 0; i < m; ++i) {
+    const int g = rem[(size_t)i];
+    const uint64_t q = qmask[g];
+    if (i < start || (q & blocked) || width[g] > kmax) {
+      blocked |= q;
+      if (nS >= full_at && (S & ~blocked) == 0) {
+        c.final = true;
+        return;
+      }
+      continue;
+    }
+    const uint64_t merged = S | q;
+    const int nm = __builtin_popcountll(merged);
+    if (nm <= kmax) {
+      S = merged;
+      nS = nm;
+      c.chosen.push_back(i);
+      c.work += weight[g];
+    } else {
+      blocked |= q;
+      if (nS >= full_at && (S & ~blocked) == 0) {
+        c.final = true;
+        return;
+      }
+    }
+  }
+  c.final = nS >= full_at && (S & ~blocked) == 0;
+}
+
+}  // namespace
+
+extern "C" int qsv_fusion_plan(int ngates, const uint64_t* qmask, const double* weight, int kmax, int lookahead,
+                               int nqubits, int strict, int min_pending, int* order_out, int* step_start_out,
+                               int* nsteps_out, int* nplanned_out) {
+  if (ngates < 0 || (ngates > 0 && (!qmask || !weight || !order_out || !step_start_out)) || !nsteps_out ||
+      !nplanned_out || kmax < 1 || kmax > 62 || lookahead < 1)
+    return set_error(nullptr, QSV_ERR_INVALID, "bad fusion plan request");
+  std::vector<int> width((size_t)std::max(ngates, 1));
+  for (int g = 0; g < ngates; ++g) width[(size_t)g] = __builtin_popcountll(qmask[g]);
+  std::vector<int> rem((size_t)ngates), next;
+  for (int g = 0; g < ngates; ++g) rem[(size_t)g] = g;
+  const int full_at = nqubits < 0 ? kmax : std::min(kmax, nqubits);
+  int nsteps = 0, nout = 0;
+  step_start_out[0] = 0;
+  Cand c, best;
+  while (!rem.empty()) {
+    const int first = rem[0];
+    if (width[(size_t)first] > kmax) {
+      order_out[nout++] = first;
+      step_start_out[++nsteps] = nout;
+      rem.erase(rem.begin());
+      continue;
+    }
+    bool have = false, undecided = false;
+    // With more than min_pending gates pending the round is decided on them anyway.
+    const bool forced = min_pending > 0 && (int)rem.size() > min_pending;
+    const int nc = std::min<int>(lookahead, (int)rem.size());
+    for (int s = 0; s < nc; ++s) {
+      if (width[(size_t)rem[(size_t)s]] > kmax) continue;
+      grow(rem, s, qmask, width.data(), weight, kmax, full_at, c);
+      if (nqubits >= 0 && strict && !forced && !c.final) {
+        undecided = true;
+        break;
+      }
+      if (!have || c.work > best.work) {
+        std::swap(best, c);
+        have = true;
+      }
+    }
+    if (undecided || (nqubits >= 0 && !forced && !best.final)) break;
+    std::vector<char> picked(rem.size(), 0);
+    for (int i : best.chosen) {
+      picked[(size_t)i] = 1;
+      order_out[nout++] = rem[(size_t)i];
+    }
+    step_start_out[++nsteps] = nout;
+    next.clear();
+    for (size_t i = 0; i < rem.size(); ++i)
+      if (!picked[i]) next.push_back(rem[i]);
+    rem.swap(next);
+  }
+  *nsteps_out = nsteps;
+  *nplanned_out = nout;
+  return QSV_OK;
+}
+
+namespace {
+
+// U <- G U for a gate on block bit positions bits[0..q) (bits[0] = MSB of the gate index).
+void embed(int k, double* U, int q, const int* bits, const double* G) {
+  const int dim = 1 << k, gd = 1 << q;
+  std::vector<int> off((size_t)gd);
+  int mask = 0;
+  for (int j = 0; j < gd; ++j) {
+    int o = 0;
+    for (int b = 0; b < q; ++b)
+      if ((j >> (q - 1 - b)) & 1) o |= 1 << bits[b];
+    off[(size_t)j] = o;
+  }
+  for (int b = 0; b < q; ++b) mask |= 1 << bits[b];
+  std::vector<double> v((size_t)2 * gd);
+  for (int r0 = 0; r0 < dim; ++r0) {
+    if (r0 & mask) continue;
+    for (int c = 0; c < dim; ++c) {
+      for (int j = 0; j < gd; ++j) {
+        const double* e = U + 2 * ((size_t)(r0 | off[(size_t)j]) * dim + c);
+        v[(size_t)2 * j] = e[0];
+        v[(size_t)2 * j + 1] = e[1];
+      }
+      for (int i = 0; i < gd; ++i) {
+        double re = 0.0, im = 0.0;
+        const double* gi = G + 2 * (size_t)i * gd;
+        for (int j = 0; j < gd; ++j) {
+          const double gr = gi[2 * j], gm = gi[2 * j + 1];
+          re += gr * v[(size_t)2 * j] - gm * v[(size_t)2 * j + 1];
+          im += gr * v[(size_t)2 * j + 1] + gm * v[(size_t)2 * j];
+        }
+        double* e = U + 2 * ((size_t)(r0 | off[(size_t)i]) * dim + c);
+        e[0] = re;
+        e[1] = im;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" int qsv_block_matrices(int nblocks, const int* block_k, const int* block_qubits, const int* block_ngates,
+                                  const int* gate_nq, const int* gate_qubits, const double* gate_mats,
+                                  double* out) {
+  if (nblocks < 0 || (nblocks > 0 && (!block_k || !block_qubits || !block_ngates || !gate_nq || !gate_qubits ||
+                                      !gate_mats || !out)))
+    return set_error(nullptr, QSV_ERR_INVALID, "bad block matrix request");
+  // Offsets of every block's qubits, gates, gate qubits, gate matrices and output.
+  std::vector<size_t> bq(nblocks + 1), bg(nblocks + 1), gq, gm, bo(nblocks + 1);
+  size_t ng = 0;
+  for (int b = 0; b < nblocks; ++b) {
+    if (block_k[b] < 1 || block_k[b] > 10 || block_ngates[b] < 0)
+      return set_error(nullptr, QSV_ERR_INVALID, "block %d: bad size", b);
+    bq[b + 1] = bq[b] + (size_t)block_k[b];
+    bg[b + 1] = bg[b] + (size_t)block_ngates[b];
+    bo[b + 1] = bo[b] + ((size_t)2 << (2 * block_k[b]));
+  }
+  ng = bg[nblocks];
+  gq.assign(ng + 1, 0);
+  gm.assign(ng + 1, 0);
+  for (size_t g = 0; g < ng; ++g) {
+    if (gate_nq[g] < 1 || gate_nq[g] > 10) return set_error(nullptr, QSV_ERR_INVALID, "gate %zu: bad width", g);
+    gq[g + 1] = gq[g] + (size_t)gate_nq[g];
+    gm[g + 1] = gm[g] + ((size_t)2 << (2 * gate_nq[g]));
+  }
+  // Check every gate qubit belongs to its block before any work.
+  for (int b = 0; b < nblocks; ++b)
+    for (size_t g = bg[b]; g < bg[b + 1]; ++g)
+      for (size_t i = gq[g]; i < gq[g + 1]; ++i) {
+        bool found = false;
+        for (size_t j = bq[b]; j < bq[b + 1]; ++j) found |= block_qubits[j] == gate_qubits[i];
+        if (!found) return set_error(nullptr, QSV_ERR_INVALID, "block %d: gate qubit %d outside the block", b,
+                                     gate_qubits[i]);
+      }
+  auto work = [&](int b) {
+    const int k = block_k[b], dim = 1 << k;
+    double* U = out + bo[(size_t)b];
+    std::memset(U, 0, sizeof(double) * ((size_t)2 << (2 * k)));
+    for (int i = 0; i < dim; ++i) U[2 * ((size_t)i * dim + i)] = 1.0;
+    int bits[10];
+    for (size_t g = bg[(size_t)b]; g < bg[(size_t)b + 1]; ++g) {
+      const int q = gate_nq[g];
+      for (int i = 0; i < q; ++i) {
+        const int qubit = gate_qubits[gq[g] + (size_t)i];
+        int pos = 0;
+        while (block_qubits[bq[(size_t)b] + (size_t)pos] != qubit) ++pos;
+        bits[i] = k - 1 - pos;  // block qubit 0 is the MSB of the row index
+      }
+      embed(k, U, q, bits, gate_mats + gm[g]);
+    }
+  };
+  const int nthreads = std::max(1, std::min<int>(nblocks, (int)std::min(16u, std::thread::hardware_concurrency())));
+  if (nthreads <= 1) {
+    for (int b = 0; b < nblocks; ++b) work(b);
+  } else {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; ++t)
+      pool.emplace_back([&, t]() {
+        for (int b = t; b < nblocks; b += nthreads) work(b);
+      });
+    for (auto& th : pool) th.join();
+  }
+  return QSV_OK;
+}

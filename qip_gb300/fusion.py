@@ -18,6 +18,7 @@ a single gate keeps that gate's own structured kernel.
 """
 from __future__ import annotations
 
+import ctypes
 from dataclasses import dataclass
 from typing import List, Sequence, Tuple, Union
 
@@ -72,8 +73,81 @@ LOOKAHEAD = 16
 
 
 def plan(gates: Sequence[GateOp], kmax: int = 6, lookahead: int = LOOKAHEAD) -> List[Step]:
-    """Group ``gates`` (program order) into fused blocks and standalone gates."""
-    steps, rest = plan_prefix(gates, kmax, nqubits=None, lookahead=lookahead)
+    """Group ``gates`` (program order) into fused blocks and standalone gates (native
+    planner and block matrices, ``qsv_fusion_plan`` / ``qsv_block_matrices``)."""
+    steps, rest = plan_prefix(gates, kmax, None, lookahead)
+    assert not rest
+    return steps
+
+
+def plan_prefix(gates: Sequence[GateOp], kmax: int = 6, nqubits=None, lookahead: int = LOOKAHEAD,
+                strict: bool = True, min_pending: int = 0) -> Tuple[List[Step], List[GateOp]]:
+    """``plan_prefix_py`` in native code: same steps, same matrices (to rounding)."""
+    from . import _native as nat
+
+    lib = nat.load()
+    ng = len(gates)
+    if ng == 0:
+        return [], []
+    qm = numpy.array([g.qmask for g in gates], dtype=numpy.uint64)
+    w = numpy.array([g.amp_update_weight() for g in gates], dtype=numpy.float64)
+    order = numpy.empty(ng, dtype=numpy.int32)
+    starts = numpy.empty(ng + 1, dtype=numpy.int32)
+    nsteps, nplanned = ctypes.c_int(), ctypes.c_int()
+    nat.check(lib.qsv_fusion_plan(ng, qm.ctypes.data_as(ctypes.c_void_p), nat.dp(w), int(kmax), int(lookahead),
+                                  -1 if nqubits is None else int(nqubits), int(bool(strict)), int(min_pending),
+                                  nat.ip(order),
+                                  nat.ip(starts), ctypes.byref(nsteps), ctypes.byref(nplanned)), None, "fusion_plan")
+    groups = [[gates[i] for i in order[starts[k]:starts[k + 1]]] for k in range(nsteps.value)]
+    planned = set(order[:nplanned.value].tolist())
+    rest = [g for i, g in enumerate(gates) if i not in planned]
+    return emit_native(groups), rest
+
+
+def emit_native(groups: Sequence[Sequence[GateOp]]) -> List[Step]:
+    """Steps for planned groups: one gate stays itself, several become a Block whose
+    matrix comes from one ``qsv_block_matrices`` call for all of them."""
+    from . import _native as nat
+
+    multi = [grp for grp in groups if len(grp) > 1]
+    mats = {}
+    if multi:
+        bk, bq, bn, gnq, gq, gm, qsets = [], [], [], [], [], [], []
+        for grp in multi:
+            qs = tuple(sorted(set().union(*[g.qubits for g in grp])))
+            qsets.append(qs)
+            bk.append(len(qs))
+            bq.extend(qs)
+            bn.append(len(grp))
+            for g in grp:
+                order, m = g.matrix()
+                gnq.append(len(order))
+                gq.extend(int(x) for x in order)
+                gm.append(numpy.ascontiguousarray(m, dtype=numpy.complex128).reshape(-1))
+        gmat = numpy.ascontiguousarray(numpy.concatenate(gm)).view(numpy.float64)
+        out = numpy.empty(sum(4 ** k for k in bk), dtype=numpy.complex128)
+        nat.check(nat.load().qsv_block_matrices(len(multi), nat.int_array(bk).ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                                nat.ip(nat.int_array(bq)), nat.ip(nat.int_array(bn)),
+                                                nat.ip(nat.int_array(gnq)), nat.ip(nat.int_array(gq)), nat.dp(gmat),
+                                                nat.dp(out.view(numpy.float64))), None, "block_matrices")
+        off = 0
+        for grp, qs in zip(multi, qsets):
+            d = 1 << len(qs)
+            mats[id(grp)] = (qs, out[off:off + d * d].reshape(d, d))
+            off += d * d
+    steps: List[Step] = []
+    for grp in groups:
+        if len(grp) == 1:
+            steps.append(grp[0])
+        else:
+            qs, U = mats[id(grp)]
+            steps.append(Block(qs, U, len(grp), sum(g.amp_update_weight() for g in grp)))
+    return steps
+
+
+def plan_py(gates: Sequence[GateOp], kmax: int = 6, lookahead: int = LOOKAHEAD) -> List[Step]:
+    """Reference (pure Python) implementation of ``plan``."""
+    steps, rest = plan_prefix_py(gates, kmax, None, lookahead)
     assert not rest
     return steps
 
@@ -105,36 +179,51 @@ def _grow(remaining: Sequence[GateOp], start: int, kmax: int, full_at: int):
     return chosen, S, blocked, nS >= full_at and (S & ~blocked) == 0
 
 
-def plan_prefix(gates: Sequence[GateOp], kmax: int = 6, nqubits=None,
-                lookahead: int = LOOKAHEAD) -> Tuple[List[Step], List[GateOp]]:
-    """Plan of ``gates``.  With ``nqubits`` given, stop at the first round whose choice
-    later gates could still change and return (steps so far, gates not yet planned): a
+def _round(remaining: List[GateOp], kmax: int, lookahead: int, nqubits, strict: bool, min_pending: int = 0):
+    """One planning round: (step, remaining after it), or (None, remaining) when
+    ``nqubits`` is given and the round cannot be decided on these gates yet (a round is
+    decided anyway while more than ``min_pending`` > 0 gates are pending)."""
+    if min_pending > 0 and len(remaining) > min_pending:
+        nqubits = None
+    first = remaining[0]
+    if first.width > kmax:
+        return first, remaining[1:]
+    best = None
+    full_at = kmax if nqubits is None else min(kmax, nqubits)
+    for start in range(min(lookahead, len(remaining))):
+        if remaining[start].width > kmax:
+            continue
+        chosen, S, blocked, final = _grow(remaining, start, kmax, full_at)
+        if nqubits is not None and strict and not final:
+            return None, remaining
+        work = sum(remaining[i].amp_update_weight() for i in chosen)
+        if best is None or work > best[0]:
+            best = (work, chosen, final)
+    if nqubits is not None and not best[2]:
+        return None, remaining
+    picked = set(best[1])
+    return _emit([remaining[i] for i in best[1]]), [g for i, g in enumerate(remaining) if i not in picked]
+
+
+def plan_prefix_py(gates: Sequence[GateOp], kmax: int = 6, nqubits=None, lookahead: int = LOOKAHEAD,
+                   strict: bool = True, min_pending: int = 0) -> Tuple[List[Step], List[GateOp]]:
+    """Reference (pure Python) plan of ``gates``.  With ``nqubits`` given, stop at the first round that later
+    gates could still change and return (steps so far, gates not yet planned): a
     candidate block is final once it is full (kmax qubits, or every qubit of the
-    register) and each of its qubits is blocked by a gate left out of it, and a round is
-    decided once all its candidates are final (the candidates and their blocks then no
-    longer depend on later gates).  The steps returned are exactly the first steps of
-    ``plan`` over any extension of ``gates``, so a caller can launch them while gates
-    keep arriving.  With ``nqubits=None`` plans everything."""
+    register) and each of its qubits is blocked by a gate left out of it.  ``strict``:
+    a round is decided once all its candidates are final (the candidates and their
+    blocks then no longer depend on later gates), so the steps returned are exactly the
+    first steps of ``plan`` over any extension of ``gates``.  Otherwise a round is
+    decided once its best candidate on these gates is final — the block is just as valid
+    (it only holds gates that commute with everything it jumps over) but a candidate
+    that later gates would have grown may lose.  ``min_pending`` > 0: while more gates
+    than that are pending a round is decided on them regardless.  With ``nqubits=None``
+    plans everything."""
     remaining = list(gates)
     steps: List[Step] = []
     while remaining:
-        first = remaining[0]
-        if first.width > kmax:
-            steps.append(first)
-            remaining = remaining[1:]
-            continue
-        best = None
-        full_at = kmax if nqubits is None else min(kmax, nqubits)
-        for start in range(min(lookahead, len(remaining))):
-            if remaining[start].width > kmax:
-                continue
-            chosen, S, blocked, final = _grow(remaining, start, kmax, full_at)
-            if nqubits is not None and not final:
-                return steps, remaining
-            work = sum(remaining[i].amp_update_weight() for i in chosen)
-            if best is None or work > best[0]:
-                best = (work, chosen)
-        picked = set(best[1])
-        steps.append(_emit([remaining[i] for i in best[1]]))
-        remaining = [g for i, g in enumerate(remaining) if i not in picked]
+        step, remaining = _round(remaining, kmax, lookahead, nqubits, strict, min_pending)
+        if step is None:
+            return steps, remaining
+        steps.append(step)
     return steps, []

@@ -240,3 +240,33 @@ def test_autotuner_cache_round_trip(tmp_path):
     t2._unpinned = []
     w2, steps2, report2 = t2.choose_width(None, n, ops)
     assert w2 == w and report2 == report and len(steps2) == len(steps)
+
+
+def _same_steps(a, b):
+    assert len(a) == len(b)
+    for x, y in zip(a, b):
+        assert type(x) is type(y)
+        if isinstance(x, fusion.Block):
+            assert x.qubits == y.qubits and x.ngates == y.ngates
+            numpy.testing.assert_allclose(x.matrix, y.matrix, atol=1e-12)
+        else:
+            assert x is y
+
+
+@pytest.mark.parametrize("kmax", [3, 4, 6])
+def test_native_planner_matches_python_reference(kmax):
+    """qsv_fusion_plan / qsv_block_matrices (the library, loadable without a GPU) give
+    the Python planner's steps and matrices: whole lists and both prefix modes."""
+    rng = numpy.random.default_rng(kmax)
+    n = 12
+    lists = [circuits.brickwork(n, 8, seed=7) + circuits.grover_gates(n, 1, seed=3)[0],
+             circuits.random_circuit(rng, n, 200), circuits.qft_gates(n)]
+    for gl in lists:
+        ops = [op for g in gl for op in gates.decompose(g)]
+        _same_steps(fusion.plan(ops, kmax=kmax), fusion.plan_py(ops, kmax=kmax))
+        for cut in (40, 120):
+            for strict, keep in ((True, 0), (False, 0), (False, 30)):
+                s1, r1 = fusion.plan_prefix(ops[:cut], kmax=kmax, nqubits=n, strict=strict, min_pending=keep)
+                s2, r2 = fusion.plan_prefix_py(ops[:cut], kmax=kmax, nqubits=n, strict=strict, min_pending=keep)
+                _same_steps(s1, s2)
+                assert all(x is y for x, y in zip(r1, r2)) and len(r1) == len(r2)
