@@ -122,19 +122,20 @@ int qsv_plan_destroy(qsv_plan* p);
  * masks (bit q <-> qubit q) and amp-update weights.  Each round grows up to lookahead
  * candidate blocks (candidate s leaves the first s pending gates out, then takes every
  * later gate whose qubits fit in kmax and are not blocked by a gate left out before it;
- * a left-out gate blocks its qubits) and keeps the one with the most weight; a gate
- * wider than kmax at the front is its own step.  nqubits < 0: plan every gate.
+ * a left-out gate blocks its qubits) and keeps the one with the best score: its weight
+ * plus (lookahead2 > 0) the most weight one of the next round's first lookahead2
+ * candidates would take after it.  A gate wider than kmax at the front is its own step.  nqubits < 0: plan every gate.
  * nqubits >= 0 (prefix mode): stop at the first round later gates could change (a
  * candidate is final once it holds min(kmax, nqubits) qubits, all blocked; strict: all
- * candidates must be final, else the best one), except that a round is decided on the
+ * candidates of both levels must be final, else the best one), except that a round is decided on the
  * pending gates anyway while more than min_pending (> 0) are pending: the block is just
  * as valid, it may only be smaller than later gates would have allowed.  Output: the
  * planned gates in step
  * order (order_out, ngates entries of room), step s = order_out[step_start_out[s] ..
  * step_start_out[s+1]) (ngates + 1 entries of room), nsteps, number of planned gates. */
 int qsv_fusion_plan(int ngates, const uint64_t* qmask, const double* weight, int kmax,
-                    int lookahead, int nqubits, int strict, int min_pending, int* order_out,
-                    int* step_start_out, int* nsteps_out, int* nplanned_out);
+                    int lookahead, int lookahead2, int nqubits, int strict, int min_pending,
+                    int* order_out, int* step_start_out, int* nsteps_out, int* nplanned_out);
 /* Dense matrices of fused blocks (host, threads across blocks; no reference
  * counterpart).  Block b has block_k[b] qubits (block_qubits, ascending: the first is
  * the MSB of the block index) and block_ngates[b] gates; gate g acts on gate_nq[g]

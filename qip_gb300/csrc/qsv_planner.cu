@@ -4,10 +4,12 @@
 // grows up to `lookahead` candidate blocks — candidate s leaves the first s pending
 // gates out and then scans in program order; a gate joins when its qubits fit (at most
 // kmax) and none of them is blocked by a gate left out earlier; a left-out gate blocks
-// its qubits — and keeps the candidate with the most work (sum of amp-update
-// weights, first on ties).  A candidate is final once it is full and all its qubits
+// its qubits — and keeps the candidate with the best score (first on ties): its work
+// (sum of amp-update weights) plus, with lookahead2 > 0, the most work one of the
+// next round's first lookahead2 candidates would take after it.  A candidate is final once it is full and all its qubits
 // are blocked; prefix mode (nqubits >= 0) stops at the first round that later gates
-// could still change (strict: some candidate is not final; relaxed: the best is not),
+// could still change (strict: some candidate, of either level, is not final; relaxed:
+// the best is not),
 // unless more than min_pending gates are pending (then the round is decided anyway).
 //
 // qsv_block_matrices multiplies each block's gates into its 2^k x 2^k matrix, blocks
@@ -71,8 +73,8 @@ void grow(const std::vector<int>& rem, int start, const uint64_t* qmask, const i
 }  // namespace
 
 extern "C" int qsv_fusion_plan(int ngates, const uint64_t* qmask, const double* weight, int kmax, int lookahead,
-                               int nqubits, int strict, int min_pending, int* order_out, int* step_start_out,
-                               int* nsteps_out, int* nplanned_out) {
+                               int lookahead2, int nqubits, int strict, int min_pending, int* order_out,
+                               int* step_start_out, int* nsteps_out, int* nplanned_out) {
   if (ngates < 0 || (ngates > 0 && (!qmask || !weight || !order_out || !step_start_out)) || !nsteps_out ||
       !nplanned_out || kmax < 1 || kmax > 62 || lookahead < 1)
     return set_error(nullptr, QSV_ERR_INVALID, "bad fusion plan request");
@@ -83,7 +85,8 @@ extern "C" int qsv_fusion_plan(int ngates, const uint64_t* qmask, const double* 
   const int full_at = nqubits < 0 ? kmax : std::min(kmax, nqubits);
   int nsteps = 0, nout = 0;
   step_start_out[0] = 0;
-  Cand c, best;
+  Cand c, best, c2;
+  std::vector<int> rest2;
   while (!rem.empty()) {
     const int first = rem[0];
     if (width[(size_t)first] > kmax) {
@@ -93,18 +96,42 @@ extern "C" int qsv_fusion_plan(int ngates, const uint64_t* qmask, const double* 
       continue;
     }
     bool have = false, undecided = false;
+    double best_score = 0.0;
     // With more than min_pending gates pending the round is decided on them anyway.
     const bool forced = min_pending > 0 && (int)rem.size() > min_pending;
     const int nc = std::min<int>(lookahead, (int)rem.size());
-    for (int s = 0; s < nc; ++s) {
+    for (int s = 0; s < nc && !undecided; ++s) {
       if (width[(size_t)rem[(size_t)s]] > kmax) continue;
       grow(rem, s, qmask, width.data(), weight, kmax, full_at, c);
       if (nqubits >= 0 && strict && !forced && !c.final) {
         undecided = true;
         break;
       }
-      if (!have || c.work > best.work) {
+      // Score: the candidate's work plus the most work a next block could take after it.
+      double score = c.work;
+      if (lookahead2 > 0) {
+        std::vector<char> in(rem.size(), 0);
+        for (int i : c.chosen) in[(size_t)i] = 1;
+        rest2.clear();
+        for (size_t i = 0; i < rem.size(); ++i)
+          if (!in[i]) rest2.push_back(rem[i]);
+        double w2 = 0.0;
+        const int nc2 = std::min<int>(lookahead2, (int)rest2.size());
+        for (int s2 = 0; s2 < nc2; ++s2) {
+          if (width[(size_t)rest2[(size_t)s2]] > kmax) continue;
+          grow(rest2, s2, qmask, width.data(), weight, kmax, full_at, c2);
+          if (nqubits >= 0 && strict && !forced && !c2.final) {
+            undecided = true;
+            break;
+          }
+          w2 = std::max(w2, c2.work);
+        }
+        score += w2;
+      }
+      if (undecided) break;
+      if (!have || score > best_score) {
         std::swap(best, c);
+        best_score = score;
         have = true;
       }
     }

@@ -1,15 +1,16 @@
 """Gate fusion: merge runs of gates into dense 2^k x 2^k blocks (k <= 6).
 
-Each round grows candidate blocks and keeps the one that absorbs the most work.  A
-candidate starts at one of the first ``lookahead`` pending gates: the gates before the
+Each round grows candidate blocks and keeps the best: the one that, together with the
+largest block that could follow it, absorbs the most work.  A candidate starts at one
+of the first ``lookahead`` pending gates: the gates before the
 start are left out, then the scan continues in program order and a gate joins when its
 qubits fit in the block (at most ``kmax`` qubits in total) and none of its qubits is
 "blocked" — touched by an earlier gate that was left out.  A gate left out blocks its
 qubits for the rest of the scan, so every gate moved into the block commutes with
 every gate it jumps over (they act on disjoint qubits).  Starting past the first gate
 lets a round take the block that fits the circuit's light cone instead of whatever the
-front gate implies (brickwork n=28, depth 40: 75 steps instead of 120 with a start at
-the front only).  Gates wider than ``kmax`` are never fused; they run on the per-gate
+front gate implies (brickwork n=28, depth 40: 69 steps instead of 120 with a start at
+the front only and no second-level score).  Gates wider than ``kmax`` are never fused; they run on the per-gate
 kernels when they reach the front of the queue.
 
 A block of 4..6 qubits runs on the tensor cores (one HBM pass for all its gates); a
@@ -69,19 +70,22 @@ def _emit(chosen: List[GateOp]) -> Step:
     return Block(qs, U, len(chosen), sum(g.amp_update_weight() for g in chosen))
 
 
-LOOKAHEAD = 16
+LOOKAHEAD = 16   # first-level candidates per round
+LOOKAHEAD2 = 8   # next-round candidates scored after each of them
 
 
-def plan(gates: Sequence[GateOp], kmax: int = 6, lookahead: int = LOOKAHEAD) -> List[Step]:
+def plan(gates: Sequence[GateOp], kmax: int = 6, lookahead: int = LOOKAHEAD,
+         lookahead2: int = LOOKAHEAD2) -> List[Step]:
     """Group ``gates`` (program order) into fused blocks and standalone gates (native
     planner and block matrices, ``qsv_fusion_plan`` / ``qsv_block_matrices``)."""
-    steps, rest = plan_prefix(gates, kmax, None, lookahead)
+    steps, rest = plan_prefix(gates, kmax, None, lookahead, lookahead2=lookahead2)
     assert not rest
     return steps
 
 
 def plan_prefix(gates: Sequence[GateOp], kmax: int = 6, nqubits=None, lookahead: int = LOOKAHEAD,
-                strict: bool = True, min_pending: int = 0) -> Tuple[List[Step], List[GateOp]]:
+                strict: bool = True, min_pending: int = 0,
+                lookahead2: int = LOOKAHEAD2) -> Tuple[List[Step], List[GateOp]]:
     """``plan_prefix_py`` in native code: same steps, same matrices (to rounding)."""
     from . import _native as nat
 
@@ -95,6 +99,7 @@ def plan_prefix(gates: Sequence[GateOp], kmax: int = 6, nqubits=None, lookahead:
     starts = numpy.empty(ng + 1, dtype=numpy.int32)
     nsteps, nplanned = ctypes.c_int(), ctypes.c_int()
     nat.check(lib.qsv_fusion_plan(ng, qm.ctypes.data_as(ctypes.c_void_p), nat.dp(w), int(kmax), int(lookahead),
+                                  int(lookahead2),
                                   -1 if nqubits is None else int(nqubits), int(bool(strict)), int(min_pending),
                                   nat.ip(order),
                                   nat.ip(starts), ctypes.byref(nsteps), ctypes.byref(nplanned)), None, "fusion_plan")
@@ -145,9 +150,10 @@ def emit_native(groups: Sequence[Sequence[GateOp]]) -> List[Step]:
     return steps
 
 
-def plan_py(gates: Sequence[GateOp], kmax: int = 6, lookahead: int = LOOKAHEAD) -> List[Step]:
+def plan_py(gates: Sequence[GateOp], kmax: int = 6, lookahead: int = LOOKAHEAD,
+            lookahead2: int = LOOKAHEAD2) -> List[Step]:
     """Reference (pure Python) implementation of ``plan``."""
-    steps, rest = plan_prefix_py(gates, kmax, None, lookahead)
+    steps, rest = plan_prefix_py(gates, kmax, None, lookahead, lookahead2=lookahead2)
     assert not rest
     return steps
 
@@ -179,12 +185,15 @@ def _grow(remaining: Sequence[GateOp], start: int, kmax: int, full_at: int):
     return chosen, S, blocked, nS >= full_at and (S & ~blocked) == 0
 
 
-def _round(remaining: List[GateOp], kmax: int, lookahead: int, nqubits, strict: bool, min_pending: int = 0):
+def _round(remaining: List[GateOp], kmax: int, lookahead: int, nqubits, strict: bool, min_pending: int = 0,
+           lookahead2: int = LOOKAHEAD2):
     """One planning round: (step, remaining after it), or (None, remaining) when
     ``nqubits`` is given and the round cannot be decided on these gates yet (a round is
-    decided anyway while more than ``min_pending`` > 0 gates are pending)."""
-    if min_pending > 0 and len(remaining) > min_pending:
-        nqubits = None
+    decided anyway while more than ``min_pending`` > 0 gates are pending).  A candidate
+    scores its work plus the most work one of the next round's first ``lookahead2``
+    candidates would take after it."""
+    forced = min_pending > 0 and len(remaining) > min_pending
+    prefix = nqubits is not None and not forced
     first = remaining[0]
     if first.width > kmax:
         return first, remaining[1:]
@@ -194,19 +203,33 @@ def _round(remaining: List[GateOp], kmax: int, lookahead: int, nqubits, strict: 
         if remaining[start].width > kmax:
             continue
         chosen, S, blocked, final = _grow(remaining, start, kmax, full_at)
-        if nqubits is not None and strict and not final:
+        if prefix and strict and not final:
             return None, remaining
         work = sum(remaining[i].amp_update_weight() for i in chosen)
-        if best is None or work > best[0]:
-            best = (work, chosen, final)
-    if nqubits is not None and not best[2]:
+        score = work
+        if lookahead2 > 0:
+            picked = set(chosen)
+            rest = [g for i, g in enumerate(remaining) if i not in picked]
+            w2 = 0.0
+            for s2 in range(min(lookahead2, len(rest))):
+                if rest[s2].width > kmax:
+                    continue
+                c2, _, _, f2 = _grow(rest, s2, kmax, full_at)
+                if prefix and strict and not f2:
+                    return None, remaining
+                w2 = max(w2, sum(rest[i].amp_update_weight() for i in c2))
+            score += w2
+        if best is None or score > best[0]:
+            best = (score, chosen, final)
+    if prefix and not best[2]:
         return None, remaining
     picked = set(best[1])
     return _emit([remaining[i] for i in best[1]]), [g for i, g in enumerate(remaining) if i not in picked]
 
 
 def plan_prefix_py(gates: Sequence[GateOp], kmax: int = 6, nqubits=None, lookahead: int = LOOKAHEAD,
-                   strict: bool = True, min_pending: int = 0) -> Tuple[List[Step], List[GateOp]]:
+                   strict: bool = True, min_pending: int = 0,
+                   lookahead2: int = LOOKAHEAD2) -> Tuple[List[Step], List[GateOp]]:
     """Reference (pure Python) plan of ``gates``.  With ``nqubits`` given, stop at the first round that later
     gates could still change and return (steps so far, gates not yet planned): a
     candidate block is final once it is full (kmax qubits, or every qubit of the
@@ -222,7 +245,7 @@ def plan_prefix_py(gates: Sequence[GateOp], kmax: int = 6, nqubits=None, lookahe
     remaining = list(gates)
     steps: List[Step] = []
     while remaining:
-        step, remaining = _round(remaining, kmax, lookahead, nqubits, strict, min_pending)
+        step, remaining = _round(remaining, kmax, lookahead, nqubits, strict, min_pending, lookahead2)
         if step is None:
             return steps, remaining
         steps.append(step)
