@@ -45,6 +45,8 @@ enum qsv_status {
  * (qip/backend.py:68-71, 88, 103).  One device buffer; updates are in place, so there
  * is no arena.  The state starts as |0...0>. */
 int qsv_create(int n, int dtype, qsv_state** out);
+/* Fault injection for tests: with QSV_INJECT_ALLOC_FAILURE set (not "0") qsv_create
+ * fails with QSV_ERR_OOM before any device call. */
 int qsv_destroy(qsv_state* s);
 /* Use an external CUDA stream (cudaStream_t passed as void*; NULL = the handle's own). */
 int qsv_set_stream(qsv_state* s, void* stream);
@@ -75,6 +77,10 @@ int qsv_add_range(qsv_state* s, const void* host, uint64_t start, uint64_t count
 /* Copy amplitudes [start, start+count) to host memory of the handle's dtype.  Blocks.
  * Replaces CythonBackend.get_state / get_relative_range (qip/backend.py:106-107,168-169). */
 int qsv_read_range(qsv_state* s, void* host, uint64_t start, uint64_t count);
+/* NVTX ranges (a profiler shows them on its timeline; no-ops otherwise).  No reference
+ * counterpart: the graph executor opens one per node when QSV_NVTX=1. */
+int qsv_trace_push(const char* name);
+int qsv_trace_pop(void);
 /* Page-locked host buffers (cudaHostAlloc / cudaFreeHost).  A read into one is a
  * single DMA with no staging copy and no page faults.  No reference counterpart: the
  * reference's state already lives in host memory. */

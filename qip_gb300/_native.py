@@ -49,6 +49,8 @@ SIGNATURES = {
     "qsv_apply_monomial": (ctypes.c_int, [_handle, ctypes.c_int, _c_int_p, ctypes.c_int, _c_int_p, _c_int_p,
                                           _c_double_p]),
     "qsv_apply_swap": (ctypes.c_int, [_handle, ctypes.c_int, _c_int_p, _c_int_p, ctypes.c_int, _c_int_p]),
+    "qsv_trace_push": (ctypes.c_int, [ctypes.c_char_p]),
+    "qsv_trace_pop": (ctypes.c_int, []),
     "qsv_host_alloc": (ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]),
     "qsv_host_free": (ctypes.c_int, [ctypes.c_void_p]),
     "qsv_batch_segment_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,

@@ -240,6 +240,10 @@ class GpuBackend(StateType):
             for q in op.qubits:
                 if not 0 <= q < self.n:
                     raise ValueError("qubit index {} out of range for n={}".format(q, self.n))
+            # Checked on the host before anything is queued or launched: a NaN or an
+            # infinity would silently spread over the whole state.
+            if op.mat is not None and not numpy.all(numpy.isfinite(op.mat)):
+                raise ValueError("matrix on qubits {} has non-finite entries".format(sorted(op.qubits)))
         if self.fusion:
             self._pending.extend(ops)
             if len(self._pending) >= self.FLUSH_LIMIT:

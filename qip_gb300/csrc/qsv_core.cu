@@ -7,8 +7,11 @@
 // index bit (n-1-q) is qubit q (qubit 0 = most significant bit), the reference's
 // convention (qip/ext/kronprod.pyx:168, 187-189).  Updates are in place.
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <mutex>
 #include <thread>
 #include <new>
@@ -1129,6 +1132,11 @@ int qsv_create(int n, int dtype, qsv_state** out) {
   *out = nullptr;
   if (n < 1 || n > QSV_MAXN) return set_error(nullptr, QSV_ERR_INVALID, "n=%d outside [1, %d]", n, QSV_MAXN);
   if (dtype != QSV_C64 && dtype != QSV_C128) return set_error(nullptr, QSV_ERR_INVALID, "unknown dtype %d", dtype);
+  // Host-side fault injection: a failed state allocation, before any device call.
+  if (const char* f = getenv("QSV_INJECT_ALLOC_FAILURE"))
+    if (f[0] && f[0] != '0')
+      return set_error(nullptr, QSV_ERR_OOM, "state allocation of %zu bytes failed (injected)",
+                       ((size_t)1 << n) * (dtype == QSV_C64 ? 8 : 16));
   auto* s = new (std::nothrow) qsv_state();
   if (!s) return set_error(nullptr, QSV_ERR_OOM, "host allocation failed");
   s->n = n;
@@ -1281,6 +1289,16 @@ bool is_pinned(const void* p) {
   return at.type == cudaMemoryTypeHost;
 }
 }  // namespace
+
+int qsv_trace_push(const char* name) {
+  nvtxRangePushA(name ? name : "");
+  return QSV_OK;
+}
+
+int qsv_trace_pop(void) {
+  nvtxRangePop();
+  return QSV_OK;
+}
 
 int qsv_host_alloc(uint64_t bytes, void** out) {
   if (!out || bytes == 0) return set_error(nullptr, QSV_ERR_INVALID, "bad host allocation request");

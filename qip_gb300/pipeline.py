@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import heapq
 import itertools
+import os
 from typing import Any, Callable, Dict, List, Mapping, Sequence, Set, Tuple, Type, Union
 
 import numpy
@@ -187,6 +188,17 @@ def run_graph(frontier: Sequence[PipelineObject], graphnodes, graphacc: GraphAcc
                     qbitindex[nxt] = nxt.select_index(flatten(qbitindex[j] for j in nxt.inputs))
 
 
+# QSV_NVTX=1: one NVTX range per graph node (named after its operator class), visible on
+# a profiler's timeline around that node's kernels.
+TRACE = os.environ.get("QSV_NVTX", "0") not in ("", "0")
+
+
+def _trace_lib():
+    from . import _native as nat
+
+    return nat.load()
+
+
 class NodeFeeder(GraphAccumulator):
     """Feeds nodes to the state and records classical results (``qip/pipeline.py:225-240``)."""
 
@@ -196,7 +208,13 @@ class NodeFeeder(GraphAccumulator):
         self.classic_map = {}
 
     def feed(self, qbitindex, node):
-        n_bits, bits = node.feed(self.state, qbitindex, self.n)
+        if TRACE:
+            _trace_lib().qsv_trace_push(type(node).__name__.encode())
+        try:
+            n_bits, bits = node.feed(self.state, qbitindex, self.n)
+        finally:
+            if TRACE:
+                _trace_lib().qsv_trace_pop()
         if n_bits > 0 or bits is not None:
             self.classic_map[node] = bits
             self.n -= n_bits

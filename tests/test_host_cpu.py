@@ -270,3 +270,20 @@ def test_native_planner_matches_python_reference(kmax):
                 s2, r2 = fusion.plan_prefix_py(ops[:cut], kmax=kmax, nqubits=n, strict=strict, min_pending=keep)
                 _same_steps(s1, s2)
                 assert all(x is y for x, y in zip(r1, r2)) and len(r1) == len(r2)
+
+
+def test_injected_allocation_failure_raises_memory_error(monkeypatch):
+    """Host-side fault injection: the state allocation fails before any device call (so
+    this runs without a GPU) and surfaces as the reference's MemoryError."""
+    from qip_gb300 import GpuBackend
+
+    monkeypatch.setenv("QSV_INJECT_ALLOC_FAILURE", "1")
+    with pytest.raises(MemoryError, match="injected"):
+        GpuBackend.make_state(12, [], [], statetype=numpy.complex64)
+
+
+def test_trace_ranges_are_callable_without_a_profiler():
+    from qip_gb300 import _native as nat
+
+    lib = nat.load()
+    assert lib.qsv_trace_push(b"node") == 0 and lib.qsv_trace_pop() == 0
