@@ -230,7 +230,7 @@ def run_ours(args):
     tuner = default_tuner()
     if args.kmax:
         kmax, width_report = args.kmax, {}
-        steps = fusion.plan(ops, kmax=kmax)
+        steps = fusion.widen_low_blocks(fusion.plan(ops, kmax=kmax), n)
         tuner.ensure_plan(st.handle, n, steps)
     else:
         # Measured fusion width and block access modes (scratch-state timings).
@@ -569,7 +569,7 @@ def run_hbm(args):
         per_kind = {}
         e0, e1 = _events()
         if fusion_on:
-            steps = fusion.plan(ops, kmax=6)
+            steps = fusion.widen_low_blocks(fusion.plan(ops, kmax=6), n)
             default_tuner().ensure_plan(st.handle, n, steps)
         else:
             steps = ops

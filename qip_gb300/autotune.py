@@ -33,7 +33,7 @@ from typing import Dict, Iterable, List, Optional, Sequence, Tuple
 import numpy
 
 from . import _native as nat
-from .fusion import Block, plan
+from .fusion import Block, plan, widen_low_blocks
 from .gates import GateOp
 
 SCRATCH_QUBITS = 26  # the library tunes on min(n, 26) qubits
@@ -71,8 +71,10 @@ class Autotuner:
     def _load(self, path: str) -> None:
         with open(path) as f:
             d = json.load(f)
-        for nt, k, low, m0, m1, m2, best in d.get("classes", []):
-            self._ms[(int(nt), int(k), int(low))] = ([float(m0), float(m1), float(m2)], int(best))
+        for row in d.get("classes", []):
+            nt, k, low, times, best = row[0], row[1], row[2], row[3:-1], row[-1]
+            times = [float(x) for x in times] + [-1.0] * (len(MODES) - len(times))
+            self._ms[(int(nt), int(k), int(low))] = (times, int(best))
             self._unpinned.append((int(k), int(low), int(best)))
         self._width = {int(n): int(w) for n, w in d.get("widths", {}).items()}
         self._reports = {int(n): {int(w): float(ms) for w, ms in r.items()} for n, r in d.get("reports", {}).items()}
@@ -110,13 +112,14 @@ class Autotuner:
             lib = nat.load()
             ks = nat.int_array([k for k, _ in todo])
             lows = nat.int_array([low for _, low in todo])
-            ms = numpy.zeros(3 * len(todo), dtype=numpy.float64)
+            nm = len(MODES)
+            ms = numpy.zeros(nm * len(todo), dtype=numpy.float64)
             best = numpy.zeros(len(todo), dtype=numpy.int32)
             nat.check(lib.qsv_tune_blocks(handle, len(todo), nat.ip(ks), nat.ip(lows), self.reps, nat.dp(ms),
                                           best.ctypes.data_as(ctypes.POINTER(ctypes.c_int))),
                       handle, "tune_blocks")
             for i, c in enumerate(todo):
-                self._ms[(nt,) + tuple(c)] = ([float(x) for x in ms[3 * i:3 * i + 3]], int(best[i]))
+                self._ms[(nt,) + tuple(c)] = ([float(x) for x in ms[nm * i:nm * i + nm]], int(best[i]))
             self._save()
 
     def measured(self, n: int, k: int, low: int) -> Optional[Tuple[List[float], int]]:
@@ -161,13 +164,13 @@ class Autotuner:
         if self._width.get(n) in widths and n in self._reports:
             # Decided before (this process or a loaded cache): reuse it.
             w = self._width[n]
-            steps = plan(ops, kmax=w)
+            steps = widen_low_blocks(plan(ops, kmax=w), n)
             self.ensure_plan(handle, n, steps)
             return w, steps, dict(self._reports[n])
         best = None
         report = {}
         for w in widths:
-            steps = plan(ops, kmax=w)
+            steps = widen_low_blocks(plan(ops, kmax=w), n)
             ms = self.predict_ms(handle, n, steps)
             report[w] = ms
             if best is None or ms < best[0]:

@@ -150,6 +150,31 @@ def emit_native(groups: Sequence[Sequence[GateOp]]) -> List[Step]:
     return steps
 
 
+LOW_BITS = 5     # address bits 0..4: the lanes of one 32-amplitude warp access
+KERNEL_MAX = 6   # widest tensor-core block
+
+
+def widen_low_blocks(steps: Sequence[Step], n: int) -> List[Step]:
+    """Place a plan on an n-qubit state.  A tensor-core block of k < 6 qubits whose
+    qubits all sit on address bits 0..4 (qubit q <-> bit n-1-q) can only move through
+    shared memory (staged access, two extra passes over each tile); one more qubit on
+    the highest free address bit, with the identity there (U -> I (x) U), lets the
+    shuffle access take it (n=28: 4 qubits on bits 1..4 staged 1.40 ms, as 5 qubits
+    ~0.9 ms).  Other steps are returned unchanged."""
+    out: List[Step] = []
+    for s in steps:
+        if isinstance(s, Block):
+            k = len(s.qubits)
+            if TC_MIN <= k < KERNEL_MAX and n - (k + 1) >= 7 and all(n - 1 - q < LOW_BITS for q in s.qubits):
+                q0 = next(q for q in range(n) if q not in s.qubits)   # highest free address bit
+                assert q0 < s.qubits[0]
+                U = numpy.kron(numpy.eye(2, dtype=numpy.complex128), numpy.asarray(s.matrix, numpy.complex128))
+                out.append(Block((q0,) + tuple(s.qubits), U, s.ngates, s.amp_weight))
+                continue
+        out.append(s)
+    return out
+
+
 def plan_py(gates: Sequence[GateOp], kmax: int = 6, lookahead: int = LOOKAHEAD,
             lookahead2: int = LOOKAHEAD2) -> List[Step]:
     """Reference (pure Python) implementation of ``plan``."""

@@ -404,3 +404,29 @@ def test_make_circuit_mat_is_the_unitary():
     x = numpy.eye(8)
     want = numpy.stack([numpy.fft.ifft(x[:, i], norm="ortho") for i in range(8)], axis=1)
     numpy.testing.assert_allclose(m, want, atol=1e-12)
+
+
+@pytest.mark.parametrize("low_bits", [(4, 3, 2, 1), (4, 3, 2, 1, 0)])
+def test_widened_low_blocks_through_the_backend(low_bits):
+    """Gates on address bits 0..4 only: the fused backend widens their block by one
+    identity qubit (shuffle access instead of staged); the state matches the oracle."""
+    n = 16
+    qs = [n - 1 - b for b in low_bits]
+    rng = numpy.random.default_rng(len(low_bits))
+    gl = []
+    for _ in range(5):
+        gl += [{q: circuits.haar_2x2(rng)} for q in qs]
+        gl += [{(a, b): numpy.diag([1, 1, 1, -1]).astype(complex)} for a, b in zip(qs[:-1], qs[1:])]
+    v = (rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)) / numpy.sqrt(2 ** (n + 1))
+    st = fresh(n, v, statetype=C64, fusion=True)
+    for g in gl:
+        st.kronselect_dot(g)
+    got = st.get_state()
+    assert st.stats["blocks"] == 1 and st.stats["ops"] == 0
+    st.close()
+    want = v.astype(complex)
+    for g in gl:
+        want = sv.kronselect_dot(g, want, n)
+    err = numpy.max(numpy.abs(got - want)) / numpy.max(numpy.abs(want))
+    assert err < 5e-5, err
+    assert infidelity(got, want) < 1e-8

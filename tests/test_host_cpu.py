@@ -160,6 +160,42 @@ def test_fusion_plan_preserves_the_circuit(kmax):
     assert sum(st.ngates if isinstance(st, fusion.Block) else 1 for st in steps) == len(ops)
 
 
+@pytest.mark.parametrize("low_bits", [(3, 2, 1, 0), (4, 3, 2, 1, 0), (4, 3, 2, 1)])
+def test_low_blocks_are_widened_on_a_free_high_bit(low_bits):
+    """A block whose qubits all sit on address bits 0..4 gets one identity qubit on the
+    highest free bit; the circuit is unchanged, other steps are untouched."""
+    n = 13
+    low_qubits = tuple(n - 1 - b for b in low_bits)
+    rng = numpy.random.default_rng(11)
+    gl = []
+    for _ in range(6):
+        for q in low_qubits:
+            gl.append({q: circuits.haar_2x2(rng)})
+        for a, b in zip(low_qubits[:-1], low_qubits[1:]):
+            gl.append({(a, b): numpy.diag([1, 1, 1, -1]).astype(complex)})
+    ops = [op for g in gl for op in gates.decompose(g)]
+    steps = fusion.plan(ops, kmax=6) + gates.decompose({(0, 1): numpy.diag([1, 1, 1, -1]).astype(complex)})
+    wide = fusion.widen_low_blocks(steps, n)
+    assert fusion.widen_low_blocks(wide, n) == wide           # idempotent
+    blocks = [s for s in wide if isinstance(s, fusion.Block)]
+    assert blocks and blocks[0].qubits == (0,) + tuple(low_qubits)
+    assert len(wide) == len(steps) and wide[-1] is steps[-1]
+    v = numpy.random.default_rng(3).standard_normal(2 ** n) + 0j
+    want = got = v
+    for a, b in zip(steps, wide):
+        for x, st in ((0, a), (1, b)):
+            if isinstance(st, fusion.Block):
+                r = sv.apply_on(want if x == 0 else got, n, st.qubits, st.matrix)
+            else:
+                order, m = st.matrix()
+                r = sv.apply_on(want if x == 0 else got, n, order, m)
+            if x == 0:
+                want = r
+            else:
+                got = r
+    numpy.testing.assert_allclose(got, want, atol=1e-12)
+
+
 def test_fusion_keeps_wide_gates_standalone():
     n = 12
     ops = [op for g in circuits.grover_gates(n, 1, seed=5)[0] for op in gates.decompose(g)]
