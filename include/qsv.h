@@ -135,13 +135,19 @@ int qsv_plan_destroy(qsv_plan* p);
  * candidate is final once it holds min(kmax, nqubits) qubits, all blocked; strict: all
  * candidates of both levels must be final, else the best one), except that a round is decided on the
  * pending gates anyway while more than min_pending (> 0) are pending: the block is just
- * as valid, it may only be smaller than later gates would have allowed.  Output: the
- * planned gates in step
+ * as valid, it may only be smaller than later gates would have allowed.
+ * beam_width or beam_branch > 1: a beam search over rounds replaces the rounds where the
+ * whole list is planned (nqubits < 0) and, in prefix mode, for the steps taken while
+ * more than min_pending gates are pending.  Each kept state (a list of unplanned gates)
+ * offers its beam_branch best distinct candidates (most weight first; ties: earlier
+ * start); of all children (merged when they planned the same gate set) the beam_width
+ * with the least weight left go on.  Output: the planned gates in step
  * order (order_out, ngates entries of room), step s = order_out[step_start_out[s] ..
  * step_start_out[s+1]) (ngates + 1 entries of room), nsteps, number of planned gates. */
 int qsv_fusion_plan(int ngates, const uint64_t* qmask, const double* weight, int kmax,
-                    int lookahead, int lookahead2, int nqubits, int strict, int min_pending,
-                    int* order_out, int* step_start_out, int* nsteps_out, int* nplanned_out);
+                    int lookahead, int lookahead2, int beam_width, int beam_branch, int nqubits,
+                    int strict, int min_pending, int* order_out, int* step_start_out,
+                    int* nsteps_out, int* nplanned_out);
 /* Dense matrices of fused blocks (host, threads across blocks; no reference
  * counterpart).  Block b has block_k[b] qubits (block_qubits, ascending: the first is
  * the MSB of the block index) and block_ngates[b] gates; gate g acts on gate_nq[g]

@@ -61,8 +61,8 @@ SIGNATURES = {
                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                                   ctypes.c_void_p]),
     "qsv_fusion_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, _c_double_p, ctypes.c_int, ctypes.c_int,
-                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_int_p, _c_int_p,
-                                        _c_int_p, _c_int_p]),
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, _c_int_p, _c_int_p, _c_int_p, _c_int_p]),
     "qsv_block_matrices": (ctypes.c_int, [ctypes.c_int, _c_int_p, _c_int_p, _c_int_p, _c_int_p, _c_int_p,
                                            _c_double_p, _c_double_p]),
     "qsv_tune_blocks": (ctypes.c_int, [_handle, ctypes.c_int, _c_int_p, _c_int_p, ctypes.c_int, _c_double_p, _c_int_p]),

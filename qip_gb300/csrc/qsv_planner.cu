@@ -11,6 +11,9 @@
 // could still change (strict: some candidate, of either level, is not final; relaxed:
 // the best is not),
 // unless more than min_pending gates are pending (then the round is decided anyway).
+// With beam_width or beam_branch > 1 a beam search over rounds (beam_plan) plans the
+// whole list, or in prefix mode the steps taken while more than min_pending gates are
+// pending.
 //
 // qsv_block_matrices multiplies each block's gates into its 2^k x 2^k matrix, blocks
 // spread over host threads.
@@ -70,13 +73,131 @@ void grow(const std::vector<int>& rem, int start, const uint64_t* qmask, const i
   c.final = nS >= full_at && (S & ~blocked) == 0;
 }
 
+uint64_t gate_hash(int g) {
+  uint64_t z = (uint64_t)g + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Beam search over planning rounds.  A state is the list of gates not yet planned;
+// each state offers its `branch` best distinct candidate blocks (most work first, ties
+// to the earlier start; a gate wider than kmax at the front is a step of its own), and
+// the `width` children with the least work left (ties: earlier child) form the next
+// level.  Children that planned the same set of gates are merged (first kept).  Returns
+// the steps of the first state that planned everything.
+struct BeamState {
+  std::vector<int> rem;
+  double remw = 0.0;
+  uint64_t key = 0;
+  int node = -1;
+};
+struct BeamNode {
+  int parent;
+  std::vector<int> gates;
+};
+
+void beam_plan(const std::vector<int>& rem0, const uint64_t* qmask, const int* width, const double* weight,
+               int kmax, int lookahead, int bwidth, int bbranch, std::vector<std::vector<int>>& steps) {
+  std::vector<BeamNode> nodes;
+  std::vector<BeamState> frontier(1);
+  frontier[0].rem = rem0;
+  for (int g : rem0) frontier[0].remw += weight[g];
+  Cand c;
+  struct Opt {
+    double work;
+    std::vector<int> chosen;
+  };
+  std::vector<Opt> opts;
+  struct Child {
+    int from;
+    std::vector<int> chosen;
+    double work;
+  };
+  std::vector<Child> kids;
+  for (;;) {
+    for (const BeamState& st : frontier)
+      if (st.rem.empty()) {
+        std::vector<std::vector<int>> rev;
+        for (int nd = st.node; nd >= 0; nd = nodes[(size_t)nd].parent) rev.push_back(nodes[(size_t)nd].gates);
+        steps.assign(rev.rbegin(), rev.rend());
+        return;
+      }
+    kids.clear();
+    for (int si = 0; si < (int)frontier.size(); ++si) {
+      const std::vector<int>& rem = frontier[(size_t)si].rem;
+      opts.clear();
+      if (width[rem[0]] > kmax) {
+        opts.push_back({weight[rem[0]], {0}});
+      } else {
+        const int nc = std::min<int>(lookahead, (int)rem.size());
+        for (int s = 0; s < nc; ++s) {
+          if (width[rem[(size_t)s]] > kmax) continue;
+          grow(rem, s, qmask, width, weight, kmax, kmax, c);
+          opts.push_back({c.work, c.chosen});
+        }
+        std::stable_sort(opts.begin(), opts.end(), [](const Opt& x, const Opt& y) { return x.work > y.work; });
+      }
+      int taken = 0;
+      for (size_t i = 0; i < opts.size() && taken < bbranch; ++i) {
+        bool dup = false;
+        for (size_t j = 0; j < i && !dup; ++j) dup = opts[j].chosen == opts[i].chosen;
+        if (dup) continue;
+        kids.push_back({si, opts[i].chosen, opts[i].work});
+        ++taken;
+      }
+    }
+    // Merge children that planned the same gates (first kept), then keep the `width`
+    // with the least work left.
+    std::vector<uint64_t> keys;
+    std::vector<double> remw;
+    std::vector<int> kid;
+    for (size_t k = 0; k < kids.size(); ++k) {
+      const BeamState& st = frontier[(size_t)kids[k].from];
+      uint64_t key = st.key;
+      for (int i : kids[k].chosen) key += gate_hash(st.rem[(size_t)i]);
+      if (std::find(keys.begin(), keys.end(), key) != keys.end()) continue;
+      keys.push_back(key);
+      remw.push_back(st.remw - kids[k].work);
+      kid.push_back((int)k);
+    }
+    std::vector<int> order(kid.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return remw[(size_t)x] < remw[(size_t)y]; });
+    if ((int)order.size() > bwidth) order.resize((size_t)bwidth);
+    std::vector<BeamState> next;
+    next.reserve(order.size());
+    for (int idx : order) {
+      const Child& kd = kids[(size_t)kid[(size_t)idx]];
+      const BeamState& st = frontier[(size_t)kd.from];
+      BeamState ns;
+      ns.key = keys[(size_t)idx];
+      ns.remw = remw[(size_t)idx];
+      std::vector<char> picked(st.rem.size(), 0);
+      BeamNode nd;
+      nd.parent = st.node;
+      for (int i : kd.chosen) {
+        picked[(size_t)i] = 1;
+        nd.gates.push_back(st.rem[(size_t)i]);
+      }
+      for (size_t i = 0; i < st.rem.size(); ++i)
+        if (!picked[i]) ns.rem.push_back(st.rem[i]);
+      ns.node = (int)nodes.size();
+      nodes.push_back(std::move(nd));
+      next.push_back(std::move(ns));
+    }
+    frontier.swap(next);
+  }
+}
+
 }  // namespace
 
 extern "C" int qsv_fusion_plan(int ngates, const uint64_t* qmask, const double* weight, int kmax, int lookahead,
-                               int lookahead2, int nqubits, int strict, int min_pending, int* order_out,
-                               int* step_start_out, int* nsteps_out, int* nplanned_out) {
+                               int lookahead2, int beam_width, int beam_branch, int nqubits, int strict,
+                               int min_pending, int* order_out, int* step_start_out, int* nsteps_out,
+                               int* nplanned_out) {
   if (ngates < 0 || (ngates > 0 && (!qmask || !weight || !order_out || !step_start_out)) || !nsteps_out ||
-      !nplanned_out || kmax < 1 || kmax > 62 || lookahead < 1)
+      !nplanned_out || kmax < 1 || kmax > 62 || lookahead < 1 || beam_width < 1 || beam_branch < 1)
     return set_error(nullptr, QSV_ERR_INVALID, "bad fusion plan request");
   std::vector<int> width((size_t)std::max(ngates, 1));
   for (int g = 0; g < ngates; ++g) width[(size_t)g] = __builtin_popcountll(qmask[g]);
@@ -87,6 +208,28 @@ extern "C" int qsv_fusion_plan(int ngates, const uint64_t* qmask, const double* 
   step_start_out[0] = 0;
   Cand c, best, c2;
   std::vector<int> rest2;
+  // Beam search plans everything at once, or (prefix mode) the steps taken while more
+  // than min_pending gates are pending; the remaining gates go through the rounds below.
+  const bool use_beam = beam_width > 1 || beam_branch > 1;
+  if (use_beam && !rem.empty() && (nqubits < 0 || (min_pending > 0 && (int)rem.size() > min_pending))) {
+    std::vector<std::vector<int>> steps;
+    beam_plan(rem, qmask, width.data(), weight, kmax, lookahead, beam_width, beam_branch, steps);
+    std::vector<char> done((size_t)ngates, 0);
+    int left = (int)rem.size();
+    for (const auto& st : steps) {
+      if (nqubits >= 0 && left <= min_pending) break;
+      for (int g : st) {
+        order_out[nout++] = g;
+        done[(size_t)g] = 1;
+      }
+      step_start_out[++nsteps] = nout;
+      left -= (int)st.size();
+    }
+    next.clear();
+    for (int g : rem)
+      if (!done[(size_t)g]) next.push_back(g);
+    rem.swap(next);
+  }
   while (!rem.empty()) {
     const int first = rem[0];
     if (width[(size_t)first] > kmax) {

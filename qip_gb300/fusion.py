@@ -10,8 +10,12 @@ qubits for the rest of the scan, so every gate moved into the block commutes wit
 every gate it jumps over (they act on disjoint qubits).  Starting past the first gate
 lets a round take the block that fits the circuit's light cone instead of whatever the
 front gate implies (brickwork n=28, depth 40: 69 steps instead of 120 with a start at
-the front only and no second-level score).  Gates wider than ``kmax`` are never fused; they run on the per-gate
-kernels when they reach the front of the queue.
+the front only and no second-level score).  A beam search over rounds (``BEAM``: 16
+states kept per level, 8 candidates offered per state) plans whole lists: 64 steps for
+that circuit.  Streams (gates planned while more keep arriving) use the rounds: each
+call re-plans a window of pending gates, and there a beam gains nothing.  Gates wider than
+``kmax`` are never fused; they run on the per-gate kernels when they reach the front
+of the queue.
 
 A block of 4..6 qubits runs on the tensor cores (one HBM pass for all its gates); a
 block of 1..3 qubits becomes one dense (or diagonal) per-gate pass; a block holding
@@ -71,21 +75,22 @@ def _emit(chosen: List[GateOp]) -> Step:
 
 
 LOOKAHEAD = 16   # first-level candidates per round
-LOOKAHEAD2 = 8   # next-round candidates scored after each of them
+LOOKAHEAD2 = 8   # next-round candidates scored after each of them (rounds without beam search)
+BEAM = (16, 8)   # beam search: states kept per level, candidates offered per state
 
 
 def plan(gates: Sequence[GateOp], kmax: int = 6, lookahead: int = LOOKAHEAD,
-         lookahead2: int = LOOKAHEAD2) -> List[Step]:
+         lookahead2: int = LOOKAHEAD2, beam: Tuple[int, int] = BEAM) -> List[Step]:
     """Group ``gates`` (program order) into fused blocks and standalone gates (native
     planner and block matrices, ``qsv_fusion_plan`` / ``qsv_block_matrices``)."""
-    steps, rest = plan_prefix(gates, kmax, None, lookahead, lookahead2=lookahead2)
+    steps, rest = plan_prefix(gates, kmax, None, lookahead, lookahead2=lookahead2, beam=beam)
     assert not rest
     return steps
 
 
 def plan_prefix(gates: Sequence[GateOp], kmax: int = 6, nqubits=None, lookahead: int = LOOKAHEAD,
                 strict: bool = True, min_pending: int = 0,
-                lookahead2: int = LOOKAHEAD2) -> Tuple[List[Step], List[GateOp]]:
+                lookahead2: int = LOOKAHEAD2, beam: Tuple[int, int] = BEAM) -> Tuple[List[Step], List[GateOp]]:
     """``plan_prefix_py`` in native code: same steps, same matrices (to rounding)."""
     from . import _native as nat
 
@@ -99,7 +104,7 @@ def plan_prefix(gates: Sequence[GateOp], kmax: int = 6, nqubits=None, lookahead:
     starts = numpy.empty(ng + 1, dtype=numpy.int32)
     nsteps, nplanned = ctypes.c_int(), ctypes.c_int()
     nat.check(lib.qsv_fusion_plan(ng, qm.ctypes.data_as(ctypes.c_void_p), nat.dp(w), int(kmax), int(lookahead),
-                                  int(lookahead2),
+                                  int(lookahead2), int(beam[0]), int(beam[1]),
                                   -1 if nqubits is None else int(nqubits), int(bool(strict)), int(min_pending),
                                   nat.ip(order),
                                   nat.ip(starts), ctypes.byref(nsteps), ctypes.byref(nplanned)), None, "fusion_plan")
@@ -176,9 +181,9 @@ def widen_low_blocks(steps: Sequence[Step], n: int) -> List[Step]:
 
 
 def plan_py(gates: Sequence[GateOp], kmax: int = 6, lookahead: int = LOOKAHEAD,
-            lookahead2: int = LOOKAHEAD2) -> List[Step]:
+            lookahead2: int = LOOKAHEAD2, beam: Tuple[int, int] = BEAM) -> List[Step]:
     """Reference (pure Python) implementation of ``plan``."""
-    steps, rest = plan_prefix_py(gates, kmax, None, lookahead, lookahead2=lookahead2)
+    steps, rest = plan_prefix_py(gates, kmax, None, lookahead, lookahead2=lookahead2, beam=beam)
     assert not rest
     return steps
 
@@ -252,23 +257,103 @@ def _round(remaining: List[GateOp], kmax: int, lookahead: int, nqubits, strict: 
     return _emit([remaining[i] for i in best[1]]), [g for i, g in enumerate(remaining) if i not in picked]
 
 
+_MASK64 = (1 << 64) - 1
+
+
+def _gate_hash(g: int) -> int:
+    """splitmix64 finaliser of g (the native planner's merge key of a planned gate)."""
+    z = (g + 0x9E3779B97F4A7C15) & _MASK64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _MASK64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _MASK64
+    return z ^ (z >> 31)
+
+
+def _beam_plan(gates: Sequence[GateOp], kmax: int, lookahead: int, width: int, branch: int) -> List[List[GateOp]]:
+    """Beam search over planning rounds (the reference of the native one).  A state is
+    the list of gates not yet planned; it offers its ``branch`` best distinct candidate
+    blocks (most work first, ties to the earlier start; a gate wider than kmax at the
+    front is a step of its own).  Children that planned the same gate set are merged
+    (first kept) and the ``width`` with the least work left (ties: earlier child) form
+    the next level.  Returns the steps (gate lists) of the first complete plan."""
+    index = {id(g): i for i, g in enumerate(gates)}
+    frontier = [(list(gates), sum(g.amp_update_weight() for g in gates), 0, [])]
+    while True:
+        for rem, _, _, path in frontier:
+            if not rem:
+                return path
+        kids = []
+        for si, (rem, _, _, _) in enumerate(frontier):
+            if rem[0].width > kmax:
+                opts = [(rem[0].amp_update_weight(), [0])]
+            else:
+                opts = []
+                for s in range(min(lookahead, len(rem))):
+                    if rem[s].width > kmax:
+                        continue
+                    chosen, _, _, _ = _grow(rem, s, kmax, kmax)
+                    work = 0.0
+                    for i in chosen:
+                        work += rem[i].amp_update_weight()
+                    opts.append((work, chosen))
+                opts.sort(key=lambda o: -o[0])
+            taken = 0
+            for i, (work, chosen) in enumerate(opts):
+                if taken >= branch:
+                    break
+                if any(opts[j][1] == chosen for j in range(i)):
+                    continue
+                kids.append((si, chosen, work))
+                taken += 1
+        keys, merged = set(), []
+        for si, chosen, work in kids:
+            rem, remw, key, path = frontier[si]
+            for i in chosen:
+                key = (key + _gate_hash(index[id(rem[i])])) & _MASK64
+            if key in keys:
+                continue
+            keys.add(key)
+            merged.append((remw - work, key, si, chosen))
+        merged.sort(key=lambda m: m[0])
+        nxt = []
+        for remw, key, si, chosen in merged[:width]:
+            rem, _, _, path = frontier[si]
+            picked = set(chosen)
+            nxt.append(([g for i, g in enumerate(rem) if i not in picked], remw, key,
+                        path + [[rem[i] for i in chosen]]))
+        frontier = nxt
+
+
 def plan_prefix_py(gates: Sequence[GateOp], kmax: int = 6, nqubits=None, lookahead: int = LOOKAHEAD,
                    strict: bool = True, min_pending: int = 0,
-                   lookahead2: int = LOOKAHEAD2) -> Tuple[List[Step], List[GateOp]]:
+                   lookahead2: int = LOOKAHEAD2, beam: Tuple[int, int] = BEAM) -> Tuple[List[Step], List[GateOp]]:
     """Reference (pure Python) plan of ``gates``.  With ``nqubits`` given, stop at the first round that later
     gates could still change and return (steps so far, gates not yet planned): a
     candidate block is final once it is full (kmax qubits, or every qubit of the
     register) and each of its qubits is blocked by a gate left out of it.  ``strict``:
     a round is decided once all its candidates are final (the candidates and their
     blocks then no longer depend on later gates), so the steps returned are exactly the
-    first steps of ``plan`` over any extension of ``gates``.  Otherwise a round is
+    first steps of ``plan(beam=(1, 1))`` (rounds only) over any extension of ``gates``.  Otherwise a round is
     decided once its best candidate on these gates is final — the block is just as valid
     (it only holds gates that commute with everything it jumps over) but a candidate
     that later gates would have grown may lose.  ``min_pending`` > 0: while more gates
     than that are pending a round is decided on them regardless.  With ``nqubits=None``
-    plans everything."""
+    plans everything.  ``beam`` = (width, branch) with either > 1: a beam search
+    (``_beam_plan``) plans everything, or in prefix mode the steps taken while more than
+    ``min_pending`` gates are pending; rounds plan the rest."""
     remaining = list(gates)
     steps: List[Step] = []
+    if (beam[0] > 1 or beam[1] > 1) and remaining and (
+            nqubits is None or (min_pending > 0 and len(remaining) > min_pending)):
+        groups = _beam_plan(remaining, kmax, lookahead, beam[0], beam[1])
+        left = len(remaining)
+        done = set()
+        for grp in groups:
+            if nqubits is not None and left <= min_pending:
+                break
+            steps.append(_emit(grp))
+            done.update(id(g) for g in grp)
+            left -= len(grp)
+        remaining = [g for g in remaining if id(g) not in done]
     while remaining:
         step, remaining = _round(remaining, kmax, lookahead, nqubits, strict, min_pending, lookahead2)
         if step is None:

@@ -208,14 +208,14 @@ def test_incremental_plan_equals_full_plan():
     n = 14
     gl = circuits.brickwork(n, 10, seed=4) + circuits.grover_gates(n, 1, seed=2)[0] + circuits.brickwork(n, 3, seed=5)
     ops = [op for g in gl for op in gates.decompose(g)]
-    full = fusion.plan(ops, kmax=6)
+    full = fusion.plan(ops, kmax=6, beam=(1, 1))
     got, pending = [], []
     for i, op in enumerate(ops):
         pending.append(op)
         if len(pending) >= 50 and i % 7 == 0:
-            steps, pending = fusion.plan_prefix(pending, kmax=6, nqubits=n)
+            steps, pending = fusion.plan_prefix(pending, kmax=6, nqubits=n, beam=(1, 1))
             got.extend(steps)
-    got.extend(fusion.plan(pending, kmax=6))
+    got.extend(fusion.plan(pending, kmax=6, beam=(1, 1)))
     assert len(got) == len(full)
     for a, b in zip(got, full):
         assert type(a) is type(b)
@@ -299,13 +299,39 @@ def test_native_planner_matches_python_reference(kmax):
              circuits.random_circuit(rng, n, 200), circuits.qft_gates(n)]
     for gl in lists:
         ops = [op for g in gl for op in gates.decompose(g)]
-        _same_steps(fusion.plan(ops, kmax=kmax), fusion.plan_py(ops, kmax=kmax))
-        for cut in (40, 120):
-            for strict, keep in ((True, 0), (False, 0), (False, 30)):
-                s1, r1 = fusion.plan_prefix(ops[:cut], kmax=kmax, nqubits=n, strict=strict, min_pending=keep)
-                s2, r2 = fusion.plan_prefix_py(ops[:cut], kmax=kmax, nqubits=n, strict=strict, min_pending=keep)
-                _same_steps(s1, s2)
-                assert all(x is y for x, y in zip(r1, r2)) and len(r1) == len(r2)
+        for beam in ((1, 1), (4, 4), fusion.BEAM):   # rounds only, streaming beam, full beam
+            _same_steps(fusion.plan(ops, kmax=kmax, beam=beam), fusion.plan_py(ops, kmax=kmax, beam=beam))
+            for cut in (40, 120):
+                for strict, keep in ((True, 0), (False, 0), (False, 30)):
+                    s1, r1 = fusion.plan_prefix(ops[:cut], kmax=kmax, nqubits=n, strict=strict, min_pending=keep,
+                                                beam=beam)
+                    s2, r2 = fusion.plan_prefix_py(ops[:cut], kmax=kmax, nqubits=n, strict=strict,
+                                                   min_pending=keep, beam=beam)
+                    _same_steps(s1, s2)
+                    assert all(x is y for x, y in zip(r1, r2)) and len(r1) == len(r2)
+
+
+def test_beam_plan_preserves_the_circuit_and_saves_blocks():
+    """The beam plan is a valid reordering (same state as the gate list) and never
+    uses more steps than rounds alone on the brickwork benchmark family."""
+    n = 14
+    gl = circuits.brickwork(n, 16, seed=9)
+    ops = [op for g in gl for op in gates.decompose(g)]
+    beam = fusion.plan(ops, kmax=6)
+    rounds = fusion.plan(ops, kmax=6, beam=(1, 1))
+    assert len(beam) <= len(rounds)
+    v = numpy.random.default_rng(2).standard_normal(2 ** n) + 0j
+    want = v
+    for g in gl:
+        want = sv.kronselect_dot(g, want, n)
+    got = v
+    for st in beam:
+        if isinstance(st, fusion.Block):
+            got = sv.apply_on(got, n, st.qubits, st.matrix)
+        else:
+            order, m = st.matrix()
+            got = sv.apply_on(got, n, order, m)
+    numpy.testing.assert_allclose(got, want, atol=1e-11)
 
 
 def test_injected_allocation_failure_raises_memory_error(monkeypatch):
