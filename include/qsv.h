@@ -47,7 +47,13 @@ enum qsv_status {
 int qsv_create(int n, int dtype, qsv_state** out);
 /* Fault injection for tests: with QSV_INJECT_ALLOC_FAILURE set (not "0") qsv_create
  * fails with QSV_ERR_OOM before any device call. */
+/* qsv_destroy parks the buffers of a healthy state (at most two states' worth; amplitude
+ * buffers up to 8 GiB in total) and the next qsv_create on that device reuses
+ * them (the amplitude buffer when the size matches), so a create / run / read / destroy
+ * loop allocates nothing after its first state.  A failed allocation in qsv_create
+ * releases the parked buffers and retries; qsv_trim releases them on request. */
 int qsv_destroy(qsv_state* s);
+int qsv_trim(void);
 /* Use an external CUDA stream (cudaStream_t passed as void*; NULL = the handle's own). */
 int qsv_set_stream(qsv_state* s, void* stream);
 int qsv_synchronize(qsv_state* s);

@@ -32,6 +32,7 @@ _handle = ctypes.c_void_p
 SIGNATURES = {
     "qsv_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "qsv_destroy": (ctypes.c_int, [_handle]),
+    "qsv_trim": (ctypes.c_int, []),
     "qsv_set_stream": (ctypes.c_int, [_handle, ctypes.c_void_p]),
     "qsv_synchronize": (ctypes.c_int, [_handle]),
     "qsv_num_qubits": (ctypes.c_int, [_handle]),

@@ -515,10 +515,17 @@ class GpuBackend(StateType):
 
     # ---- lifetime -------------------------------------------------------------------------
     def close(self):
+        """Release the state; its device buffers are parked for the next state of this
+        process (``qsv_destroy``)."""
         h, self._h = getattr(self, "_h", None), None
         if h:
             self._pending = []
             self._lib.qsv_destroy(h)
+
+    @staticmethod
+    def release_parked_buffers() -> None:
+        """Free the buffers closed states left parked for later states (``qsv_trim``)."""
+        nat.check(nat.load().qsv_trim(), None, "trim")
 
     def __del__(self):
         try:

@@ -1127,6 +1127,139 @@ const char* qsv_last_error(const qsv_state* s) { return s ? s->err : g_global_er
 
 unsigned long long qsv_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
+// ---- resources of destroyed states, parked for the next state ----------------------------
+// A caller that runs one circuit per state (create, apply, read, destroy in a loop) would
+// otherwise map a 2^n buffer, page-lock image slots and unmap both for every circuit.
+// qsv_destroy parks a state's buffers (at most kMaxSpares states' worth, amplitude buffers
+// up to kMaxParkedAmp bytes in total, so other allocators in the process keep the HBM of
+// large states); qsv_create takes them back: the
+// amplitude buffer when device and size match, the other buffers when the device
+// matches.  A failed amplitude allocation releases the parked buffers and retries;
+// qsv_trim releases them on request.
+namespace {
+struct Spare {
+  int device = -1;
+  void* d_amp = nullptr;
+  size_t amp_bytes = 0;
+  int* d_flag = nullptr;
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  void* d_images = nullptr;
+  size_t d_images_bytes = 0;
+  void* h_img[qsv_state::kImageSlots] = {nullptr};
+  size_t h_img_bytes[qsv_state::kImageSlots] = {0};
+  cudaEvent_t img_ev[qsv_state::kImageSlots] = {nullptr};
+  void* h_stage = nullptr;
+  size_t h_stage_bytes = 0;
+  cudaStream_t stream = nullptr;
+};
+constexpr size_t kMaxSpares = 2;
+constexpr size_t kMaxParkedAmp = size_t(8) << 30;
+std::mutex g_spare_mu;
+std::vector<Spare> g_spares;
+
+void free_spare(Spare& sp, bool keep_amp = false) {
+  if (sp.d_amp && !keep_amp) cudaFree(sp.d_amp);
+  if (sp.d_flag) cudaFree(sp.d_flag);
+  if (sp.d_scratch) cudaFree(sp.d_scratch);
+  if (sp.d_images) cudaFree(sp.d_images);
+  for (int i = 0; i < qsv_state::kImageSlots; ++i) {
+    if (sp.h_img[i]) cudaFreeHost(sp.h_img[i]);
+    if (sp.img_ev[i]) cudaEventDestroy(sp.img_ev[i]);
+  }
+  if (sp.h_stage) cudaFreeHost(sp.h_stage);
+  if (sp.stream) cudaStreamDestroy(sp.stream);
+  sp = Spare{};
+}
+
+// Moves a parked state's resources into s (same device; the amplitude buffer only if
+// its size is `bytes`).  Returns false if nothing was parked for this device.
+bool take_spare(qsv_state* s, size_t bytes) {
+  Spare sp;
+  {
+    std::lock_guard<std::mutex> lk(g_spare_mu);
+    int pick = -1;
+    for (size_t i = 0; i < g_spares.size(); ++i)
+      if (g_spares[i].device == s->device && (pick < 0 || g_spares[i].amp_bytes == bytes)) pick = (int)i;
+    if (pick < 0) return false;
+    sp = g_spares[(size_t)pick];
+    g_spares.erase(g_spares.begin() + pick);
+  }
+  if (sp.d_amp && sp.amp_bytes != bytes) {
+    cudaFree(sp.d_amp);
+    sp.d_amp = nullptr;
+  }
+  s->d_amp = sp.d_amp;
+  s->d_flag = sp.d_flag;
+  s->d_scratch = sp.d_scratch;
+  s->scratch_bytes = sp.scratch_bytes;
+  s->d_images = sp.d_images;
+  s->d_images_bytes = sp.d_images_bytes;
+  for (int i = 0; i < qsv_state::kImageSlots; ++i) {
+    s->h_img[i] = sp.h_img[i];
+    s->h_img_bytes[i] = sp.h_img_bytes[i];
+    s->img_ev[i] = sp.img_ev[i];
+  }
+  s->h_stage = sp.h_stage;
+  s->h_stage_bytes = sp.h_stage_bytes;
+  s->own_stream = sp.stream;
+  return true;
+}
+
+// Parks s's resources (s's stream is idle).  Returns false if the cache is full.
+bool park(qsv_state* s) {
+  std::lock_guard<std::mutex> lk(g_spare_mu);
+  if (g_spares.size() >= kMaxSpares) return false;
+  size_t amp_total = s->d_amp ? (size_t(1) << s->n) * s->amp_bytes : 0;
+  for (const Spare& sp : g_spares)
+    if (sp.device == s->device) amp_total += sp.amp_bytes;
+  Spare sp;
+  sp.device = s->device;
+  if (s->d_amp && amp_total <= kMaxParkedAmp) {
+    sp.d_amp = s->d_amp;
+    sp.amp_bytes = (size_t(1) << s->n) * s->amp_bytes;
+  } else if (s->d_amp) {
+    cudaFree(s->d_amp);
+  }
+  sp.d_flag = s->d_flag;
+  sp.d_scratch = s->d_scratch;
+  sp.scratch_bytes = s->scratch_bytes;
+  sp.d_images = s->d_images;
+  sp.d_images_bytes = s->d_images_bytes;
+  for (int i = 0; i < qsv_state::kImageSlots; ++i) {
+    sp.h_img[i] = s->h_img[i];
+    sp.h_img_bytes[i] = s->h_img_bytes[i];
+    sp.img_ev[i] = s->img_ev[i];
+  }
+  sp.h_stage = s->h_stage;
+  sp.h_stage_bytes = s->h_stage_bytes;
+  sp.stream = s->own_stream;
+  g_spares.push_back(sp);
+  return true;
+}
+
+void release_spares(int device) {
+  std::vector<Spare> drop;
+  {
+    std::lock_guard<std::mutex> lk(g_spare_mu);
+    for (size_t i = 0; i < g_spares.size();) {
+      if (device < 0 || g_spares[i].device == device) {
+        drop.push_back(g_spares[i]);
+        g_spares.erase(g_spares.begin() + (long)i);
+      } else {
+        ++i;
+      }
+    }
+  }
+  for (Spare& sp : drop) free_spare(sp);
+}
+}  // namespace
+
+int qsv_trim(void) {
+  release_spares(-1);
+  return QSV_OK;
+}
+
 int qsv_create(int n, int dtype, qsv_state** out) {
   if (!out) return set_error(nullptr, QSV_ERR_INVALID, "null output handle");
   *out = nullptr;
@@ -1142,20 +1275,28 @@ int qsv_create(int n, int dtype, qsv_state** out) {
   s->n = n;
   s->dtype = dtype;
   s->amp_bytes = dtype == QSV_C64 ? 8 : 16;
+  const size_t bytes = (size_t(1) << n) * s->amp_bytes;
   cudaError_t e = cudaGetDevice(&s->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) take_spare(s, bytes);
+  if (e == cudaSuccess && !s->own_stream) e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
-    delete s;
+    qsv_destroy(s);
     return set_error(nullptr, QSV_ERR_CUDA, "device setup: %s", cudaGetErrorString(e));
   }
   s->stream = s->own_stream;
-  const size_t bytes = (size_t(1) << n) * s->amp_bytes;
-  if (cudaMalloc(&s->d_amp, bytes) != cudaSuccess || cudaMalloc(&s->d_flag, sizeof(int)) != cudaSuccess) {
+  if (!s->d_amp && cudaMalloc(&s->d_amp, bytes) != cudaSuccess) {
+    // Parked buffers of other states may hold the memory: release them and retry.
     cudaGetLastError();
-    if (s->d_amp) cudaFree(s->d_amp);
-    cudaStreamDestroy(s->own_stream);
-    delete s;
+    s->d_amp = nullptr;
+    release_spares(s->device);
+    if (cudaMalloc(&s->d_amp, bytes) != cudaSuccess) s->d_amp = nullptr;
+  }
+  if (s->d_amp && !s->d_flag && cudaMalloc(&s->d_flag, sizeof(int)) != cudaSuccess) s->d_flag = nullptr;
+  if (!s->d_amp || !s->d_flag) {
+    cudaGetLastError();
+    s->n = 0;  // nothing to park: qsv_destroy frees what was taken
+    qsv_destroy(s);
     return set_error(nullptr, QSV_ERR_OOM, "device allocation of %zu bytes failed", bytes);
   }
   int rc = QSV_OK;
@@ -1176,6 +1317,17 @@ int qsv_create(int n, int dtype, qsv_state** out) {
 int qsv_destroy(qsv_state* s) {
   if (!s) return QSV_OK;
   if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->own_stream && s->own_stream != s->stream) cudaStreamSynchronize(s->own_stream);
+  // A healthy state's buffers are parked for the next state; otherwise freed.
+  bool healthy = s->n > 0 && s->d_amp && s->d_flag && cudaGetLastError() == cudaSuccess;
+  if (healthy && s->d_flag) {
+    int flag = 0;
+    healthy = cudaMemcpy(&flag, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && flag == 0;
+  }
+  if (healthy && park(s)) {
+    delete s;
+    return QSV_OK;
+  }
   if (s->d_amp) cudaFree(s->d_amp);
   if (s->d_flag) cudaFree(s->d_flag);
   if (s->d_scratch) cudaFree(s->d_scratch);

@@ -37,3 +37,33 @@ def test_readback_arrays_are_owned_by_the_caller(monkeypatch):
     assert not isinstance(d.base, hostbuf._PinnedOwner)
     assert numpy.array_equal(d, b)
     st.close()
+
+
+def test_parked_state_buffers_start_clean():
+    """A closed state's buffers are reused by the next state: the new state still starts
+    as |0...0> and computes correctly, for the same size, another size, and after the
+    parked buffers were released."""
+    n = 20
+    rng = numpy.random.default_rng(8)
+    v = (rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)).astype(numpy.complex64)
+    h = numpy.array([[1, 1], [1, -1]]) / numpy.sqrt(2)
+    st = GpuBackend.make_state(n, [list(range(n))], [v], statetype=numpy.complex64, fusion=True)
+    for q in range(n):
+        st.kronselect_dot({q: h})
+    st.get_state()
+    st.close()
+    e0 = numpy.zeros(2 ** n, dtype=numpy.complex64)
+    e0[0] = 1
+    for size in (n, n + 1, n):
+        st = GpuBackend.make_state(size, [], [], statetype=numpy.complex64, fusion=True)
+        want = numpy.zeros(2 ** size, dtype=numpy.complex64)
+        want[0] = 1
+        assert numpy.array_equal(st.get_state(), want)
+        st.kronselect_dot({0: h})
+        got = st.get_state()
+        st.close()
+        numpy.testing.assert_allclose(got, sv.kronselect_dot({0: h}, want.astype(complex), size), atol=1e-6)
+    GpuBackend.release_parked_buffers()
+    st = GpuBackend.make_state(n, [], [], statetype=numpy.complex128)
+    assert numpy.array_equal(st.get_state(), e0.astype(numpy.complex128))
+    st.close()
