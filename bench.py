@@ -231,7 +231,7 @@ def run_ours(args):
     tuner = default_tuner()
     if args.kmax:
         kmax, width_report = args.kmax, {}
-        steps = fusion.widen_low_blocks(fusion.plan(ops, kmax=kmax), n)
+        steps = fusion.widen_low_blocks(fusion.plan(ops, kmax=kmax, beam=fusion.BEAM_WIDE), n)
         tuner.ensure_plan(st.handle, n, steps)
     else:
         # Measured fusion width and block access modes (scratch-state timings).

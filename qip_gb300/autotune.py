@@ -33,7 +33,7 @@ from typing import Dict, Iterable, List, Optional, Sequence, Tuple
 import numpy
 
 from . import _native as nat
-from .fusion import Block, plan, widen_low_blocks
+from .fusion import BEAM_WIDE, Block, plan, widen_low_blocks
 from .gates import GateOp
 
 SCRATCH_QUBITS = 26  # the library tunes on min(n, 26) qubits
@@ -164,13 +164,13 @@ class Autotuner:
         if self._width.get(n) in widths and n in self._reports:
             # Decided before (this process or a loaded cache): reuse it.
             w = self._width[n]
-            steps = widen_low_blocks(plan(ops, kmax=w), n)
+            steps = widen_low_blocks(plan(ops, kmax=w, beam=BEAM_WIDE), n)
             self.ensure_plan(handle, n, steps)
             return w, steps, dict(self._reports[n])
         best = None
         report = {}
         for w in widths:
-            steps = widen_low_blocks(plan(ops, kmax=w), n)
+            steps = widen_low_blocks(plan(ops, kmax=w, beam=BEAM_WIDE), n)
             ms = self.predict_ms(handle, n, steps)
             report[w] = ms
             if best is None or ms < best[0]:

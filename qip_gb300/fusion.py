@@ -12,7 +12,8 @@ lets a round take the block that fits the circuit's light cone instead of whatev
 front gate implies (brickwork n=28, depth 40: 69 steps instead of 120 with a start at
 the front only and no second-level score).  A beam search over rounds (``BEAM``: 16
 states kept per level, 8 candidates offered per state) plans whole lists: 64 steps for
-that circuit.  Streams (gates planned while more keep arriving) use the rounds: each
+that circuit (62 with ``BEAM_WIDE``, 64 states, used where a circuit is planned once
+ahead of its runs).  Streams (gates planned while more keep arriving) use the rounds: each
 call re-plans a window of pending gates, and there a beam gains nothing.  Gates wider than
 ``kmax`` are never fused; they run on the per-gate kernels when they reach the front
 of the queue.
@@ -77,6 +78,7 @@ def _emit(chosen: List[GateOp]) -> Step:
 LOOKAHEAD = 16   # first-level candidates per round
 LOOKAHEAD2 = 8   # next-round candidates scored after each of them (rounds without beam search)
 BEAM = (16, 8)   # beam search: states kept per level, candidates offered per state
+BEAM_WIDE = (64, 8)  # for a circuit planned once ahead of its runs (the measured width's plan)
 
 
 def plan(gates: Sequence[GateOp], kmax: int = 6, lookahead: int = LOOKAHEAD,
