@@ -1,0 +1,72 @@
+"""Parity at the benchmark's full sizes, through properties that do not need an FP64
+state of that size on the host:
+
+* brickwork n=28 depth 40 (the headline circuit), fed gate by gate through the
+  backend: the fused complex64 state against the complex128 per-gate state (both on
+  the device; the per-gate path is pinned to the reference and the oracle at smaller
+  sizes), infidelity <= 1e-6 (the metric's bound) and the norm (5e-4: see below);
+* QFT + Grover at n=32 complex64 (fused) and n=31 complex128 (per-gate, 32 GiB each):
+  the marked probability and every single-qubit marginal against Grover's closed form
+  (relative 1e-4 for complex64, 1e-10 for complex128), and the norm.
+"""
+import ctypes
+
+import numpy
+import pytest
+
+from qip_gb300 import GpuBackend, _native as nat, circuits
+
+pytestmark = pytest.mark.gpu
+
+
+def test_brickwork_n28_fused_matches_fp64_per_gate_path():
+    n = 28
+    gl = circuits.brickwork(n, 40, seed=1234)
+    fused = GpuBackend.make_state(n, [], [], statetype=numpy.complex64, fusion=True)
+    plain = GpuBackend.make_state(n, [], [], statetype=numpy.complex128, fusion=False)
+    try:
+        for g in gl:
+            fused.kronselect_dot(g)
+            plain.kronselect_dot(g)
+        fused.flush()
+        lib = nat.load()
+        re_, im_ = ctypes.c_double(), ctypes.c_double()
+        nat.check(lib.qsv_inner_product(fused.handle, plain.handle, ctypes.byref(re_), ctypes.byref(im_)),
+                  fused.handle, "inner_product")
+        n64, n128 = fused.total_prob(), plain.total_prob()
+        infid = 1.0 - (re_.value ** 2 + im_.value ** 2) / (n64 * n128)
+        assert abs(n128 - 1.0) < 1e-12
+        # Each fused block multiplies by its matrix as a bf16 hi + lo pair, exact to about
+        # 2^-17 per entry: a slightly non-unitary block changes the norm by ~1e-5 with a
+        # random sign (measured: 7e-5 after the 67 blocks of this circuit); the direction
+        # of the state, which the metric bounds, is far tighter.
+        assert abs(n64 - 1.0) < 5e-4
+        assert infid < 1e-6, infid
+        assert fused.stats["blocks"] > 0
+    finally:
+        fused.close()
+        plain.close()
+
+
+@pytest.mark.parametrize("n,statetype,rtol", [(32, numpy.complex64, 1e-4), (31, numpy.complex128, 1e-10)])
+def test_grover_full_size_closed_form(n, statetype, rtol):
+    iterations = 2
+    gl, marked = circuits.grover_gates(n, iterations, seed=7)
+    st = GpuBackend.make_state(n, [], [], statetype=statetype, fusion=statetype == numpy.complex64)
+    try:
+        for g in gl:
+            st.kronselect_dot(g)
+        marg, norm2 = st.qubit_marginals()
+        amp = st.get_relative_range(marked, marked + 1)[0]
+    finally:
+        st.close()
+    N = 2.0 ** n
+    theta = numpy.arcsin(1 / numpy.sqrt(N))
+    pm = numpy.sin((2 * iterations + 1) * theta) ** 2
+    pu = (1 - pm) / (N - 1)
+    bits = numpy.array([(marked >> (n - 1 - q)) & 1 for q in range(n)])
+    want = pm * bits + pu * (N / 2 - bits)
+    # complex64: fused blocks move the norm by ~1e-5 each (see the brickwork test).
+    assert abs(norm2 - 1.0) < (5e-4 if statetype == numpy.complex64 else 1e-12)
+    numpy.testing.assert_allclose(abs(amp) ** 2, pm, rtol=rtol)
+    numpy.testing.assert_allclose(marg, want, rtol=rtol)
