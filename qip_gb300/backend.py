@@ -242,12 +242,15 @@ class GpuBackend(StateType):
             raise ValueError("GpuBackend holds the whole state: offsets must be 0")
         ops = decompose(mats)
         for op in ops:
-            for q in op.qubits:
-                if not 0 <= q < self.n:
-                    raise ValueError("qubit index {} out of range for n={}".format(q, self.n))
+            if op.qmask >> self.n:  # (a negative index already failed building the mask)
+                bad = [q for q in sorted(op.qubits) if not 0 <= q < self.n]
+                raise ValueError("qubit index {} out of range for n={}".format(bad[0], self.n))
             # Checked on the host before anything is queued or launched: a NaN or an
             # infinity would silently spread over the whole state.
-            if op.mat is not None and not numpy.all(numpy.isfinite(op.mat)):
+            finite = getattr(op, "finite", None)
+            if finite is None:
+                finite = op.mat is None or bool(numpy.all(numpy.isfinite(op.mat)))
+            if not finite:
                 raise ValueError("matrix on qubits {} has non-finite entries".format(sorted(op.qubits)))
         if self.fusion:
             self._pending.extend(ops)
@@ -297,28 +300,52 @@ class GpuBackend(StateType):
             for op in ops:
                 self.apply_op(op)
 
+    @staticmethod
+    def _op_args(op: GateOp):
+        """The C-ABI arguments of an op, built once and kept with it (copies of a cached
+        decomposition share them through the template's ``shared`` dict)."""
+        shared = getattr(op, "shared", None)
+        args = shared.get("ffi") if shared is not None else getattr(op, "ffi", None)
+        if args is None:
+            t = nat.int_array(op.targets)
+            c = nat.int_array(op.controls)
+            keep = [t, c]
+            if op.kind in ("dense", "diag"):
+                m = nat.c128(op.mat)
+                keep.append(m)
+                args = (len(t), nat.ip(t), len(c), nat.ip(c), nat.dp(m))
+            elif op.kind == "mono":
+                p = nat.int_array(op.perm)
+                ph = nat.c128(op.mat)
+                keep += [p, ph]
+                args = (len(t), nat.ip(t), len(c), nat.ip(c), nat.ip(p), nat.dp(ph))
+            elif op.kind == "swap":
+                b = nat.int_array(op.swap_b)
+                keep.append(b)
+                args = (len(t), nat.ip(t), nat.ip(b), len(c), nat.ip(c))
+            else:
+                raise ValueError(op.kind)
+            args = (args, keep)
+            if shared is not None:
+                shared["ffi"] = args
+            else:
+                op.ffi = args
+        return args[0]
+
     def apply_op(self, op: GateOp) -> None:
         lib, h = self._lib, self._h
-        t = nat.int_array(op.targets)
-        c = nat.int_array(op.controls)
+        args = self._op_args(op)
         self.stats["ops"] += 1
         self.stats["launch_calls"] += 1
-        if op.kind == "dense":
-            m = nat.c128(op.mat)
-            self._check(lib.qsv_apply_matrix(h, len(t), nat.ip(t), len(c), nat.ip(c), nat.dp(m)), "apply_matrix")
-        elif op.kind == "diag":
-            d = nat.c128(op.mat)
-            self._check(lib.qsv_apply_diagonal(h, len(t), nat.ip(t), len(c), nat.ip(c), nat.dp(d)), "apply_diagonal")
-        elif op.kind == "mono":
-            p = nat.int_array(op.perm)
-            ph = nat.c128(op.mat)
-            self._check(lib.qsv_apply_monomial(h, len(t), nat.ip(t), len(c), nat.ip(c), nat.ip(p), nat.dp(ph)),
-                        "apply_monomial")
-        elif op.kind == "swap":
-            b = nat.int_array(op.swap_b)
-            self._check(lib.qsv_apply_swap(h, len(t), nat.ip(t), nat.ip(b), len(c), nat.ip(c)), "apply_swap")
+        kind = op.kind
+        if kind == "dense":
+            self._check(lib.qsv_apply_matrix(h, *args), "apply_matrix")
+        elif kind == "diag":
+            self._check(lib.qsv_apply_diagonal(h, *args), "apply_diagonal")
+        elif kind == "mono":
+            self._check(lib.qsv_apply_monomial(h, *args), "apply_monomial")
         else:
-            raise ValueError(op.kind)
+            self._check(lib.qsv_apply_swap(h, *args), "apply_swap")
 
     def apply_blocks(self, blocks: Sequence[Block]) -> None:
         """Apply fused blocks of 4..6 qubits on the tensor cores (complex64 only)."""

@@ -20,6 +20,7 @@ matrix on the union of its indices.
 """
 from __future__ import annotations
 
+import copy
 from dataclasses import dataclass, field
 from typing import Any, Dict, List, Mapping, Sequence, Tuple
 
@@ -199,8 +200,63 @@ def union_matrix(entries: Dict[Tuple[int, ...], Any]) -> Tuple[Tuple[int, ...], 
     return flat, out
 
 
+def _mat_key(m: Any):
+    """Content key of a matrix value (numpy, CMat, SwapMat), or None when it has none."""
+    tag = getattr(m, "_kron_struct", None)
+    if tag == KRON_CMAT:
+        inner = _mat_key(m.m)
+        return None if inner is None else ("C", inner)
+    if tag == KRON_SWAP:
+        return ("S", int(m.n))
+    if type(m) is numpy.ndarray and m.dtype.kind in "biufc" and m.size <= 1024:
+        return (m.dtype.str, m.shape, m.tobytes())
+    return None
+
+
+_CACHE_MAX = 4096
+_cache: Dict[Any, List[GateOp]] = {}
+
+
 def decompose(mats: Mapping[Any, Any]) -> List[GateOp]:
-    """Turn one ``kronselect_dot`` dictionary into a list of GateOps (in order)."""
+    """Turn one ``kronselect_dot`` dictionary into a list of GateOps (in order).
+
+    Graph ops hand the same matrices to every run (the reference caches them per node,
+    ``qip/operators.py:17-18``), so results are cached by content: the dictionary's keys
+    and each matrix's dtype, shape and bytes.  A hit returns fresh copies of the cached
+    ops (callers own what they get; the matrix arrays are shared and never written)."""
+    key = []
+    for indices in mats:
+        if type(indices) not in (tuple, int):
+            key = None
+            break
+        mk = _mat_key(mats[indices])
+        if mk is None:
+            key = None
+            break
+        key.append((indices, mk))
+    if key is not None:
+        key = tuple(key)
+        hit = _cache.get(key)
+        if hit is not None:
+            return [copy.copy(op) for op in hit]
+    ops = _decompose(mats)
+    if key is not None:
+        if len(_cache) >= _CACHE_MAX:
+            _cache.clear()
+        for op in ops:
+            # The cached op must not alias the caller's arrays, which may change later.
+            if op.mat is not None:
+                op.mat = numpy.array(op.mat, copy=True)
+            if op.perm is not None:
+                op.perm = numpy.array(op.perm, copy=True)
+            op.finite = op.mat is None or bool(numpy.all(numpy.isfinite(op.mat)))
+            op.shared = {}  # per-template data the copies share (the backend's call arguments)
+        _cache[key] = ops
+        return [copy.copy(op) for op in ops]
+    return ops
+
+
+def _decompose(mats: Mapping[Any, Any]) -> List[GateOp]:
     entries = normalize_mats(mats)
     ops_per_entry = [(_entry_ops(key, m), key, m) for key, m in entries.items()]
     if len(entries) > 1:

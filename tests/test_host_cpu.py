@@ -349,3 +349,20 @@ def test_trace_ranges_are_callable_without_a_profiler():
 
     lib = nat.load()
     assert lib.qsv_trace_push(b"node") == 0 and lib.qsv_trace_pop() == 0
+
+
+def test_decompose_cache_follows_matrix_content():
+    """Decompositions are cached by content: a matrix edited in place after a call is
+    decomposed again, the cached ops never alias the caller's arrays, and every call
+    returns its own op objects."""
+    u = numpy.array([[0.6, 0.8], [0.8, -0.6]], dtype=numpy.complex128)
+    a = gates.decompose({3: u})
+    b = gates.decompose({3: u})
+    assert a[0] is not b[0] and a[0].kind == b[0].kind == "dense"
+    assert not numpy.shares_memory(a[0].mat, u)
+    u[:] = numpy.diag([1.0, -1.0])
+    c = gates.decompose({3: u})
+    assert c[0].kind == "diag"
+    numpy.testing.assert_array_equal(a[0].mat, [[0.6, 0.8], [0.8, -0.6]])
+    d = gates.decompose({(0, 1): CMat(numpy.array([[0, 1], [1, 0]]))})
+    assert d[0].kind == "mono" and d[0].controls == (0,) and d[0].targets == (1,)
