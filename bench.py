@@ -232,8 +232,7 @@ def run_ours(args):
     tuner = default_tuner()
     if args.kmax:
         kmax, width_report = args.kmax, {}
-        steps = fusion.widen_low_blocks(fusion.plan(ops, kmax=kmax, beam=fusion.BEAM_WIDE), n)
-        tuner.ensure_plan(st.handle, n, steps)
+        steps = tuner.place(st.handle, n, fusion.plan(ops, kmax=kmax, beam=fusion.BEAM_WIDE))
     else:
         # Measured fusion width and block access modes (scratch-state timings).
         kmax, steps, width_report = tuner.choose_width(st.handle, n, ops)
@@ -578,8 +577,7 @@ def run_hbm(args):
         per_kind = {}
         e0, e1 = _events()
         if fusion_on:
-            steps = fusion.widen_low_blocks(fusion.plan(ops, kmax=6), n)
-            default_tuner().ensure_plan(st.handle, n, steps)
+            steps = default_tuner().place(st.handle, n, fusion.plan(ops, kmax=6))
         else:
             steps = ops
         t_all0, t_all1 = _events()

@@ -33,7 +33,7 @@ from typing import Dict, Iterable, List, Optional, Sequence, Tuple
 import numpy
 
 from . import _native as nat
-from .fusion import BEAM_WIDE, Block, plan, widen_low_blocks
+from .fusion import BEAM_WIDE, Block, plan, widen_blocks
 from .gates import GateOp
 
 SCRATCH_QUBITS = 26  # the library tunes on min(n, 26) qubits
@@ -130,6 +130,22 @@ class Autotuner:
         times, best = self._ms[(min(n, SCRATCH_QUBITS), k, low)]
         return times[best] * 2.0 ** (n - min(n, SCRATCH_QUBITS))
 
+    def place(self, handle, n: int, steps) -> list:
+        """``widen_blocks`` where it measured faster: each tensor-core block of fewer
+        than 6 qubits becomes its 6-qubit form (identity on the added qubits) when that
+        class's tuned time is not above its own."""
+        wide = widen_blocks(steps, n)
+        classes = {placement_class(s.qubits, n) for s in list(steps) + wide if tensor_core_block(s, n)}
+        if classes:
+            self.tune(handle, n, classes)
+        out = []
+        for a, b in zip(steps, wide):
+            if a is not b and tensor_core_block(a, n) and tensor_core_block(b, n) and \
+                    self.block_ms(n, *placement_class(b.qubits, n)) > self.block_ms(n, *placement_class(a.qubits, n)):
+                b = a
+            out.append(b)
+        return out
+
     def ensure_plan(self, handle, n: int, steps) -> None:
         """Tune the placement classes of the tensor-core blocks of a plan."""
         classes = {placement_class(s.qubits, n) for s in steps if tensor_core_block(s, n)}
@@ -164,13 +180,12 @@ class Autotuner:
         if self._width.get(n) in widths and n in self._reports:
             # Decided before (this process or a loaded cache): reuse it.
             w = self._width[n]
-            steps = widen_low_blocks(plan(ops, kmax=w, beam=BEAM_WIDE), n)
-            self.ensure_plan(handle, n, steps)
+            steps = self.place(handle, n, plan(ops, kmax=w, beam=BEAM_WIDE))
             return w, steps, dict(self._reports[n])
         best = None
         report = {}
         for w in widths:
-            steps = widen_low_blocks(plan(ops, kmax=w, beam=BEAM_WIDE), n)
+            steps = self.place(handle, n, plan(ops, kmax=w, beam=BEAM_WIDE))
             ms = self.predict_ms(handle, n, steps)
             report[w] = ms
             if best is None or ms < best[0]:

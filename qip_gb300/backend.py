@@ -22,7 +22,7 @@ import numpy
 from . import _native as nat
 from . import hostbuf
 from .autotune import default_tuner
-from .fusion import Block, plan, plan_prefix, widen_low_blocks
+from .fusion import Block, plan, plan_prefix, widen_blocks
 from .gates import GateOp, classify_matrix, decompose
 from .util import InitialState, IndexType, MatrixType
 
@@ -363,9 +363,10 @@ class GpuBackend(StateType):
 
     def run_plan(self, steps) -> None:
         """Execute a fusion plan: runs of tensor-core blocks go in one call."""
-        steps = widen_low_blocks(steps, self.n)
         if self.autotune:
-            default_tuner().ensure_plan(self._h, self.n, steps)
+            steps = default_tuner().place(self._h, self.n, steps)
+        else:
+            steps = widen_blocks(steps, self.n)
         batch: List[Block] = []
         for st in steps:
             if isinstance(st, Block) and len(st.qubits) >= 4 and self.n - len(st.qubits) >= 7:

@@ -157,26 +157,29 @@ def emit_native(groups: Sequence[Sequence[GateOp]]) -> List[Step]:
     return steps
 
 
-LOW_BITS = 5     # address bits 0..4: the lanes of one 32-amplitude warp access
 KERNEL_MAX = 6   # widest tensor-core block
 
 
-def widen_low_blocks(steps: Sequence[Step], n: int) -> List[Step]:
-    """Place a plan on an n-qubit state.  A tensor-core block of k < 6 qubits whose
-    qubits all sit on address bits 0..4 (qubit q <-> bit n-1-q) can only move through
-    shared memory (staged access, two extra passes over each tile); one more qubit on
-    the highest free address bit, with the identity there (U -> I (x) U), lets the
-    shuffle access take it (n=28: 4 qubits on bits 1..4 staged 1.40 ms, as 5 qubits
-    ~0.9 ms).  Other steps are returned unchanged."""
+def widen_blocks(steps: Sequence[Step], n: int) -> List[Step]:
+    """Place a plan on an n-qubit state: every tensor-core block of k < 6 qubits gets
+    6 - k more qubits on the highest free address bits (qubit q <-> bit n-1-q), with the
+    identity there.  The pass costs the same HBM traffic at any k, and the 6-qubit
+    kernel runs it faster: its tiles are twice or four times larger, so the per-tile
+    overhead is paid less often (n=26, targets on high bits: 0.19 ms at k=6 against
+    0.23 ms at k=5 and 0.32 ms at k=4).  It also moves blocks whose qubits all sit on
+    address bits 0..4 (staged access only: n=28, 4 qubits on bits 1..4, 1.40 ms) to the
+    shuffle access.  Other steps are returned unchanged."""
     out: List[Step] = []
     for s in steps:
         if isinstance(s, Block):
             k = len(s.qubits)
-            if TC_MIN <= k < KERNEL_MAX and n - (k + 1) >= 7 and all(n - 1 - q < LOW_BITS for q in s.qubits):
-                q0 = next(q for q in range(n) if q not in s.qubits)   # highest free address bit
-                assert q0 < s.qubits[0]
-                U = numpy.kron(numpy.eye(2, dtype=numpy.complex128), numpy.asarray(s.matrix, numpy.complex128))
-                out.append(Block((q0,) + tuple(s.qubits), U, s.ngates, s.amp_weight))
+            if TC_MIN <= k < KERNEL_MAX and n - KERNEL_MAX >= 7:
+                extra = [q for q in range(n) if q not in s.qubits][:KERNEL_MAX - k]
+                qs = tuple(sorted(tuple(s.qubits) + tuple(extra)))
+                axis_of = {q: i for i, q in enumerate(qs)}
+                U = _embed(numpy.eye(1 << KERNEL_MAX, dtype=numpy.complex128), axis_of, KERNEL_MAX,
+                           tuple(s.qubits), numpy.asarray(s.matrix, numpy.complex128))
+                out.append(Block(qs, U, s.ngates, s.amp_weight))
                 continue
         out.append(s)
     return out

@@ -160,12 +160,13 @@ def test_fusion_plan_preserves_the_circuit(kmax):
     assert sum(st.ngates if isinstance(st, fusion.Block) else 1 for st in steps) == len(ops)
 
 
-@pytest.mark.parametrize("low_bits", [(3, 2, 1, 0), (4, 3, 2, 1, 0), (4, 3, 2, 1)])
-def test_low_blocks_are_widened_on_a_free_high_bit(low_bits):
-    """A block whose qubits all sit on address bits 0..4 gets one identity qubit on the
-    highest free bit; the circuit is unchanged, other steps are untouched."""
+@pytest.mark.parametrize("low_bits", [(3, 2, 1, 0), (4, 3, 2, 1, 0), (4, 3, 2, 1), (12, 7, 5, 3), (12, 10, 9, 1)])
+def test_small_blocks_are_widened_to_six_qubits(low_bits):
+    """A tensor-core block of fewer than 6 qubits gets identity qubits on the highest
+    free bits (also between its own qubits); the circuit is unchanged, other steps are
+    untouched."""
     n = 13
-    low_qubits = tuple(n - 1 - b for b in low_bits)
+    low_qubits = tuple(sorted(n - 1 - b for b in low_bits))
     rng = numpy.random.default_rng(11)
     gl = []
     for _ in range(6):
@@ -175,10 +176,11 @@ def test_low_blocks_are_widened_on_a_free_high_bit(low_bits):
             gl.append({(a, b): numpy.diag([1, 1, 1, -1]).astype(complex)})
     ops = [op for g in gl for op in gates.decompose(g)]
     steps = fusion.plan(ops, kmax=6) + gates.decompose({(0, 1): numpy.diag([1, 1, 1, -1]).astype(complex)})
-    wide = fusion.widen_low_blocks(steps, n)
-    assert fusion.widen_low_blocks(wide, n) == wide           # idempotent
+    wide = fusion.widen_blocks(steps, n)
+    assert fusion.widen_blocks(wide, n) == wide           # idempotent
     blocks = [s for s in wide if isinstance(s, fusion.Block)]
-    assert blocks and blocks[0].qubits == (0,) + tuple(low_qubits)
+    extra = [q for q in range(n) if q not in low_qubits][:6 - len(low_qubits)]
+    assert blocks and blocks[0].qubits == tuple(sorted(tuple(low_qubits) + tuple(extra)))
     assert len(wide) == len(steps) and wide[-1] is steps[-1]
     v = numpy.random.default_rng(3).standard_normal(2 ** n) + 0j
     want = got = v
