@@ -53,11 +53,23 @@ struct RedAcc<double> {
   __device__ __forceinline__ double value() const { return s; }
 };
 
+// Sum over the warp in the state's own precision (complex64 states: FP32, whose partial
+// sums already carry FP32 rounding; FP64 shuffles and adds run at a fraction of the FP32
+// rate here), returned as double for the FP64 accumulation that follows.
+__device__ __forceinline__ double warp_sum_r(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return (double)v;
+}
+__device__ __forceinline__ double warp_sum_r(double v);
+
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+
+__device__ __forceinline__ double warp_sum_r(double v) { return warp_sum_d(v); }
 
 __device__ __forceinline__ double block_sum_d(double v, double* sh) {
   v = warp_sum_d(v);
@@ -539,7 +551,7 @@ __global__ void __launch_bounds__(SEG_THREADS, sizeof(R) == 4 ? 2 : 1)
         if (i >= G.count) continue;
         const int k = G.first + i;
         if (!((gsh[k].gp >> 24) & 3)) continue;
-        const double w = warp_sum_d((double)part[i]);
+        const double w = warp_sum_r(part[i]);
         if (lane == 0 && slot_of[k] >= 0) accw[slot_of[k] * 16 + warp] += w;
       }
       __syncthreads();
