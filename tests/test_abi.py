@@ -44,3 +44,21 @@ def test_library_is_sm103a_only():
     from qip_gb300 import build
 
     assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_state_size_and_dtype_limits_without_a_device():
+    """qsv_create rejects n outside [1, 34] and unknown dtypes before any device call;
+    the Python layer raises the reference's ValueError for them."""
+    import numpy
+    import pytest
+
+    from qip_gb300 import GpuBackend, _native
+
+    lib = _native.load()
+    h = ctypes.c_void_p()
+    for n, dtype in ((0, 1), (35, 0), (10, 7)):
+        assert lib.qsv_create(n, dtype, ctypes.byref(h)) == 1  # QSV_ERR_INVALID
+        assert lib.qsv_last_error(None)
+        assert not h.value
+    with pytest.raises(ValueError):
+        GpuBackend.make_state(35, [], [], statetype=numpy.complex64)
