@@ -348,6 +348,16 @@ def run_ours(args):
     nat.check(lib.qsv_norm2(st.handle, nat.dp(nrm)), st.handle)
     nat.check(lib.qsv_norm2(ref.handle, nat.dp(nrm_ref)), ref.handle)
     infid = 1.0 - (re_.value ** 2 + im_.value ** 2) / (nrm[0] * nrm_ref[0])
+    # Largest amplitude difference, read back in chunks (outside any timed region).
+    max_err = 0.0
+    chunk = 1 << min(n, 24)
+    a64 = numpy.empty(chunk, dtype=numpy.complex64)
+    a128 = numpy.empty(chunk, dtype=numpy.complex128)
+    for start in range(0, 1 << n, chunk):
+        nat.check(lib.qsv_read_range(st.handle, a64.ctypes.data_as(ctypes.c_void_p), start, chunk), st.handle)
+        nat.check(lib.qsv_read_range(ref.handle, a128.ctypes.data_as(ctypes.c_void_p), start, chunk), ref.handle)
+        max_err = max(max_err, float(numpy.max(numpy.abs(a64.astype(numpy.complex128) - a128))))
+    del a64, a128
     ref.close()
     lib.qsv_plan_destroy(plan)
     st.close()
@@ -406,6 +416,7 @@ def run_ours(args):
                        "launches_per_step": len(ops)},
         "speedup_fused_vs_plain_fp64": t_plain / t_fused,
         "infidelity_vs_fp64": infid,
+        "max_abs_err_vs_fp64": max_err,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum "
                      "of one k_block_tc launch at n=25, scaled by 2^(n-25)",
