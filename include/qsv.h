@@ -54,6 +54,13 @@ int qsv_create(int n, int dtype, qsv_state** out);
  * releases the parked buffers and retries; qsv_trim releases them on request. */
 int qsv_destroy(qsv_state* s);
 int qsv_trim(void);
+/* Bounds-checked build (libqsv_checked.so, compiled with -DQSV_BOUNDS_CHECK): every
+ * kernel tests each computed state index against the state's size before the access,
+ * counts bad ones and skips them (nothing traps).  qsv_bounds_report waits for the
+ * device, returns the count and the first bad index since the last report, and clears
+ * them.  In the normal build it returns QSV_ERR_UNSUPPORTED.  No reference counterpart
+ * (the reference compiles its kernels without bounds checks, kronprod.pyx:41-42). */
+int qsv_bounds_report(unsigned long long* count, unsigned long long* first_index);
 /* Use an external CUDA stream (cudaStream_t passed as void*; NULL = the handle's own). */
 int qsv_set_stream(qsv_state* s, void* stream);
 int qsv_synchronize(qsv_state* s);

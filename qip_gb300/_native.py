@@ -33,6 +33,7 @@ SIGNATURES = {
     "qsv_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "qsv_destroy": (ctypes.c_int, [_handle]),
     "qsv_trim": (ctypes.c_int, []),
+    "qsv_bounds_report": (ctypes.c_int, [ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong)]),
     "qsv_set_stream": (ctypes.c_int, [_handle, ctypes.c_void_p]),
     "qsv_synchronize": (ctypes.c_int, [_handle]),
     "qsv_num_qubits": (ctypes.c_int, [_handle]),
@@ -118,10 +119,13 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     with _lock:
         if _lib is not None:
             return _lib
-        path = _build.LIB
+        # QSV_BOUNDS_CHECK=1 selects the bounds-checked library (tests of the kernels'
+        # indexing); it must have been built (qip_gb300.build.build(checked=True)).
+        checked = os.environ.get("QSV_BOUNDS_CHECK", "0") not in ("", "0")
+        path = _build.LIB_CHECKED if checked else _build.LIB
         if not os.path.exists(path):
-            if not build_if_missing:
-                raise OSError(f"{path} is missing; run qip_gb300.build.build()")
+            if not build_if_missing or checked:
+                raise OSError(f"{path} is missing; run qip_gb300.build.build(checked={checked})")
             _build.build()
         lib = ctypes.CDLL(path)
         for name, (res, args) in SIGNATURES.items():

@@ -112,6 +112,7 @@ __global__ void __launch_bounds__(QSV_THREADS)
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < a.ngroups; g += stride) {
     const uint64_t i0 = qsv_insert_zeros(g, a.pos, a.npos) | a.ctrl;
+    if (!QSV_IN_BOUNDS(i0 + hi, 1ull << a.n)) continue;
     const CT<R> x = v[i0], y = v[i0 + hi];
     CT<R> o0, o1;
     o0.x = R(0); o0.y = R(0); o1 = o0;
@@ -165,6 +166,7 @@ __global__ void __launch_bounds__(QSV_THREADS)
   RedAcc<R> acc;
   for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < a.ngroups; g += stride) {
     const uint64_t i0 = qsv_insert_zeros(g, a.pos, a.npos) | a.ctrl;
+    if (!QSV_IN_BOUNDS(i0 + hi, 1ull << a.n)) continue;
     const CT<R> x = pv[i0], y = pv[i0 + hi];
     const CT<R> l0 = lv[i0], l1 = lv[i0 + hi];
     if (gen == 2) {
@@ -400,7 +402,8 @@ __device__ __forceinline__ void group_adjoint(CT<R>* v, CT<R>* l, int chunk, con
 // thread issued before the first shared store (the gather is latency-bound otherwise).
 template <typename R, bool TWO>
 __device__ __forceinline__ void seg_gather(const CT<R>* src, const CT<R>* src2, CT<R>* v, CT<R>* v2, int chunk,
-                                           uint64_t base, const uint64_t* dlo, const uint64_t* dhi) {
+                                           uint64_t base, const uint64_t* dlo, const uint64_t* dhi,
+                                           [[maybe_unused]] uint64_t limit) {
   constexpr int GB = TWO ? (sizeof(R) == 4 ? 8 : 4) : (sizeof(R) == 4 ? 16 : 8);
   for (int e0 = threadIdx.x; e0 < chunk; e0 += GB * blockDim.x) {
     CT<R> t[GB], t2[TWO ? GB : 1];
@@ -409,6 +412,7 @@ __device__ __forceinline__ void seg_gather(const CT<R>* src, const CT<R>* src2, 
       const int e = e0 + j * blockDim.x;
       if (e < chunk) {
         const uint64_t ad = base + dlo[e & 127] + dhi[e >> 7];
+        if (!QSV_IN_BOUNDS(ad, limit)) continue;
         t[j] = src[ad];
         if constexpr (TWO) t2[j] = src2[ad];
       }
@@ -477,7 +481,7 @@ __global__ void __launch_bounds__(SEG_THREADS, 2)
   __syncthreads();
   for (uint64_t ch = blockIdx.x; ch < a.nchunks; ch += gridDim.x) {
     const uint64_t base = qsv_insert_zeros(ch, a.lpos, a.lb);
-    seg_gather<R, false>(st, nullptr, v, nullptr, chunk, base, dlo, dhi);
+    seg_gather<R, false>(st, nullptr, v, nullptr, chunk, base, dlo, dhi, 1ull << a.n);
     __syncthreads();
     for (int q = 0; q < a.ngroups; ++q) {
       const SegGroup G = grsh[q];
@@ -491,7 +495,8 @@ __global__ void __launch_bounds__(SEG_THREADS, 2)
         group_forward<R, 3>(v, chunk, gb, gsh, msh, G.first, G.count);
       __syncthreads();
     }
-    for (int e = threadIdx.x; e < chunk; e += blockDim.x) st[base + dlo[e & 127] + dhi[e >> 7]] = v[phys(e)];
+    for (int e = threadIdx.x; e < chunk; e += blockDim.x)
+      if (QSV_IN_BOUNDS(base + dlo[e & 127] + dhi[e >> 7], 1ull << a.n)) st[base + dlo[e & 127] + dhi[e >> 7]] = v[phys(e)];
     __syncthreads();
   }
 }
@@ -531,7 +536,7 @@ __global__ void __launch_bounds__(SEG_THREADS, sizeof(R) == 4 ? 2 : 1)
   __syncthreads();
   for (uint64_t ch = blockIdx.x; ch < a.nchunks; ch += gridDim.x) {
     const uint64_t base = qsv_insert_zeros(ch, a.lpos, a.lb);
-    seg_gather<R, true>(sp, sl, v, l, chunk, base, dlo, dhi);
+    seg_gather<R, true>(sp, sl, v, l, chunk, base, dlo, dhi, 1ull << a.n);
     __syncthreads();
     for (int q = a.ngroups - 1; q >= 0; --q) {
       const SegGroup G = grsh[q];
@@ -558,6 +563,7 @@ __global__ void __launch_bounds__(SEG_THREADS, sizeof(R) == 4 ? 2 : 1)
     }
     for (int e = threadIdx.x; e < chunk; e += blockDim.x) {
       const uint64_t ad = base + dlo[e & 127] + dhi[e >> 7];
+      if (!QSV_IN_BOUNDS(ad, 1ull << a.n)) continue;
       sp[ad] = v[phys(e)];
       sl[ad] = l[phys(e)];
     }
@@ -571,6 +577,22 @@ __global__ void __launch_bounds__(SEG_THREADS, sizeof(R) == 4 ? 2 : 1)
     atomicAdd(&grads[(uint64_t)s * grad_stride + (gates[k].gp & 0xFFFFFF)], sum);
   }
 }
+
+}  // namespace
+
+namespace qsv {
+int oob_take_adjoint(unsigned long long* count, unsigned long long* first) {
+#ifdef QSV_BOUNDS_CHECK
+  return qsv_oob_take_unit(count, first);
+#else
+  (void)count;
+  (void)first;
+  return 0;
+#endif
+}
+}  // namespace qsv
+
+namespace {
 
 int g_sms = 0;
 int sms() {

@@ -200,7 +200,8 @@ __device__ void run_segments(float2* sv, float2* out, int n, const qsv_gate_rec*
 #pragma unroll
         for (int j = 0; j < PER; ++j) {
           const int e = threadIdx.x + j * CB_THREADS;
-          t[j] = out[base + dlo[e & 127] + dhi[e >> 7]];
+          t[j] = QSV_IN_BOUNDS(base + dlo[e & 127] + dhi[e >> 7], 1ull << n) ? out[base + dlo[e & 127] + dhi[e >> 7]]
+                                                                            : make_float2(0.f, 0.f);
         }
 #pragma unroll
         for (int j = 0; j < PER; ++j) sv[threadIdx.x + j * CB_THREADS] = t[j];
@@ -212,7 +213,8 @@ __device__ void run_segments(float2* sv, float2* out, int n, const qsv_gate_rec*
         __syncthreads();
       }
 #pragma unroll 8
-      for (int e = threadIdx.x; e < CHUNK; e += blockDim.x) out[base + dlo[e & 127] + dhi[e >> 7]] = sv[e];
+      for (int e = threadIdx.x; e < CHUNK; e += blockDim.x)
+        if (QSV_IN_BOUNDS(base + dlo[e & 127] + dhi[e >> 7], 1ull << n)) out[base + dlo[e & 127] + dhi[e >> 7]] = sv[e];
       __syncthreads();
     }
   }
@@ -280,6 +282,18 @@ int capture(qsv_circuits* b, cudaStream_t stream) {
 }
 
 }  // namespace
+
+namespace qsv {
+int oob_take_circuits(unsigned long long* count, unsigned long long* first) {
+#ifdef QSV_BOUNDS_CHECK
+  return qsv_oob_take_unit(count, first);
+#else
+  (void)count;
+  (void)first;
+  return 0;
+#endif
+}
+}  // namespace qsv
 
 extern "C" {
 

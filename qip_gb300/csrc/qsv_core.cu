@@ -207,8 +207,13 @@ __global__ void __launch_bounds__(QSV_THREADS)
     k_dense(CT<R>* __restrict__ psi, const __grid_constant__ DenseArgs<R, K> a) {
   constexpr int D = 1 << K;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t lim = a.ngroups << a.npos;  // the state's size
   for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < a.ngroups; g += stride) {
     const uint64_t base = qsv_insert_zeros(g, a.pos, a.npos) | a.ctrl;
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < D; j += 1 << VB) ok = ok && QSV_IN_BOUNDS(base + a.off[j] + (1u << VB) - 1u, lim);
+    if (!ok) continue;
     CT<R> v[D];
     if constexpr (VB > 0) {
       static_assert(K <= 3 && VB <= K, "vector path covers up to 3 targets");
@@ -271,6 +276,7 @@ __global__ void __launch_bounds__(QSV_THREADS)
   const uint64_t hi = 1ull << a.p;
   for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < a.ngroups; g += stride) {
     const uint64_t i0 = ((g >> a.p) << (a.p + 1)) | (g & lowmask);
+    if (!QSV_IN_BOUNDS(i0 + hi, a.ngroups << 1)) continue;
     const CT<R> x = psi[i0];
     const CT<R> y = psi[i0 + hi];
     CT<R> o0, o1;
@@ -320,10 +326,12 @@ __global__ void __launch_bounds__(QSV_THREADS)
       CT<R> x[U];
 #pragma unroll
       for (int u = 0; u < U; ++u)
-        if (g0 + u * stride < a.ngroups) x[u] = psi[base[u] + a.off[e]];
+        if (g0 + u * stride < a.ngroups && QSV_IN_BOUNDS(base[u] + a.off[e], a.ngroups << a.npos))
+          x[u] = psi[base[u] + a.off[e]];
 #pragma unroll
       for (int u = 0; u < U; ++u)
-        if (g0 + u * stride < a.ngroups) psi[base[u] + a.off[e]] = qsv_cmul(a.ph[e], x[u]);
+        if (g0 + u * stride < a.ngroups && QSV_IN_BOUNDS(base[u] + a.off[e], a.ngroups << a.npos))
+          psi[base[u] + a.off[e]] = qsv_cmul(a.ph[e], x[u]);
     }
   }
 }
@@ -350,6 +358,10 @@ __global__ void __launch_bounds__(QSV_THREADS)
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < a.ngroups; g += stride) {
     const uint64_t base = qsv_insert_zeros(g, a.pos, a.npos) | a.ctrl;
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < D; ++j) ok = ok && QSV_IN_BOUNDS(base + a.off[j], a.ngroups << a.npos);
+    if (!ok) continue;
     CT<R> v[D];
 #pragma unroll
     for (int j = 0; j < D; ++j) v[j] = psi[base + a.off[j]];
@@ -399,14 +411,14 @@ __global__ void __launch_bounds__(QSV_THREADS)
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       idx[u] = qsv_insert_zeros(t0 + u * stride, a.pos, a.npos) | a.ctrl;
-      if (t0 + u * stride < a.nitems) {
+      if (t0 + u * stride < a.nitems && QSV_IN_BOUNDS(idx[u] | a.flip, a.nitems << a.npos)) {
         x[u] = psi[idx[u]];
         y[u] = psi[idx[u] ^ a.flip];
       }
     }
 #pragma unroll
     for (int u = 0; u < U; ++u)
-      if (t0 + u * stride < a.nitems) {
+      if (t0 + u * stride < a.nitems && QSV_IN_BOUNDS(idx[u] | a.flip, a.nitems << a.npos)) {
         psi[idx[u]] = y[u];
         psi[idx[u] ^ a.flip] = x[u];
       }
@@ -430,6 +442,7 @@ __global__ void __launch_bounds__(QSV_THREADS)
     }
     if (x < y) {
       const uint64_t partner = idx ^ flip;
+      if (!QSV_IN_BOUNDS(idx | flip, a.nitems << a.ncp)) continue;
       const CT<R> u = psi[idx];
       const CT<R> w = psi[partner];
       psi[idx] = w;
@@ -570,11 +583,17 @@ __global__ void __launch_bounds__(QSV_THREADS)
   for (; r + 3 * bd < r1; r += 4 * bd) {
     CT<R> v[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) v[u] = psi[qsv_insert_zeros(r + u * bd, a.pos, a.npos) | binbase];
+    for (int u = 0; u < 4; ++u) {
+      const uint64_t i = qsv_insert_zeros(r + u * bd, a.pos, a.npos) | binbase;
+      v[u] = QSV_IN_BOUNDS(i, a.nrest << a.npos) ? psi[i] : CT<R>{};
+    }
 #pragma unroll
     for (int u = 0; u < 4; ++u) acc[u].add(S::term(v[u]));
   }
-  for (; r < r1; r += bd) acc[0].add(S::term(psi[qsv_insert_zeros(r, a.pos, a.npos) | binbase]));
+  for (; r < r1; r += bd) {
+    const uint64_t i = qsv_insert_zeros(r, a.pos, a.npos) | binbase;
+    if (QSV_IN_BOUNDS(i, a.nrest << a.npos)) acc[0].add(S::term(psi[i]));
+  }
   acc[0].merge(acc[1]);
   acc[2].merge(acc[3]);
   acc[0].merge(acc[2]);
@@ -594,7 +613,10 @@ __global__ void __launch_bounds__(QSV_THREADS)
   for (int j = 0; j < a.m; ++j)
     if ((bin >> j) & 1ull) binbase |= a.binbit[j];
   typename S::Accum acc;
-  for (uint64_t r = 0; r < a.nrest; ++r) acc.add(S::term(psi[qsv_insert_zeros(r, a.pos, a.npos) | binbase]));
+  for (uint64_t r = 0; r < a.nrest; ++r) {
+    const uint64_t i = qsv_insert_zeros(r, a.pos, a.npos) | binbase;
+    if (QSV_IN_BOUNDS(i, a.nrest << a.npos)) acc.add(S::term(psi[i]));
+  }
   out[bin] = acc.value();
 }
 
@@ -644,7 +666,10 @@ __global__ void __launch_bounds__(QSV_THREADS)
     for (int j0 = 0; j0 < 32; j0 += 8) {
       CT<R> v[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = base[(j0 + u) << 8];
+      for (int u = 0; u < 8; ++u)
+        v[u] = QSV_IN_BOUNDS((c << MARG_CHUNK_BITS) + threadIdx.x + ((j0 + u) << 8), nchunks << MARG_CHUNK_BITS)
+                   ? base[(j0 + u) << 8]
+                   : CT<R>{};
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int j = j0 + u;
@@ -741,7 +766,9 @@ __global__ void __launch_bounds__(QSV_THREADS)
              const __grid_constant__ ReduceArgs a) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < a.total_out; j += stride) {
-    CT<R> v = src[qsv_insert_zeros(j, a.pos, a.npos) | a.pattern];
+    const uint64_t i = qsv_insert_zeros(j, a.pos, a.npos) | a.pattern;
+    if (!QSV_IN_BOUNDS(i, a.total_out << a.npos)) continue;
+    CT<R> v = src[i];
     v.x = R((double)v.x * a.scale);
     v.y = R((double)v.y * a.scale);
     dst[j] = v;
@@ -768,6 +795,7 @@ __global__ void __launch_bounds__(QSV_THREADS)
     uint64_t flip = 0;
     for (int j = 0; j < a.n2; ++j)
       if ((f >> (a.n2 - 1 - j)) & 1ull) flip |= 1ull << a.p2[j];
+    if (!QSV_IN_BOUNDS(i ^ flip, a.total)) continue;
     dst[i] = src[i ^ flip];
   }
 }
@@ -1254,6 +1282,37 @@ void release_spares(int device) {
   for (Spare& sp : drop) free_spare(sp);
 }
 }  // namespace
+
+}  // extern "C"
+
+namespace qsv {
+int oob_take_core(unsigned long long* count, unsigned long long* first) {
+#ifdef QSV_BOUNDS_CHECK
+  return qsv_oob_take_unit(count, first);
+#else
+  (void)count;
+  (void)first;
+  return 0;
+#endif
+}
+}  // namespace qsv
+
+extern "C" {
+
+int qsv_bounds_report(unsigned long long* count, unsigned long long* first_index) {
+  if (!count || !first_index) return set_error(nullptr, QSV_ERR_INVALID, "null output");
+  *count = 0;
+  *first_index = 0;
+#ifdef QSV_BOUNDS_CHECK
+  cudaDeviceSynchronize();
+  if (oob_take_core(count, first_index) || oob_take_fused(count, first_index) ||
+      oob_take_adjoint(count, first_index) || oob_take_circuits(count, first_index))
+    return set_error(nullptr, QSV_ERR_CUDA, "reading the bounds words failed");
+  return QSV_OK;
+#else
+  return set_error(nullptr, QSV_ERR_UNSUPPORTED, "not a bounds-checked build (libqsv_checked.so)");
+#endif
+}
 
 int qsv_trim(void) {
   release_spares(-1);

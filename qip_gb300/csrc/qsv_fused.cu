@@ -362,16 +362,18 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         st_lw += a.st_lw[5 + i];
       }
   }
+  [[maybe_unused]] const uint64_t lim = a.ntiles * (uint64_t)P::TILE;  // the state's size
   auto load_tile = [&](uint64_t base) {
     if constexpr (SHUF) {
       const float2* src = psi + base + ld_lw;
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[r] = __ldcs(src + a.ld_reg[r]);
+      for (int r = 0; r < R; ++r)
+        v[r] = QSV_IN_BOUNDS(base + ld_lw + a.ld_reg[r], lim) ? __ldcs(src + a.ld_reg[r]) : make_float2(0.f, 0.f);
     } else if constexpr (STAGED) {
 #pragma unroll
       for (int u = 0; u < P::VEC; ++u) {
         const int e = 2 * (u * FB_THREADS + tid);
-        buf[u] = __ldcs(reinterpret_cast<const float4*>(psi + base + dep(e)));
+        if (QSV_IN_BOUNDS(base + dep(e) + 1, lim)) buf[u] = __ldcs(reinterpret_cast<const float4*>(psi + base + dep(e)));
       }
     } else if (a.vec == 4) {
 #pragma unroll
@@ -381,7 +383,8 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         const int tg = item >> FB_BATCH_BITS;
         const uint64_t rb = base + dep(eb[b]);
 #pragma unroll
-        for (int j = 0; j < 8; j += 4) ld_v8(psi + rb + dep(et[tg * 8 + j]), &buf2[it][j]);
+        for (int j = 0; j < 8; j += 4)
+          if (QSV_IN_BOUNDS(rb + dep(et[tg * 8 + j]) + 3, lim)) ld_v8(psi + rb + dep(et[tg * 8 + j]), &buf2[it][j]);
       }
     } else if (a.vec == 2) {
 #pragma unroll
@@ -392,6 +395,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         const uint64_t rb = base + dep(eb[b]);
 #pragma unroll
         for (int j = 0; j < 8; j += 2) {
+          if (!QSV_IN_BOUNDS(rb + dep(et[tg * 8 + j]) + 1, lim)) continue;
           const float4 v = __ldcs(reinterpret_cast<const float4*>(psi + rb + dep(et[tg * 8 + j])));
           buf2[it][j] = make_float2(v.x, v.y);
           buf2[it][j + 1] = make_float2(v.z, v.w);
@@ -405,7 +409,8 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         const int tg = item >> FB_BATCH_BITS;
         const uint64_t rb = base + dep(eb[b]);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) buf2[it][j] = __ldcs(&psi[rb + dep(et[tg * 8 + j])]);
+        for (int j = 0; j < 8; ++j)
+          if (QSV_IN_BOUNDS(rb + dep(et[tg * 8 + j]), lim)) buf2[it][j] = __ldcs(&psi[rb + dep(et[tg * 8 + j])]);
       }
     }
   };
@@ -556,7 +561,8 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         }
         float2* dst = psi + tbase + st_lw;
   #pragma unroll
-        for (int c = 0; c < CHS; ++c) __stcs(dst + a.st_reg[c], make_float2(re[c], im[c]));
+        for (int c = 0; c < CHS; ++c)
+          if (QSV_IN_BOUNDS(tbase + st_lw + a.st_reg[c], lim)) __stcs(dst + a.st_reg[c], make_float2(re[c], im[c]));
       } else {
         const int q = warp & 3;
         const int h = warp >> 2;
@@ -577,17 +583,20 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
           } else if (a.vec == 4 && CH % 4 == 0) {
             const uint64_t rb = tbase + dep(eb_);
   #pragma unroll
-            for (int j = 0; j < CH; j += 4) st_v8(psi + rb + dep(et[t0 + j]), &re[j], &im[j]);
+            for (int j = 0; j < CH; j += 4)
+              if (QSV_IN_BOUNDS(rb + dep(et[t0 + j]) + 3, lim)) st_v8(psi + rb + dep(et[t0 + j]), &re[j], &im[j]);
           } else if (a.vec >= 2) {
             const uint64_t rb = tbase + dep(eb_);
   #pragma unroll
             for (int j = 0; j < CH; j += 2)
-              __stcs(reinterpret_cast<float4*>(psi + rb + dep(et[t0 + j])),
-                     make_float4(re[j], im[j], re[j + 1], im[j + 1]));
+              if (QSV_IN_BOUNDS(rb + dep(et[t0 + j]) + 1, lim))
+                __stcs(reinterpret_cast<float4*>(psi + rb + dep(et[t0 + j])),
+                       make_float4(re[j], im[j], re[j + 1], im[j + 1]));
           } else {
             const uint64_t rb = tbase + dep(eb_);
   #pragma unroll
-            for (int j = 0; j < CH; ++j) __stcs(&psi[rb + dep(et[t0 + j])], make_float2(re[j], im[j]));
+            for (int j = 0; j < CH; ++j)
+              if (QSV_IN_BOUNDS(rb + dep(et[t0 + j]), lim)) __stcs(&psi[rb + dep(et[t0 + j])], make_float2(re[j], im[j]));
           }
         }
       }
@@ -637,7 +646,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
 #pragma unroll
         for (int u = 0; u < P::VEC; ++u) {
           const int e = 2 * (u * FB_THREADS + tid);
-          __stcs(reinterpret_cast<float4*>(psi + base + dep(e)), raw4[slot(e) >> 1]);
+          if (QSV_IN_BOUNDS(base + dep(e) + 1, lim)) __stcs(reinterpret_cast<float4*>(psi + base + dep(e)), raw4[slot(e) >> 1]);
         }
         __syncthreads();
       }
@@ -1250,6 +1259,18 @@ extern "C" int qsv_apply_blocks(qsv_state* s, int nblocks, const int* ks, const 
   }
   return QSV_OK;
 }
+
+namespace qsv {
+int oob_take_fused(unsigned long long* count, unsigned long long* first) {
+#ifdef QSV_BOUNDS_CHECK
+  return qsv_oob_take_unit(count, first);
+#else
+  (void)count;
+  (void)first;
+  return 0;
+#endif
+}
+}  // namespace qsv
 
 // ---- access-mode autotuning --------------------------------------------------------------
 extern "C" int qsv_set_block_mode(qsv_state* s, int k, int low_mask, int mode) {

@@ -56,6 +56,11 @@ inline void count_launch(unsigned long long k = 1) {
 }
 
 int set_error(qsv_state* s, int code, const char* fmt, ...);
+// Out-of-bounds words of each translation unit (bounds-checked build only).
+int oob_take_core(unsigned long long* count, unsigned long long* first);
+int oob_take_fused(unsigned long long* count, unsigned long long* first);
+int oob_take_adjoint(unsigned long long* count, unsigned long long* first);
+int oob_take_circuits(unsigned long long* count, unsigned long long* first);
 int ensure_scratch(qsv_state* s, size_t bytes);
 int check_launch(qsv_state* s, const char* what);
 unsigned grid_for(const qsv_state* s, uint64_t work, unsigned per_block = QSV_THREADS,
@@ -85,6 +90,34 @@ template <> struct C2T<double> { using type = double2; };
   } while (0)
 
 // ---- device helpers --------------------------------------------------------------
+
+// ---- bounds-checked build ----------------------------------------------------------
+// Built with -DQSV_BOUNDS_CHECK (libqsv_checked.so), kernels test every computed state
+// index against the state's size before the access.  A bad index is counted in this
+// translation unit's device words (the first one kept) and the access is skipped:
+// nothing traps.  qsv_bounds_report reads and clears the words of every unit.  In the
+// normal build QSV_IN_BOUNDS is the constant true and the tests compile away.
+#ifdef QSV_BOUNDS_CHECK
+static __device__ unsigned long long qsv_oob_words[2];  // [0] count, [1] first bad index
+__device__ __forceinline__ bool qsv_in_bounds(unsigned long long idx, unsigned long long limit) {
+  if (idx < limit) return true;
+  if (atomicAdd(&qsv_oob_words[0], 1ull) == 0ull) qsv_oob_words[1] = idx;
+  return false;
+}
+#define QSV_IN_BOUNDS(idx, limit) qsv_in_bounds((unsigned long long)(idx), (unsigned long long)(limit))
+// This unit's words: adds the count to *count, keeps the first index, clears them.
+static inline int qsv_oob_take_unit(unsigned long long* count, unsigned long long* first) {
+  unsigned long long w[2] = {0, 0};
+  if (cudaMemcpyFromSymbol(w, qsv_oob_words, sizeof(w)) != cudaSuccess) return -1;
+  const unsigned long long zero[2] = {0, 0};
+  if (cudaMemcpyToSymbol(qsv_oob_words, zero, sizeof(zero)) != cudaSuccess) return -1;
+  if (w[0] && !*count) *first = w[1];
+  *count += w[0];
+  return 0;
+}
+#else
+#define QSV_IN_BOUNDS(idx, limit) true
+#endif
 
 // Spreads the bits of g over the positions that are NOT in pos[0..npos) (sorted
 // ascending): the inverse of removing those bit positions.

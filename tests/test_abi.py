@@ -62,3 +62,12 @@ def test_state_size_and_dtype_limits_without_a_device():
         assert not h.value
     with pytest.raises(ValueError):
         GpuBackend.make_state(35, [], [], statetype=numpy.complex64)
+
+
+def test_normal_build_is_not_the_bounds_checked_one():
+    """qsv_bounds_report answers only in libqsv_checked.so; the normal build says so
+    without touching a device."""
+    from qip_gb300 import _native
+
+    count, first = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+    assert _native.load().qsv_bounds_report(ctypes.byref(count), ctypes.byref(first)) == _native.QSV_ERR_UNSUPPORTED
