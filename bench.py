@@ -11,7 +11,7 @@ Our arm (default):
              back to host memory; host<->device copies inside the timed region.
   roofline   the fused block kernel: algorithmic bytes per launch (read + write of the
              2^n complex64 state) over its mean CUDA-event launch time.
-  cpu_baseline  the reference's own Cython/OpenMP kernel (cdot_loop) on the machine's cores,
+  cpu_baseline  the reference's own Cython/OpenMP kernel (cdot_loop) on the host's cores,
              a bounded sample of the same gate list at the same n.
 --impl reference: the reference CPU kernel alone, same metric/config, one JSON line.
 

@@ -70,7 +70,7 @@ def test_oracle_measurement_matches_reference():
 
 
 def test_oracle_known_measure_answers():
-    # tests/qiptest.py:296-315 and the survey probe [.1, .2, .3, sqrt(.86)].
+    # tests/qiptest.py:296-315 and a known-answer state [.1, .2, .3, sqrt(.86)].
     v = numpy.array([0.1, 0.2, 0.3, numpy.sqrt(0.86)])
     numpy.testing.assert_allclose(sv.measure_probabilities([0, 1], 2, v), [0.01, 0.09, 0.04, 0.86])
     m, p = sv.measure_top_probabilities([0, 1], 2, 4, v)
