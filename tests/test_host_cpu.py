@@ -368,3 +368,23 @@ def test_decompose_cache_follows_matrix_content():
     numpy.testing.assert_array_equal(a[0].mat, [[0.6, 0.8], [0.8, -0.6]])
     d = gates.decompose({(0, 1): CMat(numpy.array([[0, 1], [1, 0]]))})
     assert d[0].kind == "mono" and d[0].controls == (0,) and d[0].targets == (1,)
+
+
+def test_autotuner_widens_small_blocks_only_where_measured_faster():
+    """Autotuner.place: a 4- or 5-qubit block becomes its 6-qubit form (identity on the
+    added qubits) when the 6-qubit class measured no slower than its own, else it stays;
+    other steps pass through untouched."""
+    n = 20
+    rng = numpy.random.default_rng(12)
+    u4 = numpy.linalg.qr(rng.standard_normal((16, 16)) + 1j * rng.standard_normal((16, 16)))[0]
+    small = fusion.Block((3, 7, 9, 12), u4, 5, 5.0)
+    op = gates.decompose({(1,): numpy.array([[0, 1], [1, 0]])})[0]
+    fast6 = _synthetic_tuner(lambda k, low: 1.0 if k == 6 else 2.0)
+    out = fast6.place(None, n, [small, op])
+    assert len(out[0].qubits) == 6 and set(small.qubits) <= set(out[0].qubits) and out[1] is op
+    v = rng.standard_normal(2 ** n) + 0j
+    numpy.testing.assert_allclose(sv.apply_on(v, n, out[0].qubits, out[0].matrix),
+                                  sv.apply_on(v, n, small.qubits, small.matrix), atol=1e-12)
+    slow6 = _synthetic_tuner(lambda k, low: 3.0 if k == 6 else 1.0)
+    out = slow6.place(None, n, [small, op])
+    assert out[0] is small and out[1] is op
