@@ -137,6 +137,16 @@ def _feed_vector(feed, size: int) -> numpy.ndarray:
 _DTYPES = {numpy.dtype(numpy.complex64): nat.QSV_C64, numpy.dtype(numpy.complex128): nat.QSV_C128}
 
 
+class _DeviceView:
+    """``__cuda_array_interface__`` of a state's device buffer; holds the state."""
+
+    def __init__(self, state: "GpuBackend"):
+        self.state = state
+        typestr = "<c8" if state.statetype == numpy.complex64 else "<c16"
+        self.__cuda_array_interface__ = {"shape": (2 ** state.n,), "typestr": typestr,
+                                         "data": (state.device_ptr(), False), "version": 2}
+
+
 class GpuBackend(StateType):
     """GB300 state vector behind the ``StateType`` interface.
 
@@ -224,6 +234,19 @@ class GpuBackend(StateType):
 
     def device_ptr(self) -> int:
         return int(self._lib.qsv_device_ptr(self._h))
+
+    def device_state(self):
+        """The state as a torch tensor over its device buffer (no copy), with every queued
+        gate applied: for callers that keep working on the GPU, this skips the host
+        readback of ``get_state``.  Writes through it change the state.  The view keeps
+        this object alive; it is invalid after ``close()`` or a call that resizes the
+        state (``reduce_measure``).  Use it after this call returns (the state's stream is
+        synchronised) or order work with ``set_stream``."""
+        import torch
+
+        self.flush()
+        self._check(self._lib.qsv_synchronize(self._h), "synchronize")
+        return torch.as_tensor(_DeviceView(self), device="cuda")
 
     def set_stream(self, stream_ptr: int) -> None:
         self.flush()

@@ -67,3 +67,25 @@ def test_parked_state_buffers_start_clean():
     st = GpuBackend.make_state(n, [], [], statetype=numpy.complex128)
     assert numpy.array_equal(st.get_state(), e0.astype(numpy.complex128))
     st.close()
+
+
+@pytest.mark.parametrize("statetype", [numpy.complex64, numpy.complex128])
+def test_device_state_is_a_view_of_the_state(statetype):
+    """device_state(): a torch tensor over the device buffer with queued gates applied;
+    it reads what get_state reads and writes through to the state."""
+    import torch
+
+    n = 16
+    h = numpy.array([[1, 1], [1, -1]]) / numpy.sqrt(2)
+    st = GpuBackend.make_state(n, [], [], statetype=statetype, fusion=statetype == numpy.complex64)
+    for q in range(n):
+        st.kronselect_dot({q: h})
+    t = st.device_state()
+    assert t.is_cuda and t.dtype == (torch.complex64 if statetype == numpy.complex64 else torch.complex128)
+    assert t.shape == (2 ** n,) and t.data_ptr() == st.device_ptr()
+    numpy.testing.assert_allclose(t.cpu().numpy(), st.get_state(), atol=1e-7)
+    t.mul_(2.0)
+    torch.cuda.synchronize()
+    assert st.total_prob() == pytest.approx(4.0, rel=1e-5)
+    del t
+    st.close()
