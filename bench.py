@@ -363,12 +363,18 @@ def run_ours(args):
     st.close()
     torch.cuda.synchronize()
 
-    # e2e through the plugin (StateType calls with host buffers).
+    # e2e through the plugin (StateType calls with host buffers).  Every step submits the
+    # same circuit structure, so from the second circuit on the stream replays the
+    # whole-circuit plan kept after the first (qip_gb300.plancache); the blocks per step
+    # are reported.
+    e2e_stats = {}
+
     def e2e_step():
         s2 = GpuBackend.make_state(n, [], [], statetype=numpy.complex64, fusion=True, max_block=kmax)
         for g in gl:
             s2.kronselect_dot(g)
         out = s2.get_state()
+        e2e_stats.update(s2.stats)
         s2.close()
         return out
 
@@ -425,6 +431,7 @@ def run_ours(args):
                      "peak_source": f"{peak_src} hbm_gbs"},
         "e2e": {"value": ws * amp_updates / t_e2e, "unit": "amp-updates/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "seconds_per_step": t_e2e, "steps": e2e_steps,
+                "blocks_per_step": e2e_stats.get("blocks"), "replayed_steps": e2e_stats.get("replayed_steps"),
                 "clocks": clk_e2e.summary()},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),

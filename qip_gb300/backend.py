@@ -22,8 +22,9 @@ import numpy
 from . import _native as nat
 from . import hostbuf
 from .autotune import default_tuner
-from .fusion import Block, plan, plan_prefix, widen_blocks
+from .fusion import Block, emit_native, plan, plan_prefix, widen_blocks
 from .gates import GateOp, classify_matrix, decompose
+from .plancache import PlanCache, default_cache, step_hash
 from .util import InitialState, IndexType, MatrixType
 
 
@@ -181,7 +182,16 @@ class GpuBackend(StateType):
         self._pending: List[GateOp] = []
         self._window = self.PARTIAL_FLUSH_FIRST
         self._next_partial = self._window
-        self.stats = {"ops": 0, "blocks": 0, "block_gates": 0, "launch_calls": 0}
+        # This circuit's fused gates since the last full flush and the rolling hash of
+        # their structure; a kept whole-circuit plan being replayed (qip_gb300.plancache).
+        self._trace: List[GateOp] = []
+        self._trace_hash = 0
+        self._replay = None
+        self._replay_next = 0
+        self._replay_done: set = set()
+        self._replay_emitted: List[bool] = []
+        self._replay_tried = False
+        self.stats = {"ops": 0, "blocks": 0, "block_gates": 0, "launch_calls": 0, "replayed_steps": 0}
 
     # ---- construction ---------------------------------------------------------------
     @staticmethod
@@ -276,14 +286,102 @@ class GpuBackend(StateType):
             if not finite:
                 raise ValueError("matrix on qubits {} has non-finite entries".format(sorted(op.qubits)))
         if self.fusion:
-            self._pending.extend(ops)
-            if len(self._pending) >= self.FLUSH_LIMIT:
-                self.flush()
-            elif len(self._pending) >= self._next_partial:
-                self._partial_flush()
+            self._queue(ops)
         else:
             for op in ops:
                 self.apply_op(op)
+
+    REPLAY_CHECK = 16  # gates between looks for replayable steps
+    TRACE_MAX = 16384  # longer circuits are streamed without keeping their structure
+
+    def _queue(self, ops: Sequence[GateOp]) -> None:
+        """Queue gates of the fused path: while the circuit's structure matches a kept
+        whole-circuit plan, emit its steps as their gates arrive; otherwise plan the
+        stream window by window."""
+        if not ops:
+            return
+        if self._trace_hash is not None and len(self._trace) + len(ops) <= self.TRACE_MAX:
+            for op in ops:
+                self._trace.append(op)
+                self._trace_hash = step_hash(self._trace_hash, op.qmask, op.amp_update_weight())
+        elif self._trace_hash is not None:
+            # Too long to keep: streamed as usual from here on, no plan kept.
+            if self._replay is not None:
+                self._replay_abandon()
+            self._trace_hash = None
+        if self._replay is not None:
+            if len(self._trace) % self.REPLAY_CHECK < len(ops) or len(self._trace) >= self._replay.length:
+                self._replay_step()
+            return
+        self._pending.extend(ops)
+        if len(self._pending) >= self.FLUSH_LIMIT:
+            self._flush_pending()
+        elif len(self._pending) >= self._next_partial:
+            if not self._replay_tried and self._trace_hash is not None and len(self._pending) == len(self._trace):
+                # First decision of this circuit: replay a kept plan of its structure.
+                self._replay_tried = True
+                self._tune_width()
+                entry = default_cache().find(self._kmax(), len(self._trace), self._trace_hash)
+                if entry is not None:
+                    self._replay, self._replay_next, self._pending = entry, 0, []
+                    self._replay_emitted = [False] * len(entry.steps)
+                    self._replay_step()
+                    return
+            self._partial_flush()
+
+    def _replay_step(self, final: bool = False) -> None:
+        """Emit the kept plan's steps whose gates have all arrived (``final``: the circuit
+        is complete), or leave the replay when the structure no longer matches.
+
+        A ready step goes ahead of earlier steps still waiting for gates when it shares no
+        qubit with any of them: the steps it passes commute with it, and every gate
+        before one of its gates on a shared qubit is already emitted (the plan's order is
+        a dependency order), so the emitted gates stay closed under dependencies."""
+        e, n = self._replay, len(self._trace)
+        if n > e.length or e.prefix[n] != self._trace_hash or (final and n != e.length):
+            self._replay_abandon()
+            return
+        groups, blocked, mismatch = [], 0, False
+        emitted = self._replay_emitted
+        k = self._replay_next
+        while k < len(e.steps) and blocked != e.all_qubits:
+            if not emitted[k]:
+                if e.last[k] < n and not e.step_mask[k] & blocked:
+                    idx = e.steps[k]
+                    if any(self._trace[i].qmask != e.masks[i] for i in idx):
+                        mismatch = True
+                        break
+                    groups.append([self._trace[i] for i in idx])
+                    self._replay_done.update(idx)
+                    emitted[k] = True
+                else:
+                    blocked |= e.step_mask[k]
+            k += 1
+        while self._replay_next < len(e.steps) and emitted[self._replay_next]:
+            self._replay_next += 1
+        if groups:
+            self.stats["replayed_steps"] += len(groups)
+            self.run_plan(emit_native(groups))
+        if mismatch:
+            self._replay_abandon()
+
+    def _replay_abandon(self) -> None:
+        """The stream left the kept structure: the gates not emitted yet go on, in program
+        order, through the ordinary stream planning."""
+        self._pending = [op for i, op in enumerate(self._trace) if i not in self._replay_done]
+        self._replay = None
+        self._window = self.PARTIAL_FLUSH
+        self._next_partial = len(self._pending) + self._window // 3
+
+    def _end_circuit(self, replayed: bool) -> None:
+        """After a full flush: keep a plan of this circuit's structure for later streams
+        (planned in the background) unless it was replayed from one, and start a new
+        trace."""
+        if not replayed and self._trace_hash is not None and len(self._trace) >= PlanCache.MIN_GATES:
+            default_cache().plan_in_background(self._kmax(), [op.qmask for op in self._trace],
+                                               [op.amp_update_weight() for op in self._trace], self._trace_hash)
+        self._trace, self._trace_hash = [], 0
+        self._replay, self._replay_next, self._replay_done, self._replay_tried = None, 0, set(), False
 
     def _kmax(self) -> int:
         if self.autotune:
@@ -316,9 +414,7 @@ class GpuBackend(StateType):
     def apply_ops(self, ops: Sequence[GateOp]) -> None:
         """Queue (fusion) or launch (per-gate) pre-decomposed operations."""
         if self.fusion:
-            self._pending.extend(ops)
-            if len(self._pending) >= self.FLUSH_LIMIT:
-                self.flush()
+            self._queue(ops)
         else:
             for op in ops:
                 self.apply_op(op)
@@ -406,7 +502,16 @@ class GpuBackend(StateType):
         self.apply_blocks(batch)
 
     def flush(self) -> None:
-        """Fuse and launch every queued gate."""
+        """Fuse and launch every queued gate; the circuit so far ends here."""
+        replayed = self._replay is not None
+        if replayed:
+            self._replay_step(final=True)
+            replayed = self._replay is not None
+            self._replay = None
+        self._flush_pending()
+        self._end_circuit(replayed)
+
+    def _flush_pending(self) -> None:
         if not self._pending:
             return
         tuned = self._tune_width()
@@ -570,7 +675,7 @@ class GpuBackend(StateType):
         process (``qsv_destroy``)."""
         h, self._h = getattr(self, "_h", None), None
         if h:
-            self._pending = []
+            self._pending, self._trace, self._replay = [], [], None
             self._lib.qsv_destroy(h)
 
     @staticmethod

@@ -90,28 +90,39 @@ def plan(gates: Sequence[GateOp], kmax: int = 6, lookahead: int = LOOKAHEAD,
     return steps
 
 
+def plan_indices(qmasks: Sequence[int], weights: Sequence[float], kmax: int = 6, nqubits=None,
+                 lookahead: int = LOOKAHEAD, strict: bool = True, min_pending: int = 0,
+                 lookahead2: int = LOOKAHEAD2, beam: Tuple[int, int] = BEAM) -> Tuple[List[List[int]], int]:
+    """The native planner on the gates' structure alone (qubit masks and amp-update
+    weights, no matrices): (steps as lists of gate indices, number of gates planned)."""
+    from . import _native as nat
+
+    ng = len(qmasks)
+    if ng == 0:
+        return [], 0
+    qm = numpy.array([int(m) for m in qmasks], dtype=numpy.uint64)
+    w = numpy.ascontiguousarray(weights, dtype=numpy.float64)
+    order = numpy.empty(ng, dtype=numpy.int32)
+    starts = numpy.empty(ng + 1, dtype=numpy.int32)
+    nsteps, nplanned = ctypes.c_int(), ctypes.c_int()
+    nat.check(nat.load().qsv_fusion_plan(ng, qm.ctypes.data_as(ctypes.c_void_p), nat.dp(w), int(kmax),
+                                         int(lookahead), int(lookahead2), int(beam[0]), int(beam[1]),
+                                         -1 if nqubits is None else int(nqubits), int(bool(strict)),
+                                         int(min_pending), nat.ip(order), nat.ip(starts), ctypes.byref(nsteps),
+                                         ctypes.byref(nplanned)), None, "fusion_plan")
+    return [order[starts[k]:starts[k + 1]].tolist() for k in range(nsteps.value)], nplanned.value
+
+
 def plan_prefix(gates: Sequence[GateOp], kmax: int = 6, nqubits=None, lookahead: int = LOOKAHEAD,
                 strict: bool = True, min_pending: int = 0,
                 lookahead2: int = LOOKAHEAD2, beam: Tuple[int, int] = BEAM) -> Tuple[List[Step], List[GateOp]]:
     """``plan_prefix_py`` in native code: same steps, same matrices (to rounding)."""
-    from . import _native as nat
-
-    lib = nat.load()
-    ng = len(gates)
-    if ng == 0:
+    if not gates:
         return [], []
-    qm = numpy.array([g.qmask for g in gates], dtype=numpy.uint64)
-    w = numpy.array([g.amp_update_weight() for g in gates], dtype=numpy.float64)
-    order = numpy.empty(ng, dtype=numpy.int32)
-    starts = numpy.empty(ng + 1, dtype=numpy.int32)
-    nsteps, nplanned = ctypes.c_int(), ctypes.c_int()
-    nat.check(lib.qsv_fusion_plan(ng, qm.ctypes.data_as(ctypes.c_void_p), nat.dp(w), int(kmax), int(lookahead),
-                                  int(lookahead2), int(beam[0]), int(beam[1]),
-                                  -1 if nqubits is None else int(nqubits), int(bool(strict)), int(min_pending),
-                                  nat.ip(order),
-                                  nat.ip(starts), ctypes.byref(nsteps), ctypes.byref(nplanned)), None, "fusion_plan")
-    groups = [[gates[i] for i in order[starts[k]:starts[k + 1]]] for k in range(nsteps.value)]
-    planned = set(order[:nplanned.value].tolist())
+    idx, nplanned = plan_indices([g.qmask for g in gates], [g.amp_update_weight() for g in gates], kmax, nqubits,
+                                 lookahead, strict, min_pending, lookahead2, beam)
+    groups = [[gates[i] for i in step] for step in idx]
+    planned = {i for step in idx for i in step}
     rest = [g for i, g in enumerate(gates) if i not in planned]
     return emit_native(groups), rest
 
