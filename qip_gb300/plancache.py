@@ -21,6 +21,7 @@ through the ordinary stream planning and the result is the same operator.
 """
 from __future__ import annotations
 
+import os
 import struct
 import threading
 from typing import Dict, List, Optional, Sequence, Tuple
@@ -106,7 +107,7 @@ class PlanCache:
         from .fusion import BEAM_WIDE, plan_indices
 
         key = (kmax, len(masks), h)
-        if len(masks) < self.MIN_GATES or self.has(kmax, len(masks), h):
+        if self.capacity <= 0 or len(masks) < self.MIN_GATES or self.has(kmax, len(masks), h):
             return
         with self._lock:
             if key in self._busy:
@@ -140,8 +141,13 @@ class PlanCache:
             self._entries = []
 
 
-_DEFAULT = PlanCache()
+_DEFAULT: Optional[PlanCache] = None
 
 
 def default_cache() -> PlanCache:
+    """The process's plan cache; ``QSV_PLAN_CACHE=0`` in the environment keeps no plans
+    (every circuit is planned window by window, no background thread)."""
+    global _DEFAULT
+    if _DEFAULT is None:
+        _DEFAULT = PlanCache(capacity=0 if os.environ.get("QSV_PLAN_CACHE", "1") == "0" else 8)
     return _DEFAULT

@@ -138,3 +138,11 @@ def test_long_streams_are_not_kept(monkeypatch):
     _run(n, circuits.brickwork(n, 40, seed=1), cache, monkeypatch, v)
     cache.wait()
     assert cache._entries == []
+
+
+def test_disabled_cache_keeps_nothing():
+    cache = PlanCache(capacity=0)
+    ops, masks, weights = _structure(circuits.brickwork(10, 16, seed=5))
+    cache.plan_in_background(6, masks, weights, 7)
+    cache.wait()
+    assert cache.find(6, len(masks), 7) is None and cache._busy == {}
