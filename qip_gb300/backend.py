@@ -211,23 +211,29 @@ class GpuBackend(StateType):
         dt = numpy.dtype(statetype)
         if dt not in _DTYPES:
             raise ValueError("statetype must be numpy.complex64 or numpy.complex128, not {}".format(statetype))
+        # Feeds are checked on the host before any device memory is taken.
+        product = GpuBackend._product_args(index_groups, feed_list) if len(feed_list) > 0 else None
         lib = nat.load()
         h = ctypes.c_void_p()
         nat.check(lib.qsv_create(int(n), _DTYPES[dt], ctypes.byref(h)), None, "qsv_create")
         if fusion is None:
             fusion = dt == numpy.dtype(numpy.complex64)
         st = GpuBackend(n, h, dt, fusion, max_block, autotune)
-        if len(feed_list) > 0:
-            st._set_product(index_groups, feed_list)
+        if product is not None:
+            st._set_product(*product)
         return st
 
-    def _set_product(self, index_groups, feed_list) -> None:
+    @staticmethod
+    def _product_args(index_groups, feed_list):
         sizes, qubits, vecs = [], [], []
         for group, feed in zip(index_groups, feed_list):
             g = [int(q) for q in group]
             sizes.append(len(g))
             qubits.extend(g)
             vecs.append(_feed_vector(feed, 2 ** len(g)))
+        return sizes, qubits, vecs
+
+    def _set_product(self, sizes, qubits, vecs) -> None:
         sz = nat.int_array(sizes)
         qb = nat.int_array(qubits)
         feeds = numpy.ascontiguousarray(numpy.concatenate(vecs)).view(numpy.float64)
@@ -549,7 +555,7 @@ class GpuBackend(StateType):
             raise ValueError("data length does not match the range")
         self._check(self._lib.qsv_write_range(self._h, d.ctypes.data_as(ctypes.c_void_p), int(start), d.shape[0]),
                     "overwrite_relative_range")
-        self._lib.qsv_synchronize(self._h)
+        self._check(self._lib.qsv_synchronize(self._h), "overwrite_relative_range")
 
     def addto_relative_range(self, start: int, end: int, data: Sequence[complex]):
         self.flush()
@@ -558,7 +564,7 @@ class GpuBackend(StateType):
             raise ValueError("data length does not match the range")
         self._check(self._lib.qsv_add_range(self._h, d.ctypes.data_as(ctypes.c_void_p), int(start), d.shape[0]),
                     "addto_relative_range")
-        self._lib.qsv_synchronize(self._h)
+        self._check(self._lib.qsv_synchronize(self._h), "addto_relative_range")
 
     # ---- probabilities and measurement ----------------------------------------------------
     def _probs(self, qubits: Sequence[int]) -> numpy.ndarray:

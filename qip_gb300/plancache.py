@@ -109,9 +109,6 @@ class PlanCache:
         key = (kmax, len(masks), h)
         if self.capacity <= 0 or len(masks) < self.MIN_GATES or self.has(kmax, len(masks), h):
             return
-        with self._lock:
-            if key in self._busy:
-                return
         masks, weights = list(masks), list(weights)
 
         def work():
@@ -124,7 +121,9 @@ class PlanCache:
                     self._busy.pop(key, None)
 
         t = threading.Thread(target=work, daemon=True)
-        with self._lock:
+        with self._lock:  # one planner per structure: the check and the claim are one step
+            if key in self._busy:
+                return
             self._busy[key] = t
         t.start()
 

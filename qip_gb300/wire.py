@@ -505,18 +505,9 @@ class WireWorker:
         self.job_id = job_id
         groups = [pbindices_to_indices(s.indices if s.indices is not None else Indices()) for s in setup.states]
         # An index feed is the basis vector it names (messages.proto: "all zeros except
-        # this index"); the reference's worker hands the bare int to a backend that takes
-        # vectors only.
-        feeds = []
-        for grp, s in zip(groups, setup.states):
-            v = get_state_value(s)
-            if not isinstance(v, numpy.ndarray):
-                if not 0 <= v < (1 << len(grp)):
-                    raise ValueError("index feed {} out of range for {} qubits".format(v, len(grp)))
-                e = numpy.zeros(1 << len(grp), dtype=numpy.complex128)
-                e[v] = 1.0
-                v = e
-            feeds.append(v)
+        # this index"), as GpuBackend.make_state reads an int feed; the reference's worker
+        # hands the bare int to a backend that takes vectors only.
+        feeds = [get_state_value(s) for s in setup.states]
         self.state = GpuBackend.make_state(setup.n, groups, feeds, **backend_kw)
         self.closed = False
 

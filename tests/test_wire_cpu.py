@@ -137,5 +137,5 @@ def test_worker_refuses_a_slice_of_a_distributed_state():
     setup = wire.WorkerSetup(n=10, state_index_start=0, state_index_end=512, state_handle="s")
     with pytest.raises(ValueError, match="whole state"):
         wire.WireWorker(setup)
-    with pytest.raises(ValueError, match="index feed"):
+    with pytest.raises(ValueError, match="basis-state feed"):
         wire.WireWorker(wire.StateSetup(n=4, states=[wire.State(indices=wire.Indices(index=[0]), index=2)]))
