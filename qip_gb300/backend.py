@@ -171,7 +171,7 @@ class GpuBackend(StateType):
     AUTOTUNE_MIN_GATES = 64
 
     def __init__(self, n: int, handle: ctypes.c_void_p, statetype, fusion: bool, max_block: int = 6,
-                 autotune: bool = True):
+                 autotune: bool = True, keep_plans: bool = True):
         super().__init__(n, None)
         self._h = handle
         self._lib = nat.load()
@@ -179,6 +179,7 @@ class GpuBackend(StateType):
         self.fusion = bool(fusion)
         self.max_block = int(max_block)
         self.autotune = bool(autotune)
+        self.keep_plans = bool(keep_plans)
         self._pending: List[GateOp] = []
         self._window = self.PARTIAL_FLUSH_FIRST
         self._next_partial = self._window
@@ -199,11 +200,13 @@ class GpuBackend(StateType):
                    inputstartindex: Optional[int] = None, inputendindex: Optional[int] = None,
                    outputstartindex: Optional[int] = None, outputendindex: Optional[int] = None,
                    statetype: type = numpy.complex128, fusion: Optional[bool] = None,
-                   max_block: int = 6, autotune: bool = True) -> "GpuBackend":
+                   max_block: int = 6, autotune: bool = True, keep_plans: bool = True) -> "GpuBackend":
         """Same contract as ``CythonBackend.make_state`` (``qip/backend.py:73-104``): the
         product of the fed register vectors at their global indices, unfed qubits |0>,
         |0...0> without feeds, no normalisation.  ``autotune`` (fusion only): measure the
-        fusion width and the block kernel's access modes (``qip_gb300.autotune``)."""
+        fusion width and the block kernel's access modes (``qip_gb300.autotune``).
+        ``keep_plans`` (fusion only): replay whole-circuit plans kept from earlier
+        circuits of the same structure, and keep this one's (``qip_gb300.plancache``)."""
         full = 2 ** n
         for lo, hi in ((inputstartindex, inputendindex), (outputstartindex, outputendindex)):
             if (lo not in (None, 0)) or (hi not in (None, full)):
@@ -218,7 +221,7 @@ class GpuBackend(StateType):
         nat.check(lib.qsv_create(int(n), _DTYPES[dt], ctypes.byref(h)), None, "qsv_create")
         if fusion is None:
             fusion = dt == numpy.dtype(numpy.complex64)
-        st = GpuBackend(n, h, dt, fusion, max_block, autotune)
+        st = GpuBackend(n, h, dt, fusion, max_block, autotune, keep_plans)
         if product is not None:
             st._set_product(*product)
         return st
@@ -323,7 +326,8 @@ class GpuBackend(StateType):
         if len(self._pending) >= self.FLUSH_LIMIT:
             self._flush_pending()
         elif len(self._pending) >= self._next_partial:
-            if not self._replay_tried and self._trace_hash is not None and len(self._pending) == len(self._trace):
+            if (self.keep_plans and not self._replay_tried and self._trace_hash is not None
+                    and len(self._pending) == len(self._trace)):
                 # First decision of this circuit: replay a kept plan of its structure.
                 self._replay_tried = True
                 self._tune_width()
@@ -383,7 +387,8 @@ class GpuBackend(StateType):
         """After a full flush: keep a plan of this circuit's structure for later streams
         (planned in the background) unless it was replayed from one, and start a new
         trace."""
-        if not replayed and self._trace_hash is not None and len(self._trace) >= PlanCache.MIN_GATES:
+        if (self.keep_plans and not replayed and self._trace_hash is not None
+                and len(self._trace) >= PlanCache.MIN_GATES):
             default_cache().plan_in_background(self._kmax(), [op.qmask for op in self._trace],
                                                [op.amp_update_weight() for op in self._trace], self._trace_hash)
         self._trace, self._trace_hash = [], 0

@@ -65,8 +65,8 @@ def test_background_plan_is_the_whole_circuit_plan():
 class _OracleBackend(GpuBackend):
     """The backend's host logic with the device replaced by the oracle."""
 
-    def __init__(self, n, v):
-        GpuBackend.__init__(self, n, None, numpy.complex64, fusion=True, autotune=False)
+    def __init__(self, n, v, keep_plans=True):
+        GpuBackend.__init__(self, n, None, numpy.complex64, fusion=True, autotune=False, keep_plans=keep_plans)
         self.v = v.copy()
 
     def run_plan(self, steps):
@@ -80,9 +80,9 @@ class _OracleBackend(GpuBackend):
                 self.stats["ops"] += 1
 
 
-def _run(n, gl, cache, monkeypatch, v):
+def _run(n, gl, cache, monkeypatch, v, keep_plans=True):
     monkeypatch.setattr(backend_mod, "default_cache", lambda: cache)
-    b = _OracleBackend(n, v)
+    b = _OracleBackend(n, v, keep_plans)
     for g in gl:
         b.kronselect_dot(g)
     b.flush()
@@ -146,3 +146,17 @@ def test_disabled_cache_keeps_nothing():
     cache.plan_in_background(6, masks, weights, 7)
     cache.wait()
     assert cache.find(6, len(masks), 7) is None and cache._busy == {}
+
+
+def test_states_that_keep_no_plans_neither_replay_nor_keep(monkeypatch):
+    n = 12
+    cache = PlanCache()
+    v = numpy.random.default_rng(8).standard_normal(2 ** n) + 0j
+    gl = circuits.brickwork(n, 24, seed=1)
+    _run(n, gl, cache, monkeypatch, v, keep_plans=False)
+    cache.wait()
+    assert cache._entries == []
+    _run(n, gl, cache, monkeypatch, v)
+    cache.wait()
+    b = _run(n, _new_matrices(gl, 5), cache, monkeypatch, v, keep_plans=False)
+    assert b.stats["replayed_steps"] == 0 and len(cache._entries) == 1
