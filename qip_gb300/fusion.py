@@ -13,8 +13,10 @@ front gate implies (brickwork n=28, depth 40: 69 steps instead of 120 with a sta
 the front only and no second-level score).  A beam search over rounds (``BEAM``: 16
 states kept per level, 8 candidates offered per state) plans whole lists: 64 steps for
 that circuit (62 with ``BEAM_WIDE``, 64 states, used where a circuit is planned once
-ahead of its runs).  Streams (gates planned while more keep arriving) use the rounds: each
-call re-plans a window of pending gates, and there a beam gains nothing.  Gates wider than
+ahead of its runs, and for the whole-circuit plans that ``qip_gb300.plancache`` keeps
+by circuit structure).  Streams (gates planned while more keep arriving) use the rounds:
+each call re-plans a window of pending gates, and there a beam gains nothing; a stream
+whose structure has a kept plan replays that plan instead.  Gates wider than
 ``kmax`` are never fused; they run on the per-gate kernels when they reach the front
 of the queue.
 

@@ -482,11 +482,15 @@ class WireWorker:
     ``setup`` is a ``StateSetup`` or a ``WorkerSetup`` (or its bytes) covering the whole
     state; a ``WorkerSetup`` that gives this worker a slice of a distributed state is
     refused with ``ValueError``, since the slice exchange is the reference's multi-node
-    control plane.  ``backend_kw`` goes to ``GpuBackend.make_state`` (``statetype``,
-    ``fusion``, ...)."""
+    control plane.  ``backend_constructor`` builds the state, as ``run()``'s argument of
+    that name does (default ``GpuBackend.make_state``); ``backend_kw`` goes to it
+    (``statetype``, ``fusion``, ...)."""
 
-    def __init__(self, setup, job_id: str = "", **backend_kw):
-        from .backend import GpuBackend
+    def __init__(self, setup, job_id: str = "", backend_constructor=None, **backend_kw):
+        if backend_constructor is None:
+            from .backend import GpuBackend
+
+            backend_constructor = GpuBackend.make_state
 
         if isinstance(setup, (bytes, bytearray, memoryview)):
             setup = StateSetup.FromString(bytes(setup))
@@ -508,7 +512,7 @@ class WireWorker:
         # this index"), as GpuBackend.make_state reads an int feed; the reference's worker
         # hands the bare int to a backend that takes vectors only.
         feeds = [get_state_value(s) for s in setup.states]
-        self.state = GpuBackend.make_state(setup.n, groups, feeds, **backend_kw)
+        self.state = backend_constructor(setup.n, groups, feeds, **backend_kw)
         self.closed = False
 
     def handle(self, operation) -> Optional[WorkerConfirm]:

@@ -139,3 +139,54 @@ def test_worker_refuses_a_slice_of_a_distributed_state():
         wire.WireWorker(setup)
     with pytest.raises(ValueError, match="basis-state feed"):
         wire.WireWorker(wire.StateSetup(n=4, states=[wire.State(indices=wire.Indices(index=[0]), index=2)]))
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_worker_session_dispatch_on_the_oracle(cases, n):
+    """Every branch of the worker's dispatch (the GPU runs the same session in
+    test_gpu_wire.py), driven by the reference's messages with the oracle as backend."""
+    d, meta = cases
+    p = "n{}_".format(n)
+    m = meta[str(n)]
+    w = wire.WireWorker(bytes(d[p + "setup"]), job_id=m["job"], backend_constructor=sv.OracleBackend.make_state)
+    done = wire.WorkerConfirm(job_id=m["job"]).SerializeToString()
+    for raw in _msgs(d, p + "ops"):
+        assert w.handle_bytes(raw) == done
+    numpy.testing.assert_allclose(w.state.get_state(), d[p + "final"], atol=1e-12)
+    top_op, meas_op = _msgs(d, p + "mops")
+    top = wire.WorkerConfirm.FromString(w.handle_bytes(top_op))
+    numpy.testing.assert_allclose(top.measure_result.top_k_probs, m["top_k"][1], atol=1e-12)
+    assert top.measure_result.top_k_indices.index == m["top_k"][0]
+    meas = wire.WorkerConfirm.FromString(w.handle_bytes(meas_op))
+    assert meas.measure_result.measured_bits == m["measured"][0]
+    assert abs(meas.measure_result.measured_prob - m["measured"][1]) < 1e-12
+    numpy.testing.assert_allclose(w.state.get_state(), d[p + "after_measure"], atol=1e-12)
+
+    # Soft measurement of a given outcome: its marginal, state unchanged.
+    before = numpy.array(w.state.get_state())
+    want = sv.measure_probabilities([1], n, before)[1]
+    soft = wire.WorkerOperation(job_id="q", measure=wire.Measure(indices=wire.indices_to_pbindices([1]), soft=True,
+                                                                 measure_result=wire.MeasureResult(measured_bits=1)))
+    r = wire.WorkerConfirm.FromString(w.handle_bytes(soft.SerializeToString()))
+    assert r.job_id == "q" and r.measure_result.measured_bits == 1
+    assert abs(r.measure_result.measured_prob - want) < 1e-12
+    numpy.testing.assert_array_equal(w.state.get_state(), before)
+    # Reduce with a given outcome and probability: the state loses that qubit.
+    p0 = sv.measure_probabilities([1], n, before)[0]
+    red = wire.WorkerOperation(job_id="r", measure=wire.Measure(
+        indices=wire.indices_to_pbindices([1]), reduce=True,
+        measure_result=wire.MeasureResult(measured_bits=0, measured_prob=float(p0))))
+    r = wire.WorkerConfirm.FromString(w.handle_bytes(red.SerializeToString()))
+    assert r.measure_result.measured_bits == 0 and abs(r.measure_result.measured_prob - p0) < 1e-15
+    assert w.state.get_state_size() == 2 ** (n - 1)
+    numpy.testing.assert_allclose(w.state.get_state(), sv.reduce_measure([1], n, before, 0, p0), atol=1e-12)
+    tp = wire.WorkerConfirm.FromString(w.handle_bytes(wire.WorkerOperation(job_id="t", total_prob=True)
+                                                      .SerializeToString()))
+    assert abs(tp.measure_result.measured_prob - 1.0) < 1e-12
+    assert w.handle_bytes(wire.WorkerOperation(job_id="s", sync=wire.Sync(set_up_to=4)).SerializeToString()) == \
+        wire.WorkerConfirm(job_id="s").SerializeToString()
+    with pytest.raises(ValueError, match="unknown operation"):
+        w.handle(wire.WorkerOperation(job_id="x"))
+    assert w.handle_bytes(wire.WorkerOperation(close=True).SerializeToString()) == b""
+    with pytest.raises(ValueError, match="closed"):
+        w.handle(wire.WorkerOperation(total_prob=True))
