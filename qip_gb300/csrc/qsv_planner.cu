@@ -300,15 +300,58 @@ namespace {
 // U <- G U for a gate on block bit positions bits[0..q) (bits[0] = MSB of the gate index).
 void embed(int k, double* U, int q, const int* bits, const double* G) {
   const int dim = 1 << k, gd = 1 << q;
-  std::vector<int> off((size_t)gd);
   int mask = 0;
+  for (int b = 0; b < q; ++b) mask |= 1 << bits[b];
+  // Diagonal gate (every off-diagonal entry exactly zero): row r of U is scaled by the
+  // gate's diagonal entry at the gate index of r's bits; unit entries leave rows as
+  // they are.  Same products as the general loop, without the zero terms.
+  bool diagonal = true;
+  for (int i = 0; i < gd && diagonal; ++i)
+    for (int j = 0; j < gd; ++j)
+      if (i != j && (G[2 * ((size_t)i * gd + j)] != 0.0 || G[2 * ((size_t)i * gd + j) + 1] != 0.0)) {
+        diagonal = false;
+        break;
+      }
+  if (diagonal) {
+    for (int r = 0; r < dim; ++r) {
+      int j = 0;
+      for (int b = 0; b < q; ++b) j |= ((r >> bits[b]) & 1) << (q - 1 - b);
+      const double pr = G[2 * ((size_t)j * gd + j)], pi = G[2 * ((size_t)j * gd + j) + 1];
+      if (pr == 1.0 && pi == 0.0) continue;
+      double* row = U + 2 * (size_t)r * dim;
+      for (int c = 0; c < dim; ++c) {
+        const double x = row[2 * c], y = row[2 * c + 1];
+        row[2 * c] = pr * x - pi * y;
+        row[2 * c + 1] = pr * y + pi * x;
+      }
+    }
+    return;
+  }
+  // One qubit: rows r0 (bit clear) and r1 (bit set) combine, column by column.
+  if (q == 1) {
+    const int bm = 1 << bits[0];
+    const double a0 = G[0], a1 = G[1], b0 = G[2], b1 = G[3], c0 = G[4], c1 = G[5], d0 = G[6], d1 = G[7];
+    for (int r0 = 0; r0 < dim; ++r0) {
+      if (r0 & bm) continue;
+      double* x = U + 2 * (size_t)r0 * dim;
+      double* y = U + 2 * (size_t)(r0 | bm) * dim;
+      for (int c = 0; c < dim; ++c) {
+        const double xr = x[2 * c], xi = x[2 * c + 1], yr = y[2 * c], yi = y[2 * c + 1];
+        x[2 * c] = (a0 * xr - a1 * xi) + (b0 * yr - b1 * yi);
+        x[2 * c + 1] = (a0 * xi + a1 * xr) + (b0 * yi + b1 * yr);
+        y[2 * c] = (c0 * xr - c1 * xi) + (d0 * yr - d1 * yi);
+        y[2 * c + 1] = (c0 * xi + c1 * xr) + (d0 * yi + d1 * yr);
+      }
+    }
+    return;
+  }
+  std::vector<int> off((size_t)gd);
   for (int j = 0; j < gd; ++j) {
     int o = 0;
     for (int b = 0; b < q; ++b)
       if ((j >> (q - 1 - b)) & 1) o |= 1 << bits[b];
     off[(size_t)j] = o;
   }
-  for (int b = 0; b < q; ++b) mask |= 1 << bits[b];
   std::vector<double> v((size_t)2 * gd);
   for (int r0 = 0; r0 < dim; ++r0) {
     if (r0 & mask) continue;

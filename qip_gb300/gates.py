@@ -20,7 +20,6 @@ matrix on the union of its indices.
 """
 from __future__ import annotations
 
-import copy
 from dataclasses import dataclass, field
 from typing import Any, Dict, List, Mapping, Sequence, Tuple
 
@@ -66,7 +65,17 @@ class GateOp:
         return 2.0 ** (-len(self.controls))
 
     def matrix(self) -> Tuple[Tuple[int, ...], numpy.ndarray]:
-        """Dense matrix of the whole operation on ``order`` (controls first)."""
+        """Dense matrix of the whole operation on ``order`` (controls first); read-only
+        for callers.  Copies of a cached decomposition build it once (``shared``)."""
+        shared = getattr(self, "shared", None)
+        if shared is None:
+            return self._dense()
+        hit = shared.get("matrix")
+        if hit is None:
+            hit = shared["matrix"] = self._dense()
+        return hit
+
+    def _dense(self) -> Tuple[Tuple[int, ...], numpy.ndarray]:
         if self.kind == "swap":
             a, b = self.targets, self.swap_b
             m = len(a)
@@ -238,7 +247,7 @@ def decompose(mats: Mapping[Any, Any]) -> List[GateOp]:
         key = tuple(key)
         hit = _cache.get(key)
         if hit is not None:
-            return [copy.copy(op) for op in hit]
+            return [_clone(op) for op in hit]
     ops = _decompose(mats)
     if key is not None:
         if len(_cache) >= _CACHE_MAX:
@@ -252,8 +261,15 @@ def decompose(mats: Mapping[Any, Any]) -> List[GateOp]:
             op.finite = op.mat is None or bool(numpy.all(numpy.isfinite(op.mat)))
             op.shared = {}  # per-template data the copies share (the backend's call arguments)
         _cache[key] = ops
-        return [copy.copy(op) for op in ops]
+        return [_clone(op) for op in ops]
     return ops
+
+
+def _clone(op: GateOp) -> GateOp:
+    """A shallow copy of a cached op (its attributes, the arrays and ``shared`` shared)."""
+    new = object.__new__(GateOp)
+    new.__dict__.update(op.__dict__)
+    return new
 
 
 def _decompose(mats: Mapping[Any, Any]) -> List[GateOp]:

@@ -388,3 +388,47 @@ def test_autotuner_widens_small_blocks_only_where_measured_faster():
     slow6 = _synthetic_tuner(lambda k, low: 3.0 if k == 6 else 1.0)
     out = slow6.place(None, n, [small, op])
     assert out[0] is small and out[1] is op
+
+
+def test_native_block_matrices_match_numpy_for_every_gate_kind():
+    """qsv_block_matrices (diagonal and one-qubit fast paths, general gather loop) against
+    numpy products of the same gates, for blocks of 2..7 qubits."""
+    rng = numpy.random.default_rng(17)
+    n = 9
+
+    def unitary(k):
+        z = rng.standard_normal((2 ** k, 2 ** k)) + 1j * rng.standard_normal((2 ** k, 2 ** k))
+        return numpy.linalg.qr(z)[0]
+
+    def rand_gate():
+        kind = rng.integers(6)
+        qs = [int(x) for x in rng.choice(n, size=3, replace=False)]
+        if kind == 0:
+            return {(qs[0],): unitary(1)}
+        if kind == 1:
+            return {(qs[0],): numpy.diag(numpy.exp(1j * rng.uniform(0, 6, 2)))}
+        if kind == 2:
+            return {(qs[0], qs[1]): CMat(numpy.diag([1, -1.0]))}
+        if kind == 3:
+            return {tuple(qs[:2]): unitary(2)}
+        if kind == 4:
+            return {tuple(qs): CMat(SwapMat(1))}
+        return {tuple(qs): unitary(3)}
+
+    ops = [op for _ in range(400) for op in gates.decompose(rand_gate())]
+    groups, cur, cur_q = [], [], set()
+    for op in ops:
+        kmax = int(rng.integers(2, 8))
+        if cur and len(cur_q | set(op.qubits)) > kmax:
+            groups.append(cur)
+            cur, cur_q = [], set()
+        cur.append(op)
+        cur_q |= set(op.qubits)
+    groups.append(cur)
+    groups = [g for g in groups if len(g) > 1]
+    assert len(groups) > 50
+    steps = fusion.emit_native(groups)
+    for grp, st in zip(groups, steps):
+        qs, want = fusion.block_matrix(grp)
+        assert st.qubits == qs
+        numpy.testing.assert_allclose(st.matrix, want, rtol=0, atol=1e-13)
