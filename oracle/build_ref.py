@@ -31,18 +31,28 @@ import sysconfig
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("QIP_REFERENCE_ROOT", "/root/reference")
-REF_EXT = os.path.join(REF_ROOT, "qip", "ext")
+REPO = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_ref")
 SRC = os.path.join(OUT, "src")
 LIB = os.path.join(OUT, "lib")
 MODULES = ("util", "kronprod", "func_apply")
 
 
+def reference_checkout():
+    """The reference's source checkout: ``QIP_REFERENCE_ROOT`` when set, else a folder
+    named ``reference`` beside this repository; None when neither holds ``qip/ext``."""
+    for cand in (os.environ.get("QIP_REFERENCE_ROOT"), os.path.join(os.path.dirname(REPO), "reference")):
+        if cand and os.path.isdir(os.path.join(cand, "qip", "ext")):
+            return os.path.abspath(cand)
+    return None
+
+
 def _cythonize() -> bool:
     """Stage 1: .pyx -> .c (only where the reference checkout and Cython exist)."""
-    if not os.path.isdir(REF_EXT):
+    checkout = reference_checkout()
+    if checkout is None:
         return False
+    ref_ext = os.path.join(checkout, "qip", "ext")
     try:
         from Cython.Compiler import Options  # noqa: F401
         from Cython.Compiler.Main import compile as cy_compile, CompilationOptions
@@ -50,13 +60,13 @@ def _cythonize() -> bool:
         return False
     os.makedirs(SRC, exist_ok=True)
     for name in MODULES:
-        pyx = os.path.join(REF_EXT, name + ".pyx")
+        pyx = os.path.join(ref_ext, name + ".pyx")
         out_c = os.path.join(SRC, name + ".c")
         if os.path.exists(out_c) and os.path.getmtime(out_c) >= os.path.getmtime(pyx):
             continue
         opts = CompilationOptions(
             output_file=out_c,
-            include_path=[REF_EXT],
+            include_path=[ref_ext],
             compiler_directives={
                 "language_level": 3,
                 "cpow": True,

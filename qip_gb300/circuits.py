@@ -70,17 +70,32 @@ def gate_amp_updates(gates: Sequence[Mats], n: int) -> float:
     return total
 
 
-def qft_gates(n: int, first: int = 0, rev: bool = True) -> List[Mats]:
-    """``QFFT`` on qubits first..first+n-1, in the order the graph executes it."""
-    q = list(range(first, first + n))
-    gates: List[Mats] = []
-    for off in range(n):
-        gates.append({(q[off],): H_MAT})
-        for i in range(off + 1, n):
-            gates.append({(q[i], q[off]): CMat(rm_mat(1 + i - off))})
+def qft_schedule(n: int, rev: bool = True):
+    """The QFT's steps over wire positions 0..n-1, in the order QIP's ``QFFT`` graph
+    executes them (``qip/qfft.py:8-43``): ``("h", t)``; ``("cphase", c, t, m)``, an Rm(m)
+    on t controlled by c, for every later wire c with m = 1 + c - t; then with ``rev``
+    ``("swap", a, n-1-a)`` for the first n//2 wires.  Both ``qft_gates`` and the graph
+    op ``qip_gb300.qfft.QFFT`` are built from this list."""
+    for t in range(n):
+        yield ("h", t)
+        for c in range(t + 1, n):
+            yield ("cphase", c, t, 1 + c - t)
     if rev:
-        for i in range(n // 2):
-            gates.append({(q[i], q[n - 1 - i]): SwapMat(1)})
+        for a in range(n // 2):
+            yield ("swap", a, n - 1 - a)
+
+
+def qft_gates(n: int, first: int = 0, rev: bool = True) -> List[Mats]:
+    """``QFFT`` on qubits first..first+n-1 as kron dictionaries, in execution order."""
+    gates: List[Mats] = []
+    for step in qft_schedule(n, rev):
+        wires = tuple(first + w for w in step[1:3])
+        if step[0] == "h":
+            gates.append({wires[:1]: H_MAT})
+        elif step[0] == "cphase":
+            gates.append({wires: CMat(rm_mat(step[3]))})
+        else:
+            gates.append({wires: SwapMat(1)})
     return gates
 
 

@@ -223,65 +223,97 @@ def C(op: OpConstructor) -> OpConstructor:
     return QubitOpWrapper(COp, op)
 
 
+def _check_control_inputs(inputs: Sequence[Qubit]) -> None:
+    """Argument rules of a controlled op (messages as QIP's, which callers catch)."""
+    if len(inputs) < 2:
+        raise ValueError("Not enough input values given.")
+    if inputs[0].n != 1:
+        raise ValueError("Control bit can only be of size n=1")
+    if len(set(inputs)) != len(inputs):
+        raise ValueError("Cannot have repeated qubits in COp")
+
+
 class COp(MatrixOp):
+    """``op`` controlled by the first input (a single qubit, active at |1>).
+
+    The wrapped op is built on the other inputs without registering itself as their
+    consumer or splitting its output; this node takes over its qid, so it runs where
+    the plain op would.  Its dictionary is the op's, each key prefixed by the control
+    index and each matrix wrapped in ``CMat`` (nested ``C(C(...))`` nest CMats)."""
+
     def __init__(self, op: OpConstructor, *inputs: Qubit, **kwargs):
-        if len(inputs) < 2:
-            raise ValueError("Not enough input values given.")
-        if inputs[0].n != 1:
-            raise ValueError("Control bit can only be of size n=1")
-        if len(set(inputs)) < len(inputs):
-            raise ValueError("Cannot have repeated qubits in COp")
-        inner_kwargs = dict(kwargs)
-        inner_kwargs["nosink"] = True
-        inner_kwargs["nosplit"] = True
-        self.op = cast(MatrixOp, self.make_op(op, inputs, inner_kwargs))
-        if not issubclass(type(self.op), MatrixOp):
+        _check_control_inputs(inputs)
+        # A fresh dict per call: the caller's kwargs go unchanged to this node.
+        self.op = cast(MatrixOp, self.make_op(op, inputs, {**kwargs, "nosink": True, "nosplit": True}))
+        if not isinstance(self.op, MatrixOp):
             raise ValueError("C(Op) may only be applied to matrix ops and swaps, not {}".format(type(self.op)))
         super().__init__(*inputs, qid=self.op.qid, **kwargs)
 
     def make_op(self, op: OpConstructor, inputs: Sequence[Qubit], nkwargs: Mapping[str, Any]):
-        return op(*inputs[1:], **nkwargs)
+        """The controlled op, on every input but the control."""
+        target_regs = inputs[1:]
+        return op(*target_regs, **nkwargs)
 
     def makemats(self, index_groups):
-        inner = self.op.makemats(index_groups[1:])
-        return {tuple(flatten([index_groups[0], idx])): CMat(m) for idx, m in inner.items()}
+        control = list(index_groups[0])
+        return {tuple(control + list(flatten([key]))): CMat(m)
+                for key, m in self.op.makemats(index_groups[1:]).items()}
 
     def __repr__(self):
         return "C{}".format(self.op)
 
 
+def _as_dense(m) -> numpy.ndarray:
+    """A numpy matrix of ``m``: an array, a ``CMat`` or a ``SwapMat``."""
+    if isinstance(m, CMat):
+        return m.numpy()
+    if isinstance(m, SwapMat):
+        rows = numpy.arange(m.shape[0])
+        low = (1 << m.n) - 1
+        out = numpy.zeros(m.shape, dtype=numpy.complex128)
+        out[rows, ((rows & low) << m.n) | (rows >> m.n)] = 1.0
+        return out
+    return numpy.asarray(m)
+
+
 class CMat(object):
-    """Block matrix diag(I, m): identity while the leading (control) index is 0."""
+    """Block-diagonal matrix diag(I, m) of twice m's size: identity while the leading
+    (control) index bit is 0, ``m`` when it is 1.  The backend recognises it by
+    ``_kron_struct == 2`` and visits only the control-satisfied half."""
 
     _kron_struct = 2
 
     def __init__(self, mat):
-        self.m = numpy.array(mat) if type(mat) == list else mat  # noqa: E721
-        self.shape = (self.m.shape[0] * 2, self.m.shape[1] * 2)
+        self.m = numpy.array(mat) if type(mat) == list else mat  # noqa: E721 (other sequences are kept as given)
+        rows, cols = self.m.shape[0], self.m.shape[1]
+        self.shape = (2 * rows, 2 * cols)
 
     def __getitem__(self, item):
-        if type(item) == tuple and len(item) == 2:  # noqa: E721
-            r, c = item
-            h0, h1 = self.shape[0] // 2, self.shape[1] // 2
-            if r < h0 and c < h1:
-                return 1.0 if r == c else 0.0
-            if r >= h0 and c >= h1:
-                return self.m[r - h0, c - h1]
-            return 0.0
-        raise ValueError("CMat can only be indexed with M[i,j] not M[{}]".format(item))
+        if not (type(item) == tuple and len(item) == 2):  # noqa: E721
+            raise ValueError("CMat can only be indexed with M[i,j] not M[{}]".format(item))
+        r, c = item
+        hr, hc = self.shape[0] // 2, self.shape[1] // 2
+        if (r >= hr) != (c >= hc):
+            return 0.0  # off-diagonal blocks
+        if r >= hr:
+            return self.m[r - hr, c - hc]
+        return 1.0 if r == c else 0.0
 
     def conj(self):
+        """Element-wise conjugate (a CMat again)."""
         return CMat(self.m.conj())
 
     @property
     def T(self):
+        """Transpose (a CMat again)."""
         return CMat(self.m.T)
 
-    def numpy(self):
+    def numpy(self) -> numpy.ndarray:
+        inner = _as_dense(self.m).astype(numpy.complex128)
+        hr, hc = inner.shape
         out = numpy.zeros(self.shape, dtype=numpy.complex128)
-        for i in range(self.shape[0]):
-            for j in range(self.shape[1]):
-                out[i, j] = self[i, j]
+        out[:hr, :hc] = numpy.eye(hr, hc)
+        out[hr:, hc:] = inner
         return out
 
 

@@ -1,43 +1,43 @@
-"""Quantum Fourier transform circuit (``qip/qfft.py``): per qubit an H, then controlled
-phase rotations from every later qubit, then a register reversal by Swaps."""
+"""The quantum Fourier transform as a graph op (QIP's ``qip/qfft.py:8-43``).
+
+``QFFT(*registers, rev=True)`` cuts every input register into single-qubit wires and
+applies ``circuits.qft_schedule``: per wire an H, then an Rm controlled by each later
+wire, then (``rev``) Swaps that reverse the wire order.  The outputs are regrouped into
+registers of the inputs' sizes.  The controlled phase is built as QIP builds it,
+``C(lambda *q, **kw: Rm(m, *q, negate=True, **kw))``: QIP's op wrapper drops call-time
+keyword arguments (``qip/qubit_util.py:142-143``), so ``negate`` has no effect there
+and none here — the transform is the inverse DFT, as in the reference.
+"""
 from __future__ import annotations
 
-from typing import MutableSequence, Tuple, Union
+from itertools import accumulate
+from typing import Tuple, Union
 
+from .circuits import qft_schedule
 from .operators import C, H, Rm, Swap
 from .qip import Qubit
 from .qubit_util import QubitFuncWrapper
-from .util import flatten
+
+
+def _controlled_rm(m: int):
+    return C(lambda *inputs, **kwargs: Rm(m, *inputs, negate=True, **kwargs))
 
 
 @QubitFuncWrapper.wrap
 def QFFT(*inputs: Qubit, rev: bool = True) -> Union[Qubit, Tuple[Qubit, ...]]:
-    qarr = flatten([inp.split(range(inp.n)) for inp in inputs])
-    recQFFT(qarr)
-    if rev:
-        half = len(qarr) // 2
-        for i in range(half):
-            qarr[i], qarr[-1 - i] = Swap(qarr[i], qarr[-1 - i])
-    if len(inputs) < len(qarr):
-        outputs = []
-        start = 0
-        for qubit in inputs:
-            outputs.append(Qubit(*(qarr[start:start + qubit.n])))
-            start += qubit.n
+    wires = [w for reg in inputs for w in reg.split(range(reg.n))]
+    for step in qft_schedule(len(wires), rev):
+        if step[0] == "h":
+            wires[step[1]] = H(wires[step[1]])
+        elif step[0] == "cphase":
+            _, c, t, m = step
+            wires[c], wires[t] = _controlled_rm(m)(wires[c], wires[t])
+        else:
+            _, a, b = step
+            wires[a], wires[b] = Swap(wires[a], wires[b])
+    if len(wires) == len(inputs):
+        outputs = wires
     else:
-        outputs = qarr
-    return tuple(outputs) if len(outputs) > 1 else outputs[0]
-
-
-def recQFFT(qarr: MutableSequence[Qubit], offset: int = 0):
-    """Iterative form of the reference's recursion (``qip/qfft.py:33-39``): same gates in
-    the same order, without Python's recursion limit at large n."""
-    for off in range(offset, len(qarr)):
-        qarr[off] = H(qarr[off])
-        for i in range(off + 1, len(qarr)):
-            m = 1 + i - off
-            qarr[i], qarr[off] = C(makeR(m))(qarr[i], qarr[off])
-
-
-def makeR(m: int):
-    return lambda *inputs, **kwargs: Rm(m, *inputs, negate=True, **kwargs)
+        ends = list(accumulate(reg.n for reg in inputs))
+        outputs = [Qubit(*wires[lo:hi]) for lo, hi in zip([0] + ends[:-1], ends)]
+    return outputs[0] if len(outputs) == 1 else tuple(outputs)
