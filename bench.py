@@ -16,6 +16,13 @@ Our arm (default):
              2^n complex64 state) over its mean CUDA-event launch time.
   cpu_baseline  the reference's own Cython/OpenMP kernel (cdot_loop) on the host's cores,
              a bounded sample of the same gate list at the same n.
+  hbm_n32    QFT + 8 Grover iterations at n=32 complex64 (fused) and n=31 complex128
+             (per-gate): per-pass GB/s and fraction of the HBM peak, every single-qubit
+             marginal, the marked probability against Grover's closed form.
+  adjoint    adjoint gradients of the n=24, 960-angle ansatz for 64 parameter sets:
+             gradient vectors/s, backward/forward, error against central differences.
+  batched    4096 uneven circuits in one persistent launch: circuits/s, p50/p99 latency.
+  Each of the last three has its own CUDA-event timing and clock record.
 --impl reference: the reference CPU kernel alone, same metric/config, one JSON line.
 
 Multi-GPU: every rank runs an independent replica (the state vector is not sharded);
@@ -371,15 +378,27 @@ def run_ours(args):
     # whole-circuit plan kept after the first (qip_gb300.plancache); the blocks per step
     # are reported.
     e2e_stats = {}
+    stage_log = {True: [], False: []}
 
     def e2e_step(keep_plans=True):
+        # Stages: create, submit (one kronselect_dot per gate; blocks launch while gates
+        # arrive), drain (the last blocks; synchronize), readback (get_state: one DMA into
+        # a pooled page-locked array), close.  The step's time is their sum.
+        t0 = time.perf_counter()
         s2 = GpuBackend.make_state(n, [], [], statetype=numpy.complex64, fusion=True, max_block=kmax,
                                    keep_plans=keep_plans)
+        t1 = time.perf_counter()
         for g in gl:
             s2.kronselect_dot(g)
+        t2 = time.perf_counter()
+        s2.synchronize()
+        t3 = time.perf_counter()
         out = s2.get_state()
+        t4 = time.perf_counter()
         e2e_stats.update(s2.stats)
         s2.close()
+        t5 = time.perf_counter()
+        stage_log[keep_plans].append((t1 - t0, t2 - t1, t3 - t2, t4 - t3, t5 - t4))
         return out
 
     e2e_steps = max(1, min(args.steps, 3))
@@ -389,6 +408,7 @@ def run_ours(args):
     w1 = e2e_step()
     w2 = e2e_step()
     del w1, w2
+    stage_log[True].clear()
     # The objects this benchmark built for the other legs live on; keep the collector's
     # full scans from walking them during the timed steps (collection itself stays on).
     gc.collect()
@@ -447,24 +467,52 @@ def run_ours(args):
                 "blocks_per_step": replay_stats.get("blocks"), "replayed_steps": replay_stats.get("replayed_steps"),
                 "streamed": {"seconds_per_step": t_streamed, "value": ws * amp_updates / t_streamed,
                              "blocks_per_step": streamed_blocks,
+                             "stages_ms": stage_summary(stage_log[False], len(gl)),
                              "note": "the same circuits with keep_plans=False: each planned window by window "
                                      "as a circuit run once is"},
+                "stages_ms": stage_summary(stage_log[True], len(gl)),
                 "clocks": clk_e2e.summary()},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
+    # Configs 3, 4 and 5 on the same GPU, each with its own CUDA-event timing and clocks.
+    if "hbm" in parts:
+        result["hbm_n32"] = measure_hbm(args)
+    if "adjoint" in parts:
+        result["adjoint"] = measure_adjoint(args)
+    if "batched" in parts:
+        result["batched"] = measure_batched(args, cpu_seconds=0 if args.no_cpu or "cpu" not in parts
+                                            else min(args.cpu_seconds, 8.0))
     if rank == 0 and ws == 1 and not args.no_cpu and "cpu" in parts:
         v, info = cpu_reference_sample(n, gl, seconds_cap=args.cpu_seconds)
         info = dict(info)
         info["value"] = v
         info["unit"] = "amp-updates/s"
         result["cpu_baseline"] = info
+        # Precision-matched: the GPU's complex128 per-gate path against the reference's
+        # complex128 CPU kernel.
+        if v:
+            result["plain_fp64"]["vs_cpu_reference_c128"] = result["plain_fp64"]["value"] / v
     if rank == 0:
         print(json.dumps(result), flush=True)
     if ws > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def stage_summary(rows, ngates):
+    """Median milliseconds per e2e stage over the timed steps, and host microseconds per
+    gate while submitting."""
+    if not rows:
+        return None
+    names = ("create", "submit", "drain", "readback", "close")
+    med = [statistics.median(r[i] for r in rows) * 1e3 for i in range(len(names))]
+    out = {k: round(v, 3) for k, v in zip(names, med)}
+    out["submit_us_per_gate"] = round(med[1] * 1e3 / ngates, 2)
+    out["gc"] = "collector frozen over the setup objects; collection stays on"
+    out["readback_buffer"] = "pooled page-locked array (no first-touch faults after warm-up)"
+    return out
 
 
 def fusion_image_bytes(k):
@@ -588,20 +636,21 @@ def op_touched(op, n: int) -> float:
     return sub
 
 
-def run_hbm(args):
-    """QFT + 8 amplitude-amplification iterations at n=32 complex64 (fused) and n=31
-    complex128 (per-gate); all single-qubit marginals; per-pass achieved GB/s.  Checked
-    against Grover's closed form (the QFT of |0...0> is the uniform state)."""
+def measure_hbm(args):
+    """Config 3: QFT + 8 amplitude-amplification iterations at n=32 complex64 (fused) and
+    n=31 complex128 (per-gate); every single-qubit marginal; per-pass achieved GB/s by
+    CUDA events on the launching stream.  Checked against Grover's closed form (the QFT
+    of |0...0> is the uniform state)."""
     import torch
 
-    from qip_gb300 import GpuBackend, _native as nat, circuits, fusion, gates as gmod
+    from qip_gb300 import GpuBackend, circuits, fusion, gates as gmod
     from qip_gb300.autotune import default_tuner
 
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     peak, peak_src = read_peaks()
     out = {"metric": "achieved HBM GB/s per pass and amp-updates/s (QFT + 8 Grover iterations)",
-           "unit": "GB/s", "peak": peak, "peak_source": peak_src, "runs": []}
+           "unit": "GB/s", "peak": peak, "peak_source": f"{peak_src} hbm_gbs", "runs": []}
     for n, dt, fusion_on in ((args.hbm_n64, numpy.complex64, True), (args.hbm_n128, numpy.complex128, False)):
         gl, marked = circuits.grover_gates(n, 8, seed=7)
         amp = circuits.gate_amp_updates(gl, n)
@@ -610,38 +659,40 @@ def run_hbm(args):
         st.set_stream(stream.cuda_stream)
         size = 8 if dt == numpy.complex64 else 16
         per_kind = {}
-        e0, e1 = _events()
         if fusion_on:
             steps = default_tuner().place(st.handle, n, fusion.plan(ops, kmax=6))
         else:
             steps = ops
         t_all0, t_all1 = _events()
-        t_all0.record(stream)
-        for stp in steps:
-            a, b = _events()
-            a.record(stream)
-            if isinstance(stp, fusion.Block) and len(stp.qubits) >= 4:
-                st.apply_blocks([stp])
-                kind, touched = "fused_block", 2 ** n
-            elif isinstance(stp, fusion.Block):
-                for op in gmod.classify_matrix(stp.qubits, (), stp.matrix):
-                    st.apply_op(op)
-                kind, touched = "small_block", 2 ** n
-            else:
-                st.apply_op(stp)
-                kind = f"{stp.kind}{len(stp.targets)}c{len(stp.controls)}"
-                touched = op_touched(stp, n)
-            b.record(stream)
-            per_kind.setdefault(kind, []).append((a, b, touched))
-        t_all1.record(stream)
-        t_all1.synchronize()
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            torch.cuda.synchronize()
+            t_all0.record(stream)
+            for stp in steps:
+                a, b = _events()
+                a.record(stream)
+                if isinstance(stp, fusion.Block) and len(stp.qubits) >= 4:
+                    st.apply_blocks([stp])
+                    kind, touched = "fused_block", 2 ** n
+                elif isinstance(stp, fusion.Block):
+                    for op in gmod.classify_matrix(stp.qubits, (), stp.matrix):
+                        st.apply_op(op)
+                    kind, touched = "small_block", 2 ** n
+                else:
+                    st.apply_op(stp)
+                    kind = f"{stp.kind}{len(stp.targets)}c{len(stp.controls)}"
+                    touched = op_touched(stp, n)
+                b.record(stream)
+                per_kind.setdefault(kind, []).append((a, b, touched))
+            t_all1.record(stream)
+            t_all1.synchronize()
         total_s = t_all0.elapsed_time(t_all1) * 1e-3
         kinds = {}
         for k, lst in per_kind.items():
             ms = [a.elapsed_time(b) for a, b, _ in lst]
             byt = sum(2 * t * size for _, _, t in lst)
-            kinds[k] = {"passes": len(lst), "mean_ms": statistics.mean(ms),
-                        "GB_s": byt / (sum(ms) * 1e-3) / 1e9}
+            gbs = byt / (sum(ms) * 1e-3) / 1e9
+            kinds[k] = {"passes": len(lst), "mean_ms": round(statistics.mean(ms), 4), "GB_s": round(gbs, 1),
+                        "frac": round(gbs / peak, 4)}
         marg, nrm = st.qubit_marginals()
         N = 2.0 ** n
         th = numpy.arcsin(1 / numpy.sqrt(N))
@@ -654,44 +705,56 @@ def run_hbm(args):
         out["runs"].append({
             "n": n, "dtype": "c64" if dt == numpy.complex64 else "c128", "fused": fusion_on,
             "gates": len(gl), "passes": len(steps), "seconds": total_s, "amp_updates_per_s": amp / total_s,
-            "per_pass": kinds, "max_abs_err_marginals": float(numpy.max(numpy.abs(marg - want))),
-            "norm2": nrm, "marked_prob": float(abs(amp_m) ** 2), "marked_prob_expected": float(pm)})
+            "per_pass": kinds, "marginals_p1": [float(f"{x:.10g}") for x in marg],
+            "max_abs_err_marginals": float(numpy.max(numpy.abs(marg - want))),
+            "norm2": nrm, "marked_index": marked, "marked_prob": float(abs(amp_m) ** 2),
+            "marked_prob_expected": float(pm), "clocks": clk.summary()})
         torch.cuda.synchronize()
     fb = out["runs"][0]["per_pass"].get("fused_block")
     out["value"] = fb["GB_s"] if fb else None
-    out["frac"] = out["value"] / peak if fb else None
-    print(json.dumps(out), flush=True)
+    out["frac"] = fb["frac"] if fb else None
+    out["kernel"] = "k_block_tc at n=32 (fused blocks of the QFT + Grover plan)"
+    return out
 
 
-def run_batched(args):
-    """4096 independent circuits (n ~ U[8,20], depth ~ U[20,100]) in one persistent launch,
-    replayed from a CUDA graph: circuits/s and per-circuit latency percentiles."""
+def run_hbm(args):
+    print(json.dumps(measure_hbm(args)), flush=True)
+
+
+def measure_batched(args, cpu_seconds=None):
+    """Config 4: 4096 independent circuits (n ~ U[8,20], depth ~ U[20,100]) in one
+    persistent launch, replayed from a CUDA graph: circuits/s (CUDA events) and
+    per-circuit device latency percentiles (%globaltimer stamps)."""
     import torch
 
-    from qip_gb300 import batch, circuits
+    from qip_gb300 import batch
 
     circs, feeds, sizes = batch.random_batch(args.batch_count, seed=4096)
     b = batch.CircuitBatch(circs, feeds, sizes)
     stream = torch.cuda.Stream()
-    for _ in range(args.warmup):
+    for _ in range(max(3, args.warmup)):
         b.run(stream.cuda_stream)
     stream.synchronize()
     e0, e1 = _events()
-    e0.record(stream)
-    for _ in range(args.steps):
-        b.run(stream.cuda_stream)
-    e1.record(stream)
-    e1.synchronize()
-    dt = e0.elapsed_time(e1) * 1e-3 / args.steps
+    steps = max(5, args.steps)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        e0.record(stream)
+        for _ in range(steps):
+            b.run(stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+    dt = e0.elapsed_time(e1) * 1e-3 / steps
     lat = b.latencies_ns() / 1e6
+    p50, p99 = float(numpy.percentile(lat, 50)), float(numpy.percentile(lat, 99))
     res = {"metric": "circuits/s (batched uneven circuits, one persistent launch)", "value": args.batch_count / dt,
-           "unit": "circuits/s", "ms_per_step": dt * 1e3, "steps": args.steps, "dtype": "c64",
+           "unit": "circuits/s", "ms_per_step": dt * 1e3, "steps": steps, "dtype": "c64",
            "config": {"workload": f"{args.batch_count} circuits, n~U[8,20], depth~U[20,100], "
                                   "gates H/X/Rm/CNOT/C(Swap)/Haar, random product feeds"},
-           "latency_ms": {"p50": float(numpy.percentile(lat, 50)), "p99": float(numpy.percentile(lat, 99)),
-                          "max": float(lat.max())}}
+           "latency_ms": {"p50": p50, "p99": p99, "max": float(lat.max()), "p99_over_p50": p99 / p50},
+           "clocks": clk.summary()}
     b.close()
-    kp = load_reference_kernels()
+    cap = args.cpu_seconds if cpu_seconds is None else cpu_seconds
+    kp = load_reference_kernels() if cap > 0 else None
     if kp is not None:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
         t0 = time.perf_counter()
@@ -706,18 +769,24 @@ def run_batched(args):
                 kp.cdot_loop(ci, cm, st, n, o2)
                 st, o2 = o2, st
             done += 1
-            if time.perf_counter() - t0 > args.cpu_seconds:
+            if time.perf_counter() - t0 > cap:
                 break
         rt = time.perf_counter() - t0
         res["cpu_baseline"] = {"kind": "reference", "value": done / rt, "unit": "circuits/s",
                                "cores": int(os.environ["OMP_NUM_THREADS"]),
                                "sample": f"first {done} circuits of the same list through the reference cdot_loop"}
-    print(json.dumps(res), flush=True)
+    return res
 
 
-def run_adjoint(args):
-    """Adjoint gradients: n=24, 20 layers of RY/RZ on every qubit + CNOT ring (960 angles),
-    objective <sum Z>, batch of 64 parameter sets, complex64."""
+def run_batched(args):
+    print(json.dumps(measure_batched(args)), flush=True)
+
+
+def measure_adjoint(args):
+    """Config 5: adjoint gradients, n=24, 20 layers of RY/RZ on every qubit + CNOT ring
+    (960 angles), objective <sum Z>, batch of 64 parameter sets, complex64.  Forward and
+    backward timed by CUDA events on the current stream; the gradient is spot-checked
+    against complex128 central differences (h=1e-3) on seeded angles."""
     import torch
 
     from qip_gb300 import adjoint
@@ -726,24 +795,28 @@ def run_adjoint(args):
     a = adjoint.Ansatz(n, L)
     th = torch.tensor(numpy.random.default_rng(2025).uniform(0, 2 * numpy.pi, (B, a.nparams)), device="cuda")
     fwd, bwd = [], []
-    for rep in range(args.warmup + args.steps):
-        thr = th.clone().requires_grad_(True)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e = adjoint.SumZExpectation.apply(thr, a, torch.complex64)
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        e.sum().backward()
-        torch.cuda.synchronize()
-        t2 = time.perf_counter()
-        if rep >= args.warmup:
-            fwd.append(t1 - t0)
-            bwd.append(t2 - t1)
+    reps = max(1, min(args.steps, 2))
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for rep in range(1 + reps):
+            thr = th.clone().requires_grad_(True)
+            e0, e1 = _events()
+            e2 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            e = adjoint.SumZExpectation.apply(thr, a, torch.complex64)
+            e1.record()
+            e.sum().backward()
+            e2.record()
+            e2.synchronize()
+            if rep >= 1:
+                fwd.append(e0.elapsed_time(e1) * 1e-3)
+                bwd.append(e1.elapsed_time(e2) * 1e-3)
     g = thr.grad
     tf, tb = statistics.mean(fwd), statistics.mean(bwd)
-    # Spot check against complex128 central differences (h=1e-3) on a few angles.
-    checks = []
-    for j in (0, a.nparams // 2, a.nparams - 1):
+    rng = numpy.random.default_rng(77)
+    idx = sorted({0, a.nparams - 1, *(int(x) for x in rng.choice(a.nparams, 4, replace=False))})
+    errs = []
+    for j in idx:
         tp, tm = th[:1].clone(), th[:1].clone()
         tp[0, j] += 1e-3
         tm[0, j] -= 1e-3
@@ -751,15 +824,21 @@ def run_adjoint(args):
             ep = adjoint.SumZExpectation.apply(tp, a, torch.complex128)
             em = adjoint.SumZExpectation.apply(tm, a, torch.complex128)
         fd = float((ep - em).item() / 2e-3)
-        checks.append(abs(fd - float(g[0, j].item())))
-    print(json.dumps({
+        errs.append(abs(fd - float(g[0, j].item())))
+    return {
         "metric": "gradient vectors/s (adjoint method, batch of parameter sets)", "value": B / (tf + tb),
-        "unit": "gradients/s", "dtype": "c64", "steps": args.steps,
+        "unit": "gradients/s", "dtype": "c64", "steps": reps,
         "config": {"workload": f"ansatz n={n}, {L} layers RY/RZ + CNOT ring, {a.nparams} angles, batch {B}, "
                                "objective <sum Z>"},
         "forward_s": tf, "backward_s": tb, "backward_over_forward": tb / tf,
         "grad_components_per_s": B * a.nparams / (tf + tb),
-        "max_abs_err_vs_fd_c128": max(checks)}), flush=True)
+        "fd_checked_angles": idx, "max_abs_err_vs_fd_c128": max(errs),
+        "cpu_baseline": None, "cpu_baseline_note": "the reference has no gradient code (qip/backend.py:14-65)",
+        "clocks": clk.summary()}
+
+
+def run_adjoint(args):
+    print(json.dumps(measure_adjoint(args)), flush=True)
 
 
 def run_block_placements(args):
@@ -879,8 +958,8 @@ def main():
                     help="JSON file of autotuner decisions: loaded if present, written after tuning")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--parts", default="fused,plain,e2e,cpu",
-                    help="comma list of fused,plain,e2e,cpu (profiling runs use fused only)")
+    ap.add_argument("--parts", default="fused,plain,e2e,cpu,hbm,adjoint,batched",
+                    help="comma list of fused,plain,e2e,cpu,hbm,adjoint,batched (profiling runs use fused only)")
     ap.add_argument("--workload", default="brickwork", choices=["brickwork", "qft16", "hbm", "batched", "adjoint", "blocks", "gates"])
     ap.add_argument("--hbm-n64", type=int, default=32)
     ap.add_argument("--hbm-n128", type=int, default=31)

@@ -136,6 +136,16 @@ int qsv_plan_create(qsv_state* s, int nblocks, const int* ks, const int* targets
                     const double* mats_c128, qsv_plan** out);
 int qsv_plan_launch(qsv_state* s, const qsv_plan* p, int first, int count);
 int qsv_plan_destroy(qsv_plan* p);
+/* Fault injection for tests of the bounded device waits (no reference counterpart: the
+ * reference's failure handling is host-side, qip/distributed/manager.py:219-236).  Arms
+ * the next fused-block launch on this handle (qsv_apply_blocks or qsv_plan_launch):
+ * in every CTA, the first wait for a tile's products waits on an mbarrier that nothing
+ * arrives on and gives up after wait_ns (1 us .. 1 s).  The kernel then waits (bounded,
+ * 2 s) for the products it has in flight, frees its tensor memory, sets the handle's
+ * status word and returns; it stores nothing, so the state is unchanged.  The next
+ * qsv_synchronize returns QSV_ERR_TIMEOUT and clears the status word; the handle stays
+ * usable. */
+int qsv_inject_block_stall(qsv_state* s, uint64_t wait_ns);
 
 /* Fusion planning on the host (no reference counterpart).  Gates are given as qubit bit
  * masks (bit q <-> qubit q) and amp-update weights.  Each round grows up to lookahead

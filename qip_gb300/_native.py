@@ -79,6 +79,7 @@ SIGNATURES = {
                                        ctypes.POINTER(ctypes.c_void_p)]),
     "qsv_plan_launch": (ctypes.c_int, [_handle, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "qsv_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "qsv_inject_block_stall": (ctypes.c_int, [_handle, ctypes.c_uint64]),
     "qsv_probabilities_static": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_int_p,
                                                 ctypes.c_void_p, ctypes.c_void_p]),
     "qsv_inner_product": (ctypes.c_int, [_handle, _handle, _c_double_p, _c_double_p]),

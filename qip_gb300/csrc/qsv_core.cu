@@ -1896,6 +1896,24 @@ int static_partials(double** out, int* sms) {
   return QSV_OK;
 }
 
+// The state and the output must be device memory of the current device, whose copy of
+// the static array the kernels use: a buffer on another GPU (or in host memory) is
+// rejected here rather than read over a peer link or faulted on.  Allocates nothing.
+int check_current_device_buffer(const void* p, const char* what) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return set_error(nullptr, QSV_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  cudaPointerAttributes at{};
+  e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(nullptr, QSV_ERR_INVALID, "%s: not a CUDA pointer (%s)", what, cudaGetErrorString(e));
+  }
+  if ((at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) || at.device != dev)
+    return set_error(nullptr, QSV_ERR_INVALID, "%s is not device memory of the current device (%d)", what, dev);
+  return QSV_OK;
+}
+
 template <typename R>
 int launch_probs_static(const void* d_amp, int n, int m, const int* pos_in_order, double* d_out,
                         cudaStream_t stream, double* partial, int sms) {
@@ -1953,9 +1971,13 @@ extern "C" int qsv_probabilities_static(const void* d_amp, int n, int dtype, int
     seen |= 1ull << p;
     pos[j] = p;
   }
+  int rc = check_current_device_buffer(d_amp, "the state");
+  if (rc) return rc;
+  rc = check_current_device_buffer(d_out, "the output");
+  if (rc) return rc;
   double* partial = nullptr;
   int sms = 0;
-  int rc = static_partials(&partial, &sms);
+  rc = static_partials(&partial, &sms);
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   return dtype == QSV_C64 ? launch_probs_static<float>(d_amp, n, m, pos, d_out, st, partial, sms)

@@ -113,6 +113,8 @@ struct BlockArgs {
   uint8_t tperm[64];    // kernel target order t' -> the caller's block matrix index
   const uint4* wimg;    // hi image then lo image (2 * W_BYTES bytes)
   int* flag;            // status word
+  uint64_t wait_ns;     // limit of each wait for a tile's products
+  int stall_first;      // fault injection: the first such wait is on a barrier nothing arrives on
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -155,11 +157,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Returns false if the phase did not complete within FB_WAIT_NS.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+// Returns false if the phase did not complete within limit_ns.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity,
+                                                  uint64_t limit_ns = FB_WAIT_NS) {
   const uint64_t t0 = globaltimer();
   while (!mbar_try_wait(bar, parity)) {
-    if (globaltimer() - t0 > FB_WAIT_NS) return false;
+    if (globaltimer() - t0 > limit_ns) return false;
   }
   return true;
 }
@@ -290,10 +293,12 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   uint16_t* et = eb + FB_M;
   uint8_t* swz = reinterpret_cast<uint8_t*>(et + P::T);
   uint64_t* dephi = reinterpret_cast<uint64_t*>(swz + P::TILE / 16);
-  // Tail: two mbarriers (one per accumulator), the TMEM address, the abort flag.
+  // Tail: two mbarriers (one per accumulator), the TMEM address, the abort flag, and
+  // the barrier of the injected stall (initialised, never arrived on).
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + SMEM_USED - 64);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 2);
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+  uint64_t* stall_bar = mbar + 3;
   constexpr int TCOLS = SHUF ? P::TMEM_COLS2 : P::TMEM_COLS;
 
   const int tid = threadIdx.x;
@@ -316,6 +321,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   if (tid == 0) {
     mbar_init(smem_u32(mbar), 1);
     mbar_init(smem_u32(mbar + 1), 1);
+    mbar_init(smem_u32(stall_bar), 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -610,6 +616,19 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
 
   uint32_t ph[2] = {0u, 0u};
   bool pending[2] = {false, false};
+  // Wait for the products in accumulator s (bounded by a.wait_ns).  With the injected
+  // stall, the CTA's first such wait is on stall_bar, which nothing arrives on: it gives
+  // up after a.wait_ns and takes the abort path (drain, free TMEM, status word).  Every
+  // CTA's first wait comes before its first store, so an aborted launch leaves the state
+  // as it was.
+  bool stall = a.stall_first != 0;
+  auto wait_products = [&](int s) -> bool {
+    if (stall) {
+      stall = false;
+      if (!mbar_wait_bounded(smem_u32(stall_bar), 0u, a.wait_ns)) return false;
+    }
+    return mbar_wait_bounded(bar_of(s), ph[s], a.wait_ns);
+  };
   uint64_t tile = blockIdx.x;
   uint64_t base = 0;
   if (tile < a.ntiles) {
@@ -629,7 +648,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         next_base = qsv_insert_zeros(next, a.ptile, P::EBITS);
         load_tile(next_base);
       }
-      if (mbar_wait_bounded(bar_of(0), ph[0])) {
+      if (wait_products(0)) {
         ph[0] ^= 1u;
         pending[0] = false;
       } else {
@@ -660,7 +679,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
       const int s = it & 1;
       if (it > 0) {
         // Products of the previous tile: A is free again and accumulator s^1 is ready.
-        if (mbar_wait_bounded(bar_of(s ^ 1), ph[s ^ 1])) {
+        if (wait_products(s ^ 1)) {
           ph[s ^ 1] ^= 1u;
           pending[s ^ 1] = false;
         } else {
@@ -687,7 +706,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
     }
     if (it > 0 && !*abort_flag) {
       const int s = (it - 1) & 1;
-      if (mbar_wait_bounded(bar_of(s), ph[s])) {
+      if (wait_products(s)) {
         ph[s] ^= 1u;
         pending[s] = false;
       } else {
@@ -1054,8 +1073,16 @@ bool mode_applies(int k, int low, int mode) {
 }
 
 template <int KQ, int MODE>
-int launch_block_variant(qsv_state* s, const BlockArgs& a, float2* psi) {
+int launch_block_variant(qsv_state* s, const BlockArgs& args, float2* psi) {
   using P = FB<KQ>;
+  BlockArgs a = args;
+  a.wait_ns = FB_WAIT_NS;
+  a.stall_first = 0;
+  if (s->inject_stall_ns) {  // armed by qsv_inject_block_stall for this one launch
+    a.wait_ns = s->inject_stall_ns;
+    a.stall_first = 1;
+    s->inject_stall_ns = 0;
+  }
   constexpr int SMEM = MODE == MODE_STAGED ? P::SMEM : P::SMEM_DIRECT;
   static bool configured = false;
   if (!configured) {
@@ -1192,6 +1219,14 @@ extern "C" int qsv_plan_launch(qsv_state* s, const qsv_plan* p, int first, int c
     int rc = launch_args(s, a);
     if (rc) return rc;
   }
+  return QSV_OK;
+}
+
+extern "C" int qsv_inject_block_stall(qsv_state* s, uint64_t wait_ns) {
+  QSV_CHECK_HANDLE(s);
+  if (wait_ns < 1000 || wait_ns > 1000000000ull)
+    return set_error(s, QSV_ERR_INVALID, "stall limit %llu ns outside [1 us, 1 s]", (unsigned long long)wait_ns);
+  s->inject_stall_ns = wait_ns;
   return QSV_OK;
 }
 

@@ -31,6 +31,9 @@ struct qsv_state {
   size_t scratch_bytes = 0;
   // Device status word written by kernels with bounded waits.
   int* d_flag = nullptr;
+  // Fault injection for tests (qsv_inject_block_stall): the limit of the stalled wait of
+  // the next fused-block launch, 0 when not armed.
+  uint64_t inject_stall_ns = 0;
   // Fused-block matrix images: a ring of pinned host staging slots (a slot is reused
   // only after its upload completed, so the host rarely waits for queued kernels) and
   // one device buffer (stream order keeps uploads behind the kernels reading it).

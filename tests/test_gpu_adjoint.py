@@ -62,3 +62,31 @@ def test_segmented_sweeps_match_per_gate_sweeps(statetype, rtol):
     scale = float(torch.max(torch.abs(g0)))
     numpy.testing.assert_allclose(e1.cpu().numpy(), e0.cpu().numpy(), atol=rtol * n)
     numpy.testing.assert_allclose(g1.cpu().numpy(), g0.cpu().numpy(), atol=rtol * scale * 10)
+
+
+def test_config5_full_size_against_central_differences():
+    """Config 5 at its own size: n=24, 20 layers (960 angles), 64 parameter sets,
+    complex64 adjoint gradients; seeded (set, angle) pairs against central differences
+    (h=1e-3) of the complex128 energy (per-gate FP64 kernels, pinned to the oracle and
+    the reference's parameter-shift gradients at small n by the tests above)."""
+    n, layers, B = 24, 20, 64
+    a = adjoint.Ansatz(n, layers)
+    th = torch.tensor(numpy.random.default_rng(2025).uniform(0, 2 * numpy.pi, (B, a.nparams)), device="cuda")
+    e, g = adjoint.energy_and_grad(th, a, torch.complex64)
+    assert e.shape == (B,) and g.shape == (B, a.nparams)
+    assert torch.all(torch.isfinite(g))
+    rng = numpy.random.default_rng(31)
+    pairs = [(int(rng.integers(B)), int(j)) for j in rng.choice(a.nparams, 6, replace=False)]
+    pairs += [(0, 0), (B - 1, a.nparams - 1)]
+    for b, j in pairs:
+        tp, tm = th[b:b + 1].clone(), th[b:b + 1].clone()
+        tp[0, j] += 1e-3
+        tm[0, j] -= 1e-3
+        with torch.no_grad():
+            ep = adjoint.SumZExpectation.apply(tp, a, torch.complex128)
+            em = adjoint.SumZExpectation.apply(tm, a, torch.complex128)
+        fd = float((ep - em).item() / 2e-3)
+        assert abs(g[b, j].item() - fd) < 1e-5 + 1e-3 * abs(fd), (b, j, g[b, j].item(), fd)
+    with torch.no_grad():
+        e128 = adjoint.SumZExpectation.apply(th[:2].clone(), a, torch.complex128)
+    numpy.testing.assert_allclose(e[:2].cpu().numpy(), e128.cpu().numpy(), atol=2e-5)

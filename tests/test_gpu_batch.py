@@ -58,3 +58,34 @@ def test_streamed_circuits_many_segments_match_oracle():
             assert err < 2e-5, (i, n, err)
     finally:
         b.close()
+
+
+def test_config4_list_seeded_subset_matches_oracle():
+    """The benchmark's own list (4096 circuits, n ~ U[8,20], depth ~ U[20,100], seed 4096)
+    in one launch; a seeded subset of 24 circuits, covering every n from 8 to 20
+    (n > 14 streamed), against the oracle."""
+    import torch
+
+    circs, feeds, sizes = batch.random_batch(4096, seed=4096)
+    b = batch.CircuitBatch(circs, feeds, sizes)
+    stream = torch.cuda.Stream()
+    rng = numpy.random.default_rng(404)
+    pick = []
+    for n in range(8, 21):
+        cands = [i for i, s in enumerate(sizes) if s == n]
+        pick.append(int(rng.choice(cands)))
+    pick += [int(i) for i in rng.choice(len(sizes), 11, replace=False)]
+    try:
+        b.run(stream.cuda_stream)
+        stream.synchronize()
+        for i in pick:
+            n = sizes[i]
+            want = sv.make_state(n, [[q] for q in range(n)], feeds[i])
+            for g in circs[i]:
+                want = sv.kronselect_dot(g, want, n)
+            err = numpy.max(numpy.abs(b.state(i) - want))
+            assert err < 2e-5, (i, n, err)
+        lat = b.latencies_ns()
+        assert lat.shape == (4096,) and numpy.all(lat > 0)
+    finally:
+        b.close()

@@ -5,9 +5,13 @@ state of that size on the host:
   backend: the fused complex64 state against the complex128 per-gate state (both on
   the device; the per-gate path is pinned to the reference and the oracle at smaller
   sizes), infidelity <= 1e-6 (the metric's bound) and the norm (5e-4: see below);
-* QFT + Grover at n=32 complex64 (fused) and n=31 complex128 (per-gate, 32 GiB each):
-  the marked probability and every single-qubit marginal against Grover's closed form
-  (relative 1e-4 for complex64, 1e-10 for complex128), and the norm.
+* the same brickwork followed by its inverse (every gate's adjoint, in reverse order)
+  returns to |0...0>: a round trip that involves no other GPU path, at full size, for
+  the fused complex64 path (fidelity 1 - 1e-6) and the complex128 per-gate path (1e-12);
+* QFT + 8 Grover iterations (config 3's circuit) at n=32 complex64 (fused) and n=31
+  complex128 (per-gate, 32 GiB each): the marked probability and every single-qubit
+  marginal against Grover's closed form (relative 1e-4 for complex64, 1e-10 for
+  complex128), and the norm.
 """
 import ctypes
 
@@ -47,9 +51,42 @@ def test_brickwork_n28_fused_matches_fp64_per_gate_path():
         plain.close()
 
 
+def _inverse(gate):
+    """The adjoint of one kron dictionary: every entry's conjugate transpose (CMat and
+    SwapMat entries of this workload are real symmetric or permutations)."""
+    out = {}
+    for key, m in gate.items():
+        out[key] = m if getattr(m, "_kron_struct", None) in (2, 3) else numpy.conj(numpy.asarray(m)).T
+    return out
+
+
+@pytest.mark.parametrize("statetype,tol", [(numpy.complex64, 1e-6), (numpy.complex128, 1e-12)])
+def test_brickwork_n28_round_trip_returns_to_zero_state(statetype, tol):
+    n = 28
+    gl = circuits.brickwork(n, 40, seed=1234)
+    for g in gl:  # the workload's CMat entries hold Z or SwapMat(1): self-inverse
+        for m in g.values():
+            if getattr(m, "_kron_struct", None) == 2:
+                assert getattr(m.m, "_kron_struct", None) == 3 or numpy.allclose(m.m, numpy.diag([1, -1]))
+    st = GpuBackend.make_state(n, [], [], statetype=statetype, fusion=statetype == numpy.complex64)
+    try:
+        for g in gl:
+            st.kronselect_dot(g)
+        for g in reversed(gl):
+            st.kronselect_dot(_inverse(g))
+        norm2 = st.total_prob()
+        a0 = st.get_relative_range(0, 1)[0]
+        probe = st.get_relative_range(1, 1 << 12)
+    finally:
+        st.close()
+    fidelity = abs(a0) ** 2 / norm2
+    assert 1.0 - fidelity < tol, 1.0 - fidelity
+    assert numpy.max(numpy.abs(probe)) < (1e-4 if statetype == numpy.complex64 else 1e-7)
+
+
 @pytest.mark.parametrize("n,statetype,rtol", [(32, numpy.complex64, 1e-4), (31, numpy.complex128, 1e-10)])
 def test_grover_full_size_closed_form(n, statetype, rtol):
-    iterations = 2
+    iterations = 8
     gl, marked = circuits.grover_gates(n, iterations, seed=7)
     st = GpuBackend.make_state(n, [], [], statetype=statetype, fusion=statetype == numpy.complex64)
     try:

@@ -51,5 +51,15 @@ def test_static_scratch_probabilities_match_allocating_entry_point(statetype, at
         rc = _static_probs(lib, st, list(range(17)), d_out)
         assert rc == _native.QSV_ERR_INVALID
         assert b"at most 16" in lib.qsv_last_error(None)
+        # An output buffer that is not device memory of the current GPU is rejected
+        # before any launch (here: host memory).
+        host_out = numpy.zeros(16)
+        q = (ctypes.c_int * 4)(0, 1, 2, 3)
+        dtype = 0 if st.statetype == numpy.complex64 else 1
+        rc = lib.qsv_probabilities_static(ctypes.c_void_p(st.device_ptr()), st.n, dtype, 4, q,
+                                          host_out.ctypes.data_as(ctypes.c_void_p), None)
+        assert rc == _native.QSV_ERR_INVALID
+        assert b"not device memory" in lib.qsv_last_error(None) or b"not a CUDA pointer" in lib.qsv_last_error(None)
+        assert numpy.all(host_out == 0)
     finally:
         st.close()
