@@ -17,6 +17,7 @@ from __future__ import annotations
 import heapq
 import itertools
 import os
+from collections import OrderedDict
 from typing import Any, Callable, Dict, List, Mapping, Sequence, Set, Tuple, Type, Union
 
 import numpy
@@ -82,7 +83,13 @@ def run(*args: PipelineObject,
     if backend_constructor is None:
         backend_constructor = _default_backend()
 
-    frontier, graphnodes = get_deps(*args, feed=feed)
+    walk_key = (args, tuple(feed.keys()))
+    walk = _WALKS.get(walk_key)
+    if walk is not None:
+        _WALKS.move_to_end(walk_key)
+        frontier, graphnodes = walk.frontier, walk.graphnodes
+    else:
+        frontier, graphnodes = get_deps(*args, feed=feed)
     for qubit in frontier:
         if qubit not in fed_qubits and qubit.default is not None:
             if type(qubit.default) == int:  # noqa: E721
@@ -114,7 +121,16 @@ def run(*args: PipelineObject,
         feed_states = [kwargs["state"]]
 
     state = backend_constructor(n, feed_index_groups, feed_states, statetype=statetype)
-    return feed_forward(frontier, state, graphnodes)
+    if walk is not None:
+        return walk.replay(state, n)
+    if not _walk_is_structural(graphnodes):
+        return feed_forward(frontier, state, graphnodes)
+    acc = _RecordingFeeder(state, n)
+    run_graph(frontier, graphnodes, acc)
+    _WALKS[walk_key] = _Walk(frontier, graphnodes, acc.schedule)
+    if len(_WALKS) > _WALKS_MAX:
+        _WALKS.popitem(last=False)
+    return acc.state.get_state(), acc.classic_map
 
 
 def _truthy(v) -> bool:
@@ -218,6 +234,61 @@ class NodeFeeder(GraphAccumulator):
         if n_bits > 0 or bits is not None:
             self.classic_map[node] = bits
             self.n -= n_bits
+
+
+class _RecordingFeeder(NodeFeeder):
+    """A NodeFeeder that also records each node with the index groups it was given."""
+
+    def __init__(self, state, n: int):
+        super().__init__(state, n)
+        self.schedule: List[Tuple[PipelineObject, List[Sequence[int]]]] = []
+
+    def feed(self, qbitindex, node):
+        self.schedule.append((node, [qbitindex[q] for q in node.inputs]))
+        super().feed(qbitindex, node)
+
+
+# Compiled walks.  The executor's node order, and the global indices each node is given,
+# depend only on the graph's structure (qids, inputs, sinks, register sizes), not on the
+# state or the feeds' values, as long as every node keeps the base ``feed`` and
+# ``remap_index``.  ``run`` records the walk of a graph (keyed by its output nodes and
+# fed registers) and later runs of the same graph replay it: the same ``feed_indices``
+# calls in the same order, without re-deriving the order.  The most recent graphs are
+# kept (the entries hold references to their nodes).
+_WALKS_MAX = 32
+_WALKS: "OrderedDict[Any, _Walk]" = OrderedDict()
+
+
+def _walk_is_structural(graphnodes) -> bool:
+    base_feed, base_remap = PipelineObject.feed, PipelineObject.remap_index
+    return all(type(node).feed is base_feed and type(node).remap_index is base_remap for node in graphnodes)
+
+
+class _Walk:
+    def __init__(self, frontier, graphnodes, schedule):
+        self.frontier = frontier
+        self.graphnodes = graphnodes
+        self.schedule = schedule
+
+    def replay(self, state, n: int):
+        classic = {}
+        for node, groups in self.schedule:
+            if TRACE:
+                _trace_lib().qsv_trace_push(type(node).__name__.encode())
+            try:
+                n_bits, bits = node.feed_indices(state, groups, n)
+            finally:
+                if TRACE:
+                    _trace_lib().qsv_trace_pop()
+            if n_bits > 0 or bits is not None:
+                classic[node] = bits
+                n -= n_bits
+        return state.get_state(), classic
+
+
+def clear_compiled_walks() -> None:
+    """Forget the recorded walks (and release the graphs they reference)."""
+    _WALKS.clear()
 
 
 def feed_forward(frontier: Sequence[PipelineObject], state, graphnodes):

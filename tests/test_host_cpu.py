@@ -50,6 +50,44 @@ def test_graph_api_mirror_matches_reference_runs():
     assert run_scenarios(sv.OracleBackend.make_state) >= 40
 
 
+def test_replayed_walks_match_fresh_walks():
+    """run() records a graph's walk and replays it on later runs of the same graph: every
+    scenario run twice (first walk, replay) gives the goldens both times, and a graph
+    with a node that overrides ``feed`` is walked afresh every time."""
+    from qip_gb300 import pipeline
+
+    pipeline.clear_compiled_walks()
+    d, meta = load_npz("scenarios.npz")
+    api = api_ns()
+    for name, fn in SCENARIOS.items():
+        for r, (outs, feed, measured) in enumerate(fn(api)):
+            for rep in range(2):
+                o, classic = api.run(*outs, feed=feed, backend_constructor=sv.OracleBackend.make_state)
+                numpy.testing.assert_allclose(o, d[f"{name}_{r}_state"], rtol=0, atol=1e-12,
+                                              err_msg=f"{name}[{r}] run {rep}")
+                for j, node in enumerate(measured):
+                    val = classic[node]
+                    want = d[f"{name}_{r}_m{j}_p"]
+                    got = val[1] if meta[name][r]["measured"][j] == "topk" else val
+                    numpy.testing.assert_allclose(got, want, atol=1e-12)
+    assert len(pipeline._WALKS) > 0
+
+    class Tracing(api_mod.Qubit):
+        seen = 0
+
+        def feed(self, state, qbitindex, n):
+            Tracing.seen += 1
+            return super().feed(state, qbitindex, n)
+
+    q = api_mod.Qubit(n=2)
+    h = api_mod.H(q)
+    t = Tracing(h)
+    for _ in range(3):
+        o, _ = api_mod.run(t, feed={q: [0, 1, 0, 0]}, backend_constructor=sv.OracleBackend.make_state)
+    assert Tracing.seen == 3
+    numpy.testing.assert_allclose(o, [0.5, -0.5, 0.5, -0.5], atol=1e-15)
+
+
 def test_qft_negate_keyword_is_dropped_like_reference():
     # QubitOpWrapper forwards only construction-time kwargs, so QFFT's negate=True has
     # no effect and the circuit is the inverse DFT (matches the reference output).
