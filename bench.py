@@ -398,7 +398,8 @@ def run_ours(args):
         e2e_stats.update(s2.stats)
         s2.close()
         t5 = time.perf_counter()
-        stage_log[keep_plans].append((t1 - t0, t2 - t1, t3 - t2, t4 - t3, t5 - t4))
+        stage_log[keep_plans].append((t1 - t0, t2 - t1, t3 - t2, t4 - t3, t5 - t4,
+                                      s2.stats["readback_buffer_ms"] * 1e-3, s2.stats["readback_copy_ms"] * 1e-3))
         return out
 
     e2e_steps = max(1, min(args.steps, 3))
@@ -506,12 +507,12 @@ def stage_summary(rows, ngates):
     gate while submitting."""
     if not rows:
         return None
-    names = ("create", "submit", "drain", "readback", "close")
+    names = ("create", "submit", "drain", "readback", "close", "readback_buffer", "readback_copy")
     med = [statistics.median(r[i] for r in rows) * 1e3 for i in range(len(names))]
     out = {k: round(v, 3) for k, v in zip(names, med)}
     out["submit_us_per_gate"] = round(med[1] * 1e3 / ngates, 2)
     out["gc"] = "collector frozen over the setup objects; collection stays on"
-    out["readback_buffer"] = "pooled page-locked array (no first-touch faults after warm-up)"
+    out["readback_note"] = "pooled page-locked array (no first-touch faults after warm-up)"
     return out
 
 
@@ -813,6 +814,20 @@ def measure_adjoint(args):
                 bwd.append(e1.elapsed_time(e2) * 1e-3)
     g = thr.grad
     tf, tb = statistics.mean(fwd), statistics.mean(bwd)
+    # The same gradients on the CUDA-core segment kernels (one timed repetition), for scale.
+    thr2 = th.clone().requires_grad_(True)
+    s0, s1 = _events()
+    s2 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    s0.record()
+    e_seg = adjoint.SumZExpectation.apply(thr2, a, torch.complex64, "segmented")
+    s1.record()
+    e_seg.sum().backward()
+    s2.record()
+    s2.synchronize()
+    seg = {"forward_s": s0.elapsed_time(s1) * 1e-3, "backward_s": s1.elapsed_time(s2) * 1e-3}
+    seg["value"] = B / (seg["forward_s"] + seg["backward_s"])
+    seg["max_abs_grad_diff_vs_tensor"] = float((thr2.grad - g).abs().max())
     rng = numpy.random.default_rng(77)
     idx = sorted({0, a.nparams - 1, *(int(x) for x in rng.choice(a.nparams, 4, replace=False))})
     errs = []
@@ -832,6 +847,9 @@ def measure_adjoint(args):
                                "objective <sum Z>"},
         "forward_s": tf, "backward_s": tb, "backward_over_forward": tb / tf,
         "grad_components_per_s": B * a.nparams / (tf + tb),
+        "method": "tensor cores: 6-qubit blocks, per-set block images, correlation GEMM + FP64 walk per block",
+        "blocks": len(adjoint.tensor_core_plan(a).blocks), "cuda_core_segmented": seg,
+        "max_abs_grad": float(g.abs().max()),
         "fd_checked_angles": idx, "max_abs_err_vs_fd_c128": max(errs),
         "cpu_baseline": None, "cpu_baseline_note": "the reference has no gradient code (qip/backend.py:14-65)",
         "clocks": clk.summary()}

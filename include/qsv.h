@@ -290,6 +290,38 @@ int qsv_batch_segment_adjoint(void* psi, void* lam, int nsets, int n, int dtype,
                               const void* gates_dev, const void* mats_dagger, double* grads,
                               int grad_stride, void* stream);
 
+/* ---- adjoint gradients on the tensor cores ---------------------------------------------
+ * No reference counterpart (the reference has no gradients).  For complex64 batches of
+ * nsets states (13 <= n <= 34) of a circuit of rotations RY(theta) = exp(-i theta Y/2),
+ * RZ(theta) = exp(-i theta Z/2) and CNOTs, split by the caller into blocks of six qubits
+ * (a valid execution order of the circuit, e.g. the fusion planner's).
+ * block_qubits: 6 ascending qubit indices per block; block_ngates[b]: gates of block b;
+ * gates: 4 ints per gate, blocks one after another, each block's gates in execution
+ * order: kind (0 RY, 1 RZ, 2 CNOT), target qubit, control qubit (CNOT; else -1),
+ * parameter index (rotations; else -1).  The plan uploads its tables once.
+ * qsv_adjoint_forward: psi[s] <- U_blocks psi[s], each set's block matrices built on the
+ * device from its angles thetas[s * nparams + p] (device doubles) and applied as
+ * split-bf16 tensor-core products (as qsv_apply_blocks).
+ * qsv_adjoint_backward: psi = the final states, lam = H psi; for the blocks in reverse,
+ * one tensor-core correlation X = sum_g psi[g] lam[g]^+ over the other qubits gives every
+ * gradient of the block (dE/dtheta_j = Im Tr(P_j Q_j), Q walked through the block's gates
+ * in FP64), added to grads[s * grad_stride + p]; then psi, lam <- U^+ psi, U^+ lam.
+ * scratch: caller-owned device memory of qsv_adjoint_scratch_bytes (per-set images and
+ * correlations); psi, lam and scratch 256-byte aligned; work queued on `stream`.
+ * qsv_adjoint_status synchronises and reports a bounded device wait that gave up
+ * (QSV_ERR_TIMEOUT).  Errors: qsv_last_error(NULL). */
+typedef struct qsv_adjoint_plan qsv_adjoint_plan;
+int qsv_adjoint_plan_create(int n, int nblocks, const int* block_qubits, const int* block_ngates,
+                            const int* gates, qsv_adjoint_plan** out);
+int qsv_adjoint_plan_destroy(qsv_adjoint_plan* p);
+size_t qsv_adjoint_scratch_bytes(const qsv_adjoint_plan* p, int nsets);
+int qsv_adjoint_forward(qsv_adjoint_plan* p, void* psi, int nsets, const double* thetas, int nparams,
+                        void* scratch, size_t scratch_bytes, void* stream);
+int qsv_adjoint_backward(qsv_adjoint_plan* p, void* psi, void* lam, int nsets, const double* thetas,
+                         int nparams, double* grads, int grad_stride, void* scratch,
+                         size_t scratch_bytes, void* stream);
+int qsv_adjoint_status(qsv_adjoint_plan* p);
+
 /* ---- many small circuits in one persistent launch --------------------------------------
  * No reference counterpart (the reference runs one circuit per run() call).  A batch
  * object holds a gate table, a circuit table, per-qubit product-state feeds and the

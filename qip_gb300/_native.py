@@ -80,6 +80,16 @@ SIGNATURES = {
     "qsv_plan_launch": (ctypes.c_int, [_handle, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "qsv_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "qsv_inject_block_stall": (ctypes.c_int, [_handle, ctypes.c_uint64]),
+    "qsv_adjoint_plan_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p, ctypes.c_void_p]),
+    "qsv_adjoint_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "qsv_adjoint_scratch_bytes": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int]),
+    "qsv_adjoint_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "qsv_adjoint_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                            ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                            ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "qsv_adjoint_status": (ctypes.c_int, [ctypes.c_void_p]),
     "qsv_probabilities_static": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_int_p,
                                                 ctypes.c_void_p, ctypes.c_void_p]),
     "qsv_inner_product": (ctypes.c_int, [_handle, _handle, _c_double_p, _c_double_p]),

@@ -17,6 +17,16 @@ gates are grouped by at most 3 local bits and applied in registers to 8-amplitud
 items, one shared-memory pass per group.  Two state vectors
 per set (psi, lambda).  ``segmented=False`` runs the same algorithm one launch per gate.
 
+On the tensor cores (``method="tensor"``, the default for complex64 states of n >= 13):
+the gates are split into blocks of six qubits by the fusion planner.  Forward: per block,
+every set's 64x64 block matrix is built on the device from its angles and applied to all
+sets in one split-bf16 tensor-core launch.  Backward: per block (in reverse), one
+tensor-core GEMM correlates psi and lambda over the other qubits,
+X = sum_g psi[g] lambda[g]^+ (64x64 per set), and every gradient of the block follows
+from X by a walk through the block's gates in FP64 (dE/dtheta_j = Im Tr(P_j Q_j),
+Q <- U_j^+ Q U_j); then psi and lambda are un-computed by U^+ with two more block
+launches (``qsv_adjoint_forward`` / ``qsv_adjoint_backward``).
+
 There is no reference counterpart (the reference has no gradients); results are checked
 against central finite differences and the parameter-shift rule on the FP64 oracle and
 on the reference's own kernel (tests/golden).
@@ -260,23 +270,122 @@ def _scratch(B: int, device) -> torch.Tensor:
     return torch.empty(B * 4096, dtype=torch.float64, device=device)
 
 
+TC_MIN_QUBITS = 13  # a six-qubit block needs seven more qubits for a tensor-core tile
+
+
+class TensorCorePlan:
+    """The ansatz split into blocks of six qubits (the fusion planner's steps, each a run
+    of gates in a valid execution order; a step on fewer qubits gets identity qubits, the
+    lowest-index ones not in it) and the native plan built from it (``qsv_adjoint_*``)."""
+
+    def __init__(self, ansatz: Ansatz):
+        gates = ansatz.gates()
+        self.blocks = block_partition(ansatz)
+        qubits_flat, ngates, recs = [], [], []
+        for qs, step in self.blocks:
+            qubits_flat.extend(qs)
+            ngates.append(len(step))
+            for i in step:
+                kind, t, c, pi = gates[i]
+                recs.extend([kind, t, c, pi])
+        n = ansatz.n
+        lib = nat.load()
+        h = ctypes.c_void_p()
+        qb, ng, gr = nat.int_array(qubits_flat), nat.int_array(ngates), nat.int_array(recs)
+        _check(lib.qsv_adjoint_plan_create(n, len(self.blocks), nat.ip(qb), nat.ip(ng), nat.ip(gr), ctypes.byref(h)),
+               "adjoint_plan_create")
+        self.handle = h
+        self.nparams = ansatz.nparams
+
+    def scratch(self, nsets: int, device) -> torch.Tensor:
+        nbytes = int(nat.load().qsv_adjoint_scratch_bytes(self.handle, nsets))
+        return torch.empty(nbytes, dtype=torch.uint8, device=device)
+
+    def __del__(self):
+        try:
+            if self.handle:
+                nat.load().qsv_adjoint_plan_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def block_partition(ansatz: Ansatz) -> List[Tuple[Tuple[int, ...], List[int]]]:
+    """[(six qubits ascending, gate indices in execution order)] covering every gate of
+    the ansatz once: the fusion planner's steps at width 6 (whole list, wide beam), each
+    widened to six qubits by the lowest-index qubits it does not touch."""
+    from .fusion import BEAM_WIDE, LOOKAHEAD, LOOKAHEAD2, plan_indices
+
+    gates = ansatz.gates()
+    qmasks = [(1 << t) | ((1 << c) if c >= 0 else 0) for _, t, c, _ in gates]
+    steps, planned = plan_indices(qmasks, [1.0] * len(gates), 6, None, LOOKAHEAD, True, 0, LOOKAHEAD2, BEAM_WIDE)
+    if planned != len(gates):
+        raise RuntimeError("fusion planner left gates unplanned")
+    blocks = []
+    for step in steps:
+        qs = {q for i in step for q in (gates[i][1], gates[i][2]) if q >= 0}
+        for q in range(ansatz.n):
+            if len(qs) >= 6:
+                break
+            qs.add(q)
+        blocks.append((tuple(sorted(qs)), list(step)))
+    return blocks
+
+
+_TC_PLANS = {}
+
+
+def tensor_core_plan(ansatz: Ansatz) -> TensorCorePlan:
+    key = (ansatz.n, ansatz.layers)
+    if key not in _TC_PLANS:
+        _TC_PLANS[key] = TensorCorePlan(ansatz)
+    return _TC_PLANS[key]
+
+
+def _method(segmented, ansatz: Ansatz, cdtype) -> str:
+    """``segmented``: True / False (segment kernels / one launch per gate, CUDA cores),
+    a method name, or None: the tensor cores where they apply, else segments."""
+    if isinstance(segmented, str):
+        if segmented not in ("tensor", "segmented", "per_gate"):
+            raise ValueError("method must be 'tensor', 'segmented' or 'per_gate'")
+        if segmented == "tensor" and (cdtype != torch.complex64 or ansatz.n < TC_MIN_QUBITS):
+            raise ValueError("the tensor-core adjoint needs complex64 states of at least 13 qubits")
+        return segmented
+    if segmented is None:
+        return "tensor" if cdtype == torch.complex64 and ansatz.n >= TC_MIN_QUBITS else "segmented"
+    return "segmented" if segmented else "per_gate"
+
+
 class SumZExpectation(torch.autograd.Function):
     """E[b] = <psi(thetas[b])| sum_i Z_i |psi(thetas[b])> with adjoint gradients."""
 
     @staticmethod
-    def forward(ctx, thetas: torch.Tensor, ansatz: Ansatz, statetype=torch.complex64, segmented: bool = True):
+    def forward(ctx, thetas: torch.Tensor, ansatz: Ansatz, statetype=torch.complex64, segmented=None):
         if not thetas.is_cuda:
             raise ValueError("thetas must live on the CUDA device")
         cdtype, qdtype = _dtype(statetype)
-        U, Ud = gate_matrices(ansatz, thetas.detach(), cdtype)
-        lb = local_bits(cdtype)
-        psi = forward_states_segmented(ansatz, U, cdtype, qdtype, lb) if segmented else \
-            forward_states(ansatz, U, cdtype, qdtype)
-        lam = torch.empty_like(psi)
+        method = _method(segmented, ansatz, cdtype)
         B = thetas.shape[0]
+        lib = nat.load()
+        if method == "tensor":
+            plan = tensor_core_plan(ansatz)
+            th64 = thetas.detach().to(torch.float64).contiguous()
+            psi = torch.empty((B, 2 ** ansatz.n), dtype=cdtype, device=thetas.device)
+            tc_scratch = plan.scratch(B, thetas.device)
+            st = ctypes.c_void_p(_stream_ptr())
+            _check(lib.qsv_batch_reset(ctypes.c_void_p(psi.data_ptr()), B, ansatz.n, qdtype, st), "batch_reset")
+            _check(lib.qsv_adjoint_forward(plan.handle, ctypes.c_void_p(psi.data_ptr()), B,
+                                           ctypes.c_void_p(th64.data_ptr()), ansatz.nparams,
+                                           ctypes.c_void_p(tc_scratch.data_ptr()), tc_scratch.numel(), st),
+                   "adjoint_forward")
+            Ud = (plan, th64, tc_scratch)
+        else:
+            U, Ud = gate_matrices(ansatz, thetas.detach(), cdtype)
+            lb = local_bits(cdtype)
+            psi = forward_states_segmented(ansatz, U, cdtype, qdtype, lb) if method == "segmented" else \
+                forward_states(ansatz, U, cdtype, qdtype)
+        lam = torch.empty_like(psi)
         energies = torch.empty(B, dtype=torch.float64, device=thetas.device)
         scratch = _scratch(B, thetas.device)
-        lib = nat.load()
         _check(lib.qsv_batch_observable_sumz(ctypes.c_void_p(psi.data_ptr()), ctypes.c_void_p(lam.data_ptr()),
                                              B, ansatz.n, qdtype, ctypes.c_void_p(energies.data_ptr()),
                                              ctypes.c_void_p(scratch.data_ptr()), scratch.numel(),
@@ -284,18 +393,34 @@ class SumZExpectation(torch.autograd.Function):
         ctx.ansatz, ctx.qdtype = ansatz, qdtype
         ctx.buffers = (psi, lam, Ud, scratch)
         ctx.tdtype = thetas.dtype
-        ctx.segmented, ctx.lb = segmented, local_bits(cdtype, backward=True)
+        ctx.method, ctx.lb = method, local_bits(cdtype, backward=True)
         return energies.to(thetas.dtype)
 
     @staticmethod
     def backward(ctx, grad_e: torch.Tensor):
         psi, lam, Ud, scratch = ctx.buffers
         ctx.buffers = None
-        if ctx.segmented:
+        if ctx.method == "tensor":
+            grads = adjoint_sweep_tensor(ctx.ansatz, psi, lam, *Ud)
+        elif ctx.method == "segmented":
             grads = adjoint_sweep_segmented(ctx.ansatz, psi, lam, Ud, ctx.qdtype, ctx.lb)
         else:
             grads = adjoint_sweep(ctx.ansatz, psi, lam, Ud, scratch, ctx.qdtype)
         return (grad_e.to(torch.float64)[:, None] * grads).to(ctx.tdtype), None, None, None
+
+
+def adjoint_sweep_tensor(ansatz: Ansatz, psi, lam, plan: TensorCorePlan, th64, tc_scratch) -> torch.Tensor:
+    """Reverse sweep on the tensor cores; consumes psi and lambda.  Returns dE/dtheta
+    [B, P] float64 (waits for the device: the status of its bounded waits is checked)."""
+    lib = nat.load()
+    B, P = psi.shape[0], ansatz.nparams
+    grads = torch.zeros((B, P), dtype=torch.float64, device=psi.device)
+    _check(lib.qsv_adjoint_backward(plan.handle, ctypes.c_void_p(psi.data_ptr()), ctypes.c_void_p(lam.data_ptr()), B,
+                                    ctypes.c_void_p(th64.data_ptr()), P, ctypes.c_void_p(grads.data_ptr()), P,
+                                    ctypes.c_void_p(tc_scratch.data_ptr()), tc_scratch.numel(),
+                                    ctypes.c_void_p(_stream_ptr())), "adjoint_backward")
+    _check(lib.qsv_adjoint_status(plan.handle), "adjoint_status")
+    return grads
 
 
 def adjoint_sweep(ansatz: Ansatz, psi, lam, Ud, scratch, qdtype) -> torch.Tensor:
@@ -319,7 +444,7 @@ def adjoint_sweep(ansatz: Ansatz, psi, lam, Ud, scratch, qdtype) -> torch.Tensor
     return grads
 
 
-def energy_and_grad(thetas: torch.Tensor, ansatz: Ansatz, statetype=torch.complex64, segmented: bool = True):
+def energy_and_grad(thetas: torch.Tensor, ansatz: Ansatz, statetype=torch.complex64, segmented=None):
     """Convenience: (E [B], dE/dtheta [B, P]) through the autograd Function."""
     th = thetas.detach().clone().requires_grad_(True)
     e = SumZExpectation.apply(th, ansatz, statetype, segmented)

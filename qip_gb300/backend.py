@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes
 import random
+import time
 from typing import Callable, List, Mapping, Optional, Sequence, Tuple, Union
 
 import numpy
@@ -537,9 +538,13 @@ class GpuBackend(StateType):
         page faults; ``qip_gb300.hostbuf``), owned by the caller like the reference's
         returned state array."""
         self.flush()
+        t0 = time.perf_counter()
         out = hostbuf.empty(2 ** self.n, self.statetype)
+        t1 = time.perf_counter()
         self._check(self._lib.qsv_read_range(self._h, out.ctypes.data_as(ctypes.c_void_p), 0, out.shape[0]),
                     "get_state")
+        self.stats["readback_buffer_ms"] = (t1 - t0) * 1e3
+        self.stats["readback_copy_ms"] = (time.perf_counter() - t1) * 1e3
         return out
 
     def get_state_size(self) -> int:

@@ -1306,7 +1306,8 @@ int qsv_bounds_report(unsigned long long* count, unsigned long long* first_index
 #ifdef QSV_BOUNDS_CHECK
   cudaDeviceSynchronize();
   if (oob_take_core(count, first_index) || oob_take_fused(count, first_index) ||
-      oob_take_adjoint(count, first_index) || oob_take_circuits(count, first_index))
+      oob_take_adjoint(count, first_index) || oob_take_circuits(count, first_index) ||
+      oob_take_adjtc(count, first_index))
     return set_error(nullptr, QSV_ERR_CUDA, "reading the bounds words failed");
   return QSV_OK;
 #else

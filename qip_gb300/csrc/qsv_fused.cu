@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "qsv_internal.cuh"
+#include "qsv_tc.cuh"
 
 using namespace qsv;
 
@@ -41,7 +42,6 @@ namespace {
 constexpr int FB_M = 128;         // groups per tile (MMA M)
 constexpr int FB_THREADS = 256;   // 8 warps
 constexpr int FB_BATCH_BITS = 7;  // log2(FB_M)
-constexpr unsigned long long FB_WAIT_NS = 2000000000ull;  // 2 s per wait
 
 template <int KQ>
 struct FB {
@@ -115,157 +115,13 @@ struct BlockArgs {
   int* flag;            // status word
   uint64_t wait_ns;     // limit of each wait for a tile's products
   int stall_first;      // fault injection: the first such wait is on a barrier nothing arrives on
+  // Batches (the tensor-core adjoint): psi holds several states of set_amps amplitudes,
+  // each with its own matrix; state s's image is at wimg + s * img_stride bytes.  Tiles
+  // are numbered state by state, set_tiles per state (a power of two); 0: one state.
+  uint64_t set_tiles;
+  uint64_t set_amps;
+  uint64_t img_stride;
 };
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ uint64_t globaltimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ uint64_t make_smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)((lbo & 0x3FFFFu) >> 4) << 16;
-  d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
-  return d;                // base offset 0, no swizzle
-}
-
-// kind::f16 instruction descriptor: BF16 x BF16 -> F32, both operands K-major.
-__host__ __device__ constexpr uint32_t make_idesc(int m, int n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Returns false if the phase did not complete within limit_ns.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity,
-                                                  uint64_t limit_ns = FB_WAIT_NS) {
-  const uint64_t t0 = globaltimer();
-  while (!mbar_try_wait(bar, parity)) {
-    if (globaltimer() - t0 > limit_ns) return false;
-  }
-  return true;
-}
-
-__device__ __forceinline__ void tc_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void fence_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                       uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-
-__device__ __forceinline__ void tc_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-               : "memory");
-}
-
-template <int NREG>
-__device__ __forceinline__ void tmem_ld(uint32_t taddr, float* v);
-
-template <>
-__device__ __forceinline__ void tmem_ld<8>(uint32_t taddr, float* v) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-#pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-template <>
-__device__ __forceinline__ void tmem_ld<16>(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-template <>
-__device__ __forceinline__ void tmem_ld<32>(uint32_t taddr, float* v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-
-__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
-  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-  return *reinterpret_cast<uint32_t*>(&h);
-}
-
-// 256-bit global accesses (4 adjacent complex64 amplitudes, 32-byte aligned), streaming.
-__device__ __forceinline__ void ld_v8(const float2* p, float2* v) {
-  float f[8];
-  asm volatile("ld.global.cs.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=f"(f[0]), "=f"(f[1]), "=f"(f[2]), "=f"(f[3]), "=f"(f[4]), "=f"(f[5]), "=f"(f[6]), "=f"(f[7])
-               : "l"(p));
-#pragma unroll
-  for (int i = 0; i < 4; ++i) v[i] = make_float2(f[2 * i], f[2 * i + 1]);
-}
-__device__ __forceinline__ void st_v8(float2* p, const float* re, const float* im) {
-  asm volatile("st.global.cs.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(re[0]), "f"(im[0]), "f"(re[1]),
-               "f"(im[1]), "f"(re[2]), "f"(im[2]), "f"(re[3]), "f"(im[3])
-               : "memory");
-}
-
-// Splits 8 floats into bf16 hi/lo halves, packed 8 per uint4.
-__device__ __forceinline__ void split8(const float* x, uint4& hi, uint4& lo) {
-  float h[8], l[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const float hv = __bfloat162float(__float2bfloat16_rn(x[i]));
-    h[i] = hv;
-    l[i] = x[i] - hv;
-  }
-  hi = make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
-  lo = make_uint4(pack_bf16(l[0], l[1]), pack_bf16(l[2], l[3]), pack_bf16(l[4], l[5]), pack_bf16(l[6], l[7]));
-}
 
 // MODE_DIRECT: each thread loads (b, 8 targets) items straight from global memory and
 // the epilogue stores TMEM rows straight back; coalesced when the 5 lowest address bits
@@ -305,13 +161,19 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   const int warp = tid >> 5;
   const int lane = tid & 31;
 
-  // W image (hi then lo) and the geometry tables into shared memory.
-  {
-    const uint4* src = a.wimg;
+  // W image (hi then lo) and the geometry tables into shared memory.  In a batch the
+  // image is that of the state the CTA's current tile belongs to (reloaded below when a
+  // tile of another state comes up, with no products in flight).
+  const int set_shift = a.set_tiles ? __ffsll((long long)a.set_tiles) - 1 : 0;
+  auto set_of = [&](uint64_t t) -> uint64_t { return a.set_tiles ? (t >> set_shift) : 0ull; };
+  auto load_w = [&](uint64_t set) {
+    const uint4* src = reinterpret_cast<const uint4*>(reinterpret_cast<const uint8_t*>(a.wimg) + set * a.img_stride);
     uint4* dst = reinterpret_cast<uint4*>(sW_hi);
     constexpr int NV = (2 * P::W_BYTES) / 16;
     for (int i = tid; i < NV; i += FB_THREADS) dst[i] = src[i];
-  }
+  };
+  uint64_t cur_set = set_of(blockIdx.x);
+  load_w(cur_set);
   for (int i = tid; i < FB_M; i += FB_THREADS) eb[i] = a.eb[i];
   for (int i = tid; i < P::T; i += FB_THREADS) {
     et[i] = a.et[i];
@@ -631,12 +493,29 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   };
   uint64_t tile = blockIdx.x;
   uint64_t base = 0;
+  // Amplitude offset of a tile: its state's start plus the tile's zero-inserted index.
+  auto tile_base = [&](uint64_t t) -> uint64_t {
+    if (!a.set_tiles) return qsv_insert_zeros(t, a.ptile, P::EBITS);
+    const uint64_t st = t >> set_shift;
+    return st * a.set_amps + qsv_insert_zeros(t - (st << set_shift), a.ptile, P::EBITS);
+  };
+  // Batches: before a tile of another state is written into the operand, its state's W
+  // replaces the current one (callers have no products in flight at that point; the
+  // operand_ready() that follows publishes W to the tensor cores).
+  auto switch_set = [&](uint64_t t) {
+    if (!a.set_tiles) return;
+    const uint64_t st = t >> set_shift;
+    if (st == cur_set) return;
+    cur_set = st;
+    load_w(st);
+  };
   if (tile < a.ntiles) {
-    base = qsv_insert_zeros(tile, a.ptile, P::EBITS);
+    base = tile_base(tile);
     load_tile(base);
   }
   if constexpr (!SHUF) {
     for (; tile < a.ntiles; tile += gridDim.x) {
+      switch_set(tile);
       write_a();
       operand_ready();
       issue_mma(tmem, bar_of(0));
@@ -645,7 +524,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
       const uint64_t next = tile + gridDim.x;
       uint64_t next_base = 0;
       if (next < a.ntiles) {
-        next_base = qsv_insert_zeros(next, a.ptile, P::EBITS);
+        next_base = tile_base(next);
         load_tile(next_base);
       }
       if (wait_products(0)) {
@@ -689,6 +568,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
       }
       __syncthreads();
       if (*abort_flag) break;
+      switch_set(tile);
       write_a();
       operand_ready();
       issue_mma(tmem + (uint32_t)(s * P::KD), bar_of(s));
@@ -696,7 +576,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
       const uint64_t next = tile + gridDim.x;
       uint64_t next_base = 0;
       if (next < a.ntiles) {
-        next_base = qsv_insert_zeros(next, a.ptile, P::EBITS);
+        next_base = tile_base(next);
         load_tile(next_base);
       }
       if (it > 0) epilogue(prev_base, tmem + (uint32_t)((s ^ 1) * P::KD));
@@ -1072,6 +952,29 @@ bool mode_applies(int k, int low, int mode) {
   return mode == MODE_SHUF && j >= 1 && j <= k - 1;
 }
 
+// One launch of the fused-block kernel: one CTA per SM (TMEM and shared memory allow no
+// more at k = 6), persistent over the tiles.
+template <int KQ, int MODE>
+cudaError_t launch_fb(const BlockArgs& a, float2* psi, cudaStream_t stream, int sm_count) {
+  using P = FB<KQ>;
+  constexpr int SMEM = MODE == MODE_STAGED ? P::SMEM : P::SMEM_DIRECT;
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_block_tc<KQ, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_block_tc<KQ, MODE>, FB_THREADS, SMEM);
+  if (per_sm < 1) per_sm = 1;
+  // Bound co-resident CTAs so their TMEM allocations always fit (512 columns per SM).
+  per_sm = std::min(per_sm, 512 / (MODE == MODE_SHUF ? P::TMEM_COLS2 : P::TMEM_COLS));
+  uint64_t grid = (uint64_t)std::max(1, sm_count) * per_sm;
+  if (grid > a.ntiles) grid = a.ntiles;
+  k_block_tc<KQ, MODE><<<(unsigned)grid, FB_THREADS, SMEM, stream>>>(psi, a);
+  return cudaGetLastError();
+}
+
 template <int KQ, int MODE>
 int launch_block_variant(qsv_state* s, const BlockArgs& args, float2* psi) {
   using P = FB<KQ>;
@@ -1083,21 +986,8 @@ int launch_block_variant(qsv_state* s, const BlockArgs& args, float2* psi) {
     a.stall_first = 1;
     s->inject_stall_ns = 0;
   }
-  constexpr int SMEM = MODE == MODE_STAGED ? P::SMEM : P::SMEM_DIRECT;
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_block_tc<KQ, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
-    if (e != cudaSuccess) return set_error(s, QSV_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(e));
-    configured = true;
-  }
-  int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_block_tc<KQ, MODE>, FB_THREADS, SMEM);
-  if (per_sm < 1) per_sm = 1;
-  // Bound co-resident CTAs so their TMEM allocations always fit (512 columns per SM).
-  per_sm = std::min(per_sm, 512 / (MODE == MODE_SHUF ? P::TMEM_COLS2 : P::TMEM_COLS));
-  uint64_t grid = (uint64_t)std::max(1, s->sm_count) * per_sm;
-  if (grid > a.ntiles) grid = a.ntiles;
-  k_block_tc<KQ, MODE><<<(unsigned)grid, FB_THREADS, SMEM, s->stream>>>(psi, a);
+  cudaError_t e = launch_fb<KQ, MODE>(a, psi, s->stream, s->sm_count);
+  if (e != cudaSuccess) return set_error(s, QSV_ERR_CUDA, "block_tc launch: %s", cudaGetErrorString(e));
   return check_launch(s, "block_tc");
 }
 
@@ -1294,6 +1184,69 @@ extern "C" int qsv_apply_blocks(qsv_state* s, int nblocks, const int* ks, const 
   }
   return QSV_OK;
 }
+
+// ---- batched launches for the tensor-core adjoint (qsv_adjtc.cu) ----------------------
+namespace qsv {
+struct FusedGeom {
+  BlockArgs a;
+};
+
+size_t fused_image_bytes(int k) { return image_bytes(k); }
+
+int fused_geom_create(int device, int n, int k, const int* qubits, FusedGeom** out, uint8_t* tperm_out) {
+  *out = nullptr;
+  if (k < 4 || k > 6 || n - k < FB_BATCH_BITS) return QSV_ERR_INVALID;
+  auto* g = new (std::nothrow) FusedGeom();
+  if (!g) return QSV_ERR_OOM;
+  int pos[8];
+  int low = 0;
+  for (int j = 0; j < k; ++j) {
+    if (qubits[j] < 0 || qubits[j] >= n) {
+      delete g;
+      return QSV_ERR_INVALID;
+    }
+    pos[j] = n - 1 - qubits[j];
+    if (pos[j] < FB_BATCH_BITS) low |= 1 << pos[j];
+  }
+  g->a = BlockArgs{};
+  g->a.k = k;
+  g->a.ntiles = 1ull << (n - k - FB_BATCH_BITS);
+  tile_geometry(k, pos, g->a, lookup_mode(device, k, low));
+  memcpy(tperm_out, g->a.tperm, 64);
+  *out = g;
+  return QSV_OK;
+}
+
+void fused_geom_destroy(FusedGeom* g) { delete g; }
+
+int fused_geom_launch_sets(const FusedGeom* g, float2* psi, int nsets, int n, const void* images,
+                           size_t img_stride, int* flag, cudaStream_t stream, int sm_count) {
+  BlockArgs a = g->a;
+  a.set_tiles = a.ntiles;
+  a.set_amps = 1ull << n;
+  a.ntiles = a.set_tiles * (uint64_t)nsets;
+  a.img_stride = img_stride;
+  a.wimg = static_cast<const uint4*>(images);
+  a.flag = flag;
+  a.wait_ns = FB_WAIT_NS;
+  a.stall_first = 0;
+  cudaError_t e;
+  switch (a.k * 4 + a.mode) {
+#define QSV_FB_CASE(KQ, MODE) \
+  case KQ * 4 + MODE:         \
+    e = launch_fb<KQ, MODE>(a, psi, stream, sm_count); \
+    break;
+    QSV_FB_CASE(4, MODE_DIRECT) QSV_FB_CASE(4, MODE_STAGED) QSV_FB_CASE(4, MODE_SHUF)
+    QSV_FB_CASE(5, MODE_DIRECT) QSV_FB_CASE(5, MODE_STAGED) QSV_FB_CASE(5, MODE_SHUF)
+    QSV_FB_CASE(6, MODE_DIRECT) QSV_FB_CASE(6, MODE_STAGED) QSV_FB_CASE(6, MODE_SHUF)
+#undef QSV_FB_CASE
+    default: return QSV_ERR_INVALID;
+  }
+  if (e != cudaSuccess) return QSV_ERR_CUDA;
+  count_launch();
+  return QSV_OK;
+}
+}  // namespace qsv
 
 namespace qsv {
 int oob_take_fused(unsigned long long* count, unsigned long long* first) {

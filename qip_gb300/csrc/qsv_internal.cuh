@@ -64,10 +64,23 @@ int oob_take_core(unsigned long long* count, unsigned long long* first);
 int oob_take_fused(unsigned long long* count, unsigned long long* first);
 int oob_take_adjoint(unsigned long long* count, unsigned long long* first);
 int oob_take_circuits(unsigned long long* count, unsigned long long* first);
+int oob_take_adjtc(unsigned long long* count, unsigned long long* first);
 int ensure_scratch(qsv_state* s, size_t bytes);
 int check_launch(qsv_state* s, const char* what);
 unsigned grid_for(const qsv_state* s, uint64_t work, unsigned per_block = QSV_THREADS,
                   unsigned waves = 16);
+
+// Fused-block geometry for batches of states (qsv_fused.cu), used by the tensor-core
+// adjoint: k target qubits in the caller's matrix order (first = most significant);
+// tperm_out[t'] is the caller's matrix index of kernel target index t' (64 bytes).
+struct FusedGeom;
+size_t fused_image_bytes(int k);
+int fused_geom_create(int device, int n, int k, const int* qubits, FusedGeom** out, uint8_t* tperm_out);
+void fused_geom_destroy(FusedGeom* g);
+// One launch over nsets states of 2^n complex64 amplitudes (psi); state s uses the W
+// image at images + s * img_stride.  A bounded wait that gives up sets *flag.
+int fused_geom_launch_sets(const FusedGeom* g, float2* psi, int nsets, int n, const void* images,
+                           size_t img_stride, int* flag, cudaStream_t stream, int sm_count);
 
 // Validates qubit indices (range, duplicates) and converts them to bit positions.
 int to_positions(qsv_state* s, int count, const int* qubits, int* pos_out,

@@ -111,3 +111,33 @@ def test_segment_device_tables_decode_to_the_circuit():
                     got = sv.kronselect_dot(mats[gi], got, n)
         assert sorted(seen) == list(range(len(mats)))
         numpy.testing.assert_allclose(got, want, atol=1e-12)
+
+
+def test_tensor_core_block_partition_is_a_valid_order():
+    """The six-qubit blocks of the tensor-core adjoint cover every gate once, and their
+    concatenated gate order applied by the oracle gives the circuit's state (the blocks
+    only move gates past gates on other qubits)."""
+    from qip_gb300 import adjoint
+
+    n, layers = 8, 3
+    a = adjoint.Ansatz(n, layers)
+    blocks = adjoint.block_partition(a)
+    order = [i for _, step in blocks for i in step]
+    assert sorted(order) == list(range(len(a.gates())))
+    gates = a.gates()
+    for qs, step in blocks:
+        assert len(qs) == 6 and list(qs) == sorted(set(qs))
+        for i in step:
+            _, t, c, _ = gates[i]
+            assert t in qs and (c < 0 or c in qs)
+    rng = numpy.random.default_rng(3)
+    th = rng.uniform(0, 2 * numpy.pi, a.nparams)
+    mats = circuits.ansatz_layers(n, layers, th)
+    want = numpy.zeros(2 ** n, complex)
+    want[0] = 1
+    got = want.copy()
+    for g in mats:
+        want = sv.kronselect_dot(g, want, n)
+    for i in order:
+        got = sv.kronselect_dot(mats[i], got, n)
+    numpy.testing.assert_allclose(got, want, atol=1e-12)

@@ -64,17 +64,51 @@ def test_segmented_sweeps_match_per_gate_sweeps(statetype, rtol):
     numpy.testing.assert_allclose(g1.cpu().numpy(), g0.cpu().numpy(), atol=rtol * scale * 10)
 
 
+@pytest.mark.parametrize("n,layers,B", [(14, 3, 4), (16, 4, 3)])
+def test_tensor_core_adjoint_matches_fp64_path(n, layers, B):
+    """Tensor-core adjoint (complex64, split-bf16 block products, tensor-core
+    correlations, FP64 walks) against the complex128 segment kernels: energies within
+    1e-5, gradients within 5e-5 (measured: 1.3e-6 and 8e-6 at n=14)."""
+    a = adjoint.Ansatz(n, layers)
+    th = torch.tensor(numpy.random.default_rng(n).uniform(0, 2 * numpy.pi, (B, a.nparams)), device="cuda")
+    e1, g1 = adjoint.energy_and_grad(th, a, torch.complex64, "tensor")
+    e0, g0 = adjoint.energy_and_grad(th, a, torch.complex128, "segmented")
+    assert len(adjoint.tensor_core_plan(a).blocks) > 1
+    numpy.testing.assert_allclose(e1.cpu().numpy(), e0.cpu().numpy(), atol=1e-5)
+    numpy.testing.assert_allclose(g1.cpu().numpy(), g0.cpu().numpy(), atol=5e-5)
+
+
+def test_tensor_core_adjoint_upstream_gradient_and_defaults():
+    """complex64 at n >= 13 takes the tensor cores by default; the upstream gradient
+    scales each set's row; a set with weight 0 gets zeros."""
+    n, layers = 13, 2
+    a = adjoint.Ansatz(n, layers)
+    th = torch.tensor(numpy.random.default_rng(4).uniform(0, 6, (3, a.nparams)), device="cuda", requires_grad=True)
+    e = adjoint.SumZExpectation.apply(th, a, torch.complex64)
+    w = torch.tensor([2.0, 0.0, -1.0], device="cuda", dtype=torch.float64)
+    (e * w).sum().backward()
+    _, g = adjoint.energy_and_grad(th.detach(), a, torch.complex64, "tensor")
+    numpy.testing.assert_allclose(th.grad[0].cpu().numpy(), 2 * g[0].cpu().numpy(), atol=1e-12)
+    numpy.testing.assert_allclose(th.grad[2].cpu().numpy(), -g[2].cpu().numpy(), atol=1e-12)
+    assert torch.all(th.grad[1] == 0)
+    with pytest.raises(ValueError):
+        adjoint.energy_and_grad(th.detach(), adjoint.Ansatz(8, 2), torch.complex64, "tensor")
+
+
 def test_config5_full_size_against_central_differences():
     """Config 5 at its own size: n=24, 20 layers (960 angles), 64 parameter sets,
-    complex64 adjoint gradients; seeded (set, angle) pairs against central differences
+    complex64 adjoint gradients (the default: tensor cores) and the CUDA-core segment
+    kernels; seeded (set, angle) pairs against central differences
     (h=1e-3) of the complex128 energy (per-gate FP64 kernels, pinned to the oracle and
     the reference's parameter-shift gradients at small n by the tests above)."""
     n, layers, B = 24, 20, 64
     a = adjoint.Ansatz(n, layers)
     th = torch.tensor(numpy.random.default_rng(2025).uniform(0, 2 * numpy.pi, (B, a.nparams)), device="cuda")
     e, g = adjoint.energy_and_grad(th, a, torch.complex64)
+    es, gs = adjoint.energy_and_grad(th, a, torch.complex64, "segmented")
     assert e.shape == (B,) and g.shape == (B, a.nparams)
     assert torch.all(torch.isfinite(g))
+    numpy.testing.assert_allclose(g.cpu().numpy(), gs.cpu().numpy(), atol=5e-6)
     rng = numpy.random.default_rng(31)
     pairs = [(int(rng.integers(B)), int(j)) for j in rng.choice(a.nparams, 6, replace=False)]
     pairs += [(0, 0), (B - 1, a.nparams - 1)]
@@ -87,6 +121,7 @@ def test_config5_full_size_against_central_differences():
             em = adjoint.SumZExpectation.apply(tm, a, torch.complex128)
         fd = float((ep - em).item() / 2e-3)
         assert abs(g[b, j].item() - fd) < 1e-5 + 1e-3 * abs(fd), (b, j, g[b, j].item(), fd)
+        assert abs(gs[b, j].item() - fd) < 1e-6 + 1e-4 * abs(fd), (b, j, gs[b, j].item(), fd)
     with torch.no_grad():
         e128 = adjoint.SumZExpectation.apply(th[:2].clone(), a, torch.complex128)
     numpy.testing.assert_allclose(e[:2].cpu().numpy(), e128.cpu().numpy(), atol=2e-5)
