@@ -246,6 +246,13 @@ int qsv_inner_product(qsv_state* a, qsv_state* b, double* re, double* im);
  * the adjoint-method differentiation of parameterised circuits. */
 /* Every state of the batch := |0...0>. */
 int qsv_batch_reset(void* psi, int nsets, int n, int dtype, void* stream);
+/* Per-gate, per-set 2x2 matrices of a rotation circuit, built on the device: gate g has
+ * kind_param[2g] = 0 (RY(theta) = exp(-i theta Y/2)), 1 (RZ(theta) = exp(-i theta Z/2)) or
+ * 2 (CNOT: X on its target) and kind_param[2g+1] = its parameter index; theta of set s is
+ * thetas[s * nparams + parameter] (device doubles).  U[(g * nsets + s) * 4 ..] row-major in
+ * the batch's dtype, Ud = U^+ likewise (all device memory). */
+int qsv_batch_rotation_matrices(const double* thetas, int nsets, int nparams, int ngates,
+                                const int* kind_param, int dtype, void* U, void* Ud, void* stream);
 /* psi[s] <- M_s psi[s] on `target` (qubit index), controlled by `control` (-1: none);
  * mats holds nsets row-major 2x2 matrices of the batch's dtype. */
 int qsv_batch_apply_1q(void* psi, int nsets, int n, int dtype, int target, int control,

@@ -90,6 +90,9 @@ SIGNATURES = {
                                             ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                             ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "qsv_adjoint_status": (ctypes.c_int, [ctypes.c_void_p]),
+    "qsv_batch_rotation_matrices": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                   ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                                   ctypes.c_void_p]),
     "qsv_probabilities_static": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_int_p,
                                                 ctypes.c_void_p, ctypes.c_void_p]),
     "qsv_inner_product": (ctypes.c_int, [_handle, _handle, _c_double_p, _c_double_p]),

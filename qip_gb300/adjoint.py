@@ -75,29 +75,29 @@ def _dtype(statetype):
     return torch.complex128, nat.QSV_C128
 
 
+_KIND_TABLES = {}
+
+
 def gate_matrices(ansatz: Ansatz, thetas: torch.Tensor, cdtype) -> Tuple[torch.Tensor, torch.Tensor]:
-    """Per-gate, per-set 2x2 matrices U and U^+ as [G, B, 4] tensors on the device."""
+    """Per-gate, per-set 2x2 matrices U and U^+ as [G, B, 4] tensors on the device, built
+    by ``qsv_batch_rotation_matrices`` from the angles."""
     B = thetas.shape[0]
     gates = ansatz.gates()
     G = len(gates)
-    th = thetas.to(torch.float64)
-    U = torch.zeros((G, B, 4), dtype=torch.complex128, device=thetas.device)
-    kinds = torch.tensor([g[0] for g in gates], device=thetas.device)
-    pidx = torch.tensor([max(g[3], 0) for g in gates], device=thetas.device)
-    ang = th[:, pidx].T  # [G, B]
-    c, s = torch.cos(ang / 2), torch.sin(ang / 2)
-    e = torch.exp(-0.5j * ang.to(torch.complex128))
-    ry = (kinds == RY)[:, None]
-    rz = (kinds == RZ)[:, None]
-    cx = (kinds == CNOT)[:, None]
-    zero = torch.zeros_like(c, dtype=torch.complex128)
-    one = torch.ones_like(c, dtype=torch.complex128)
-    U[:, :, 0] = torch.where(ry, c.to(torch.complex128), torch.where(rz, e, zero))
-    U[:, :, 1] = torch.where(ry, -s.to(torch.complex128), torch.where(cx, one, zero))
-    U[:, :, 2] = torch.where(ry, s.to(torch.complex128), torch.where(cx, one, zero))
-    U[:, :, 3] = torch.where(ry, c.to(torch.complex128), torch.where(rz, torch.conj(e), zero))
-    Ud = torch.stack([U[..., 0].conj(), U[..., 2].conj(), U[..., 1].conj(), U[..., 3].conj()], dim=-1)
-    return U.to(cdtype).contiguous(), Ud.to(cdtype).contiguous()
+    key = (ansatz.n, ansatz.layers, str(thetas.device))
+    if key not in _KIND_TABLES:
+        _KIND_TABLES[key] = torch.tensor([[k, max(p, 0)] for k, _, _, p in gates], dtype=torch.int32,
+                                         device=thetas.device)
+    kinds = _KIND_TABLES[key]
+    th = thetas.detach().to(torch.float64).contiguous()
+    U = torch.empty((G, B, 4), dtype=cdtype, device=thetas.device)
+    Ud = torch.empty_like(U)
+    _, qdtype = _dtype(cdtype)
+    _check(nat.load().qsv_batch_rotation_matrices(ctypes.c_void_p(th.data_ptr()), B, th.shape[1], G,
+                                                  ctypes.c_void_p(kinds.data_ptr()), qdtype,
+                                                  ctypes.c_void_p(U.data_ptr()), ctypes.c_void_p(Ud.data_ptr()),
+                                                  ctypes.c_void_p(_stream_ptr())), "batch_rotation_matrices")
+    return U, Ud
 
 
 def _stream_ptr() -> int:

@@ -644,6 +644,48 @@ int launch_check(const char* what) {
 
 }  // namespace
 
+// Per-gate, per-set 2x2 matrices of rotation circuits: gate g of kind 0 (RY(theta)),
+// 1 (RZ(theta)) or 2 (CNOT: X on the target) with angle thetas[s * nparams + param[g]];
+// U[(g * nsets + s) * 4 + ...] row-major and Ud = U^+, in the batch's precision.
+template <typename R>
+__global__ void k_batch_rotations(const double* __restrict__ thetas, int nsets, int nparams, int ngates,
+                                  const int2* __restrict__ kind_param, CT<R>* __restrict__ U,
+                                  CT<R>* __restrict__ Ud) {
+  const uint64_t total = (uint64_t)ngates * nsets;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const int g = (int)(i / nsets), s = (int)(i % nsets);
+    const int2 kp = kind_param[g];
+    double m[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // re/im of u00, u01, u10, u11
+    if (kp.x == 2) {
+      m[2] = 1.0;
+      m[4] = 1.0;
+    } else {
+      double sn, cs;
+      sincos(0.5 * thetas[(size_t)s * nparams + kp.y], &sn, &cs);
+      if (kp.x == 0) {
+        m[0] = cs;
+        m[2] = -sn;
+        m[4] = sn;
+        m[6] = cs;
+      } else {
+        m[0] = cs;
+        m[1] = -sn;
+        m[6] = cs;
+        m[7] = sn;
+      }
+    }
+    CT<R>* u = U + i * 4;
+    CT<R>* ud = Ud + i * 4;
+    for (int e = 0; e < 4; ++e) u[e] = {(R)m[2 * e], (R)m[2 * e + 1]};
+    // (U^+)[r][c] = conj(U[c][r])
+    ud[0] = {(R)m[0], (R)-m[1]};
+    ud[1] = {(R)m[4], (R)-m[5]};
+    ud[2] = {(R)m[2], (R)-m[3]};
+    ud[3] = {(R)m[6], (R)-m[7]};
+  }
+}
+
 extern "C" {
 
 int qsv_batch_reset(void* psi, int nsets, int n, int dtype, void* stream) {
@@ -658,6 +700,25 @@ int qsv_batch_reset(void* psi, int nsets, int n, int dtype, void* stream) {
   else
     return set_error(nullptr, QSV_ERR_INVALID, "unknown dtype %d", dtype);
   return launch_check("batch_reset");
+}
+
+int qsv_batch_rotation_matrices(const double* thetas, int nsets, int nparams, int ngates, const int* kind_param,
+                                int dtype, void* U, void* Ud, void* stream) {
+  if (!thetas || !kind_param || !U || !Ud || nsets < 1 || ngates < 0 || nparams < 0)
+    return set_error(nullptr, QSV_ERR_INVALID, "bad rotation-matrix arguments");
+  if (ngates == 0) return QSV_OK;
+  const uint64_t total = (uint64_t)ngates * nsets;
+  const unsigned grid = (unsigned)std::min<uint64_t>((total + QSV_THREADS - 1) / QSV_THREADS, (uint64_t)sms() * 8);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == QSV_C64)
+    k_batch_rotations<float><<<grid, QSV_THREADS, 0, st>>>(thetas, nsets, nparams, ngates, (const int2*)kind_param,
+                                                           (float2*)U, (float2*)Ud);
+  else if (dtype == QSV_C128)
+    k_batch_rotations<double><<<grid, QSV_THREADS, 0, st>>>(thetas, nsets, nparams, ngates, (const int2*)kind_param,
+                                                            (double2*)U, (double2*)Ud);
+  else
+    return set_error(nullptr, QSV_ERR_INVALID, "unknown dtype %d", dtype);
+  return launch_check("batch_rotations");
 }
 
 int qsv_batch_apply_1q(void* psi, int nsets, int n, int dtype, int target, int control, const void* mats,

@@ -42,7 +42,12 @@ constexpr int AKD = 2 * AT;         // 128: [Re | Im]
 constexpr int A_THREADS = 256;
 constexpr int CORR_K = 64;          // groups per correlation tile (the GEMM's K)
 constexpr int CORR_OP_BYTES = AKD * CORR_K * 2;  // one bf16 operand image (16 KiB)
-constexpr int CORR_SMEM = 4 * CORR_OP_BYTES + 64;  // A hi/lo, B hi/lo, mbarrier, TMEM slot
+constexpr int CORR_RAW_BYTES = 2 * AT * CORR_K * 8;  // one tile of psi and lambda, complex64 (64 KiB)
+constexpr int CORR_STAGES = 2;                        // tiles in flight ahead of the one multiplied
+constexpr int CORR_GROUPS = 8;                        // sets read concurrently
+constexpr int CORR_THREADS = 512;                     // 16 warps: one (t, 8 groups) run per thread
+// A hi/lo, B hi/lo, the raw stages, then the mbarrier, the TMEM slot and the abort flag.
+constexpr int CORR_SMEM = 4 * CORR_OP_BYTES + CORR_STAGES * CORR_RAW_BYTES + 64;
 constexpr int GATE_RY = 0, GATE_RZ = 1, GATE_CNOT = 2;
 
 // A gate of a block: kind, local target bit, local control bit (-1), parameter index.
@@ -173,8 +178,23 @@ __global__ void __launch_bounds__(A_THREADS)
 // (hi*lo + lo*hi + hi*hi) with FP32 accumulation in TMEM, a fresh accumulator per tile
 // (12 accumulating MMA steps).  Each thread adds its 64 entries of every tile into FP32
 // registers (round to nearest) and flushes them with FP64 atomics into corr[set][m][nn]
-// whenever its contiguous range of tiles moves to another set, and at the end.  Then
+// whenever its next tile belongs to another set, and at the end.  Then
 // X[b][a] = D[b][a] + D[64+b][64+a] + i (D[64+b][a] - D[b][64+a]).
+// Tiles go to CTAs grid-stride (tile = blockIdx.x + i * gridDim.x), so the CTAs running
+// at one time read neighbouring memory, as the fused block kernel does; a CTA then meets
+// every set once and flushes once per set.
+//
+// Loads: a tile is, for each state (psi, lambda) and local index t, a row of 64 groups
+// (512 contiguous bytes when the block has no target among address bits 0..5).  A warp
+// copies whole rows with cp.async (lane l: groups 2l, 2l+1, 16 bytes; 8-byte halves when
+// address bit 0 is a target), into a ring of CORR_STAGES raw tiles, CORR_STAGES tiles
+// ahead of the tile being multiplied.  Row (state, t) sits at ((state * 64 + t) * 512)
+// bytes with 16-byte chunk c at position c ^ (t & 7), so the transposing reads below (8
+// groups of one t per thread, consecutive t across lanes) hit distinct bank quads.
+//
+// Order: the CTAs form CORR_GROUPS groups; group q takes sets q, q + CORR_GROUPS, ... and
+// its CTAs stride through each set's tiles together, so concurrent reads stay close in
+// memory and a CTA flushes its sums once per set it visits.
 struct CorrArgs {
   const float2* psi;
   const float2* lam;
@@ -187,23 +207,31 @@ struct CorrArgs {
   const AdjBlockDev* blk;
 };
 
-__global__ void __launch_bounds__(A_THREADS, 1) k_adj_corr(const __grid_constant__ CorrArgs a) {
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+__global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr(const __grid_constant__ CorrArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA_hi = smem;
   uint8_t* sA_lo = smem + CORR_OP_BYTES;
   uint8_t* sB_hi = smem + 2 * CORR_OP_BYTES;
   uint8_t* sB_lo = smem + 3 * CORR_OP_BYTES;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + 4 * CORR_OP_BYTES);
+  uint8_t* raw = smem + 4 * CORR_OP_BYTES;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(raw + CORR_STAGES * CORR_RAW_BYTES);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
   __shared__ uint64_t dept[AT];
-  __shared__ uint64_t dlow[8];  // address offsets of the 3 lowest group bits
   __shared__ int tpos[AK];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  for (int i = tid; i < AT; i += A_THREADS) dept[i] = a.blk->dept[i];
+  for (int i = tid; i < AT; i += CORR_THREADS) dept[i] = a.blk->dept[i];
   if (tid < AK) tpos[tid] = a.blk->tpos[tid];
-  __syncthreads();
-  if (tid < 8) dlow[tid] = qsv_insert_zeros((uint64_t)tid, tpos, AK);
   if (tid == 0) {
     mbar_init(smem_u32(mbar), 1);
     *abort_flag = 0;
@@ -219,74 +247,80 @@ __global__ void __launch_bounds__(A_THREADS, 1) k_adj_corr(const __grid_constant
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const bool contig = tpos[0] > 2;  // group bits 0..2 are address bits 0..2
+  const bool pairs = tpos[0] > 0;  // groups 2l, 2l+1 are adjacent amplitudes
+  // Address offsets of this lane's groups 2l and 2l+1 within a tile (the tile's first
+  // group is a multiple of 64, so its offset adds).
+  const uint64_t dlane0 = qsv_insert_zeros((uint64_t)(2 * lane), tpos, AK);
+  const uint64_t dlane1 = qsv_insert_zeros((uint64_t)(2 * lane + 1), tpos, AK);
 
-  // Contiguous tile range of this CTA.
-  const uint64_t per = (a.ntiles + gridDim.x - 1) / gridDim.x;
-  const uint64_t t_begin = (uint64_t)blockIdx.x * per;
-  const uint64_t t_end = t_begin + per < a.ntiles ? t_begin + per : a.ntiles;
+  // This CTA's tiles: group q of the CTAs, rank within the group.
+  const uint64_t nsets = a.ntiles >> a.tile_shift;
+  const uint64_t tps = 1ull << a.tile_shift;
+  uint64_t ngr64 = nsets < (uint64_t)gridDim.x ? nsets : (uint64_t)gridDim.x;
+  if (ngr64 > (uint64_t)CORR_GROUPS) ngr64 = CORR_GROUPS;
+  const int ngr = (int)ngr64;
+  const int grp = blockIdx.x % ngr;
+  const uint64_t rank = blockIdx.x / ngr;
+  const uint64_t nctas = (gridDim.x - grp + ngr - 1) / ngr;
+  const uint64_t cnt = rank < tps ? (tps - rank + nctas - 1) / nctas : 0;  // tiles per visited set
+  const uint64_t nsg = (nsets - grp + ngr - 1) / ngr;                      // sets visited
+  const uint64_t total = cnt * nsg;
+  auto tile_of = [&](uint64_t i) -> uint64_t {
+    const uint64_t si = i / cnt;
+    return ((grp + si * ngr) << a.tile_shift) + rank + (i - si * cnt) * nctas;
+  };
 
-  // Items (t, j): t = local index, j = which 8 groups of the tile; item i -> t = i % 64,
-  // j = i / 64; thread tid holds items tid and tid + 256.
   const int it_t = tid & (AT - 1);
-  const int it_j0 = tid >> 6;  // 0..3, second item j0 + 4
-  float2 vp[2][8], vl[2][8];
-  const uint64_t lim = a.set_amps * (a.ntiles >> a.tile_shift);
-  auto load = [&](uint64_t tile) {
+  const int it_j = tid >> 6;  // which 8 groups of the tile
+  const uint64_t lim = a.set_amps * nsets;
+  const uint32_t raw_u32 = smem_u32(raw);
+  // Queue this warp's rows (state, t) = rows warp, warp + 8, ... of tile `tile` into `stage`.
+  auto fetch = [&](uint64_t tile, int stage) {
     const uint64_t set = tile >> a.tile_shift;
-    const uint64_t g0 = (tile & ((1ull << a.tile_shift) - 1)) << 6;
-#pragma unroll
-    for (int it = 0; it < 2; ++it) {
-      const uint64_t g = g0 + (uint64_t)(it_j0 + 4 * it) * 8;
-      const uint64_t base = set * a.set_amps + dept[it_t] + qsv_insert_zeros(g, tpos, AK);
-      if (contig) {
-        if (QSV_IN_BOUNDS(base + 7, lim)) {
-          ld_v8(a.psi + base, &vp[it][0]);
-          ld_v8(a.psi + base + 4, &vp[it][4]);
-          ld_v8(a.lam + base, &vl[it][0]);
-          ld_v8(a.lam + base + 4, &vl[it][4]);
-        }
+    const uint64_t gbase = qsv_insert_zeros((tile & (tps - 1)) << 6, tpos, AK);
+#pragma unroll 4
+    for (int r = warp; r < 2 * AT; r += CORR_THREADS / 32) {
+      const int state = r >> 6, t = r & (AT - 1);
+      const uint64_t idx = set * a.set_amps + dept[t] + gbase;  // the row's first amplitude
+      const float2* src = (state ? a.lam : a.psi) + idx;
+      const uint32_t dst = raw_u32 + (uint32_t)stage * CORR_RAW_BYTES + (uint32_t)(r * 512) +
+                           (uint32_t)((lane ^ (t & 7)) * 16);
+      if (pairs) {
+        if (QSV_IN_BOUNDS(idx + dlane0 + 1, lim)) cp_async16(dst, src + dlane0);
       } else {
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-          if (QSV_IN_BOUNDS(base + dlow[r], lim)) {
-            vp[it][r] = __ldcs(a.psi + base + dlow[r]);
-            vl[it][r] = __ldcs(a.lam + base + dlow[r]);
-          }
-        }
+        if (QSV_IN_BOUNDS(idx + dlane0, lim)) cp_async8(dst, src + dlane0);
+        if (QSV_IN_BOUNDS(idx + dlane1, lim)) cp_async8(dst + 8, src + dlane1);
       }
     }
   };
-  auto write_ops = [&]() {
-#pragma unroll
-    for (int it = 0; it < 2; ++it) {
-      const int j = it_j0 + 4 * it;
-      float re[8], im[8];
-      uint4 rh, rl, ih, il;
+  // Split this thread's runs (t, 8 groups) of stage `stage` into the bf16 operand images.
+  auto write_ops = [&](int stage) {
+    {
+      const int j = it_j;
       const uint32_t off_re = (uint32_t)j * (AKD * 16) + (uint32_t)it_t * 16;
       const uint32_t off_im = off_re + AT * 16;
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
-        re[r] = vp[it][r].x;
-        im[r] = vp[it][r].y;
-      }
-      split8(re, rh, rl);
-      split8(im, ih, il);
-      *reinterpret_cast<uint4*>(sA_hi + off_re) = rh;
-      *reinterpret_cast<uint4*>(sA_lo + off_re) = rl;
-      *reinterpret_cast<uint4*>(sA_hi + off_im) = ih;
-      *reinterpret_cast<uint4*>(sA_lo + off_im) = il;
+      for (int state = 0; state < 2; ++state) {
+        const uint8_t* row = raw + stage * CORR_RAW_BYTES + (state * AT + it_t) * 512;
+        float re[8], im[8];
 #pragma unroll
-      for (int r = 0; r < 8; ++r) {
-        re[r] = vl[it][r].x;
-        im[r] = vl[it][r].y;
+        for (int k = 0; k < 4; ++k) {
+          const float4 v = *reinterpret_cast<const float4*>(row + (((4 * j + k) ^ (it_t & 7)) * 16));
+          re[2 * k] = v.x;
+          im[2 * k] = v.y;
+          re[2 * k + 1] = v.z;
+          im[2 * k + 1] = v.w;
+        }
+        uint4 rh, rl, ih, il;
+        split8(re, rh, rl);
+        split8(im, ih, il);
+        uint8_t* hi = state ? sB_hi : sA_hi;
+        uint8_t* lo = state ? sB_lo : sA_lo;
+        *reinterpret_cast<uint4*>(hi + off_re) = rh;
+        *reinterpret_cast<uint4*>(lo + off_re) = rl;
+        *reinterpret_cast<uint4*>(hi + off_im) = ih;
+        *reinterpret_cast<uint4*>(lo + off_im) = il;
       }
-      split8(re, rh, rl);
-      split8(im, ih, il);
-      *reinterpret_cast<uint4*>(sB_hi + off_re) = rh;
-      *reinterpret_cast<uint4*>(sB_lo + off_re) = rl;
-      *reinterpret_cast<uint4*>(sB_hi + off_im) = ih;
-      *reinterpret_cast<uint4*>(sB_lo + off_im) = il;
     }
   };
   constexpr uint32_t idesc = make_idesc(AKD, AKD);
@@ -309,53 +343,70 @@ __global__ void __launch_bounds__(A_THREADS, 1) k_adj_corr(const __grid_constant
       tc_commit(smem_u32(mbar));
     }
   };
-  // This thread's TMEM quadrant (rows 32*q + lane) and column half h (64 columns).
+  // This thread's TMEM quadrant (rows 32*q + lane) and column quarter h (32 columns).
   const int q = warp & 3, h = warp >> 2;
-  const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 64);
-  float sum[64];
+  const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 32);
+  float sum[32];
 #pragma unroll
-  for (int i = 0; i < 64; ++i) sum[i] = 0.f;
+  for (int i = 0; i < 32; ++i) sum[i] = 0.f;
   auto flush = [&](uint64_t set) {
-    double* dst = a.corr + set * (uint64_t)(AKD * AKD) + (uint64_t)(q * 32 + lane) * AKD + h * 64;
+    double* dst = a.corr + set * (uint64_t)(AKD * AKD) + (uint64_t)(q * 32 + lane) * AKD + h * 32;
 #pragma unroll
-    for (int i = 0; i < 64; ++i) {
+    for (int i = 0; i < 32; ++i) {
       if (sum[i] != 0.f) atomicAdd(dst + i, (double)sum[i]);
       sum[i] = 0.f;
     }
   };
   uint32_t phase = 0;
   bool pending = false;
-  if (t_begin < t_end) load(t_begin);
-  for (uint64_t tile = t_begin; tile < t_end; ++tile) {
-    write_ops();
+  // Prologue: the first CORR_STAGES tiles in flight (one commit group per tile; empty
+  // groups past the end keep the count uniform).
+#pragma unroll
+  for (int k = 0; k < CORR_STAGES; ++k) {
+    if ((uint64_t)k < total) fetch(tile_of(k), k);
+    cp_async_commit();
+  }
+  int stage = 0;
+  for (uint64_t i = 0; i < total; ++i) {
+    const uint64_t tile = tile_of(i);
+    cp_async_wait<CORR_STAGES - 1>();  // this tile's group has landed (this thread's copies)
+    __syncthreads();                   // ... and every other thread's
+    write_ops(stage);
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     issue();
     pending = true;
-    if (tile + 1 < t_end) load(tile + 1);
-    if (mbar_wait_bounded(smem_u32(mbar), phase)) {
-      phase ^= 1u;
-      pending = false;
-    } else {
-      atomicExch(abort_flag, 1);
+    // The stage just consumed takes the tile CORR_STAGES ahead.
+    if (i + CORR_STAGES < total) fetch(tile_of(i + CORR_STAGES), stage);
+    cp_async_commit();
+    stage = stage + 1 == CORR_STAGES ? 0 : stage + 1;
+    // One warp waits for the products; the others wait at the barrier (no polling).
+    if (warp == 0) {
+      const bool done = mbar_wait_bounded(smem_u32(mbar), phase);
+      if (!done && lane == 0) atomicExch(abort_flag, 1);
     }
-    tc_fence_after();
+    phase ^= 1u;
+    pending = false;
     __syncthreads();
-    if (*abort_flag) break;
-#pragma unroll
-    for (int half = 0; half < 2; ++half) {
+    tc_fence_after();
+    if (*abort_flag) {
+      pending = true;
+      phase ^= 1u;
+      break;
+    }
+    {
       float d[32];
-      tmem_ld<32>(taddr + 32 * half, d);
+      tmem_ld<32>(taddr, d);
       tmem_ld_wait();
 #pragma unroll
-      for (int i = 0; i < 32; ++i) sum[32 * half + i] += d[i];
+      for (int k = 0; k < 32; ++k) sum[k] += d[k];
     }
     tc_fence_before();
-    const uint64_t set = tile >> a.tile_shift;
-    if (tile + 1 == t_end || ((tile + 1) >> a.tile_shift) != set) flush(set);
+    if ((i + 1) % cnt == 0) flush(tile >> a.tile_shift);
   }
+  cp_async_wait<0>();  // no copy may still target shared memory when the CTA exits
   __syncthreads();
   if (*abort_flag) {
     if (pending) mbar_wait_bounded(smem_u32(mbar), phase);
@@ -657,13 +708,13 @@ extern "C" int qsv_adjoint_backward(qsv_adjoint_plan* p, void* psi, void* lam, i
   ca.set_amps = 1ull << p->n;
   ca.flag = p->d_flag;
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adj_corr, A_THREADS, CORR_SMEM);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adj_corr, CORR_THREADS, CORR_SMEM);
   per_sm = std::max(1, std::min(per_sm, 4));  // 128 TMEM columns each
   uint64_t grid = (uint64_t)std::max(1, p->sm_count) * per_sm;
   if (grid > ca.ntiles) grid = ca.ntiles;
   for (int b = p->nblocks - 1; b >= 0; --b) {
     ca.blk = p->d_blocks + b;
-    k_adj_corr<<<(unsigned)grid, A_THREADS, CORR_SMEM, st>>>(ca);
+    k_adj_corr<<<(unsigned)grid, CORR_THREADS, CORR_SMEM, st>>>(ca);
     rc = check_stream_launch("adjoint correlation");
     if (rc) return rc;
     k_adj_walk<<<nsets, A_THREADS, AT * AT * sizeof(double2), st>>>(p->d_blocks + b, p->d_gates, thetas, nparams,

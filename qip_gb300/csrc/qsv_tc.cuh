@@ -150,17 +150,19 @@ __device__ __forceinline__ void st_v8(float2* p, const float* re, const float* i
                : "memory");
 }
 
-// Splits 8 floats into bf16 hi/lo halves, packed 8 per uint4.
+// Splits 8 floats into bf16 hi/lo halves (x = hi + lo, each rounded to nearest even),
+// packed 8 per uint4.  Pairs are converted with one packed conversion each; the hi
+// values come back to FP32 by shifting their bits (exact), so lo = x - hi is exact.
 __device__ __forceinline__ void split8(const float* x, uint4& hi, uint4& lo) {
-  float h[8], l[8];
+  uint32_t h[4], l[4];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const float hv = __bfloat162float(__float2bfloat16_rn(x[i]));
-    h[i] = hv;
-    l[i] = x[i] - hv;
+  for (int i = 0; i < 4; ++i) {
+    h[i] = pack_bf16(x[2 * i], x[2 * i + 1]);  // x[2i] in the low half
+    const float h0 = __uint_as_float(h[i] << 16), h1 = __uint_as_float(h[i] & 0xffff0000u);
+    l[i] = pack_bf16(x[2 * i] - h0, x[2 * i + 1] - h1);
   }
-  hi = make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
-  lo = make_uint4(pack_bf16(l[0], l[1]), pack_bf16(l[2], l[3]), pack_bf16(l[4], l[5]), pack_bf16(l[6], l[7]));
+  hi = make_uint4(h[0], h[1], h[2], h[3]);
+  lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
 }  // namespace

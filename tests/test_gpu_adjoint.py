@@ -125,3 +125,23 @@ def test_config5_full_size_against_central_differences():
     with torch.no_grad():
         e128 = adjoint.SumZExpectation.apply(th[:2].clone(), a, torch.complex128)
     numpy.testing.assert_allclose(e[:2].cpu().numpy(), e128.cpu().numpy(), atol=2e-5)
+
+
+@pytest.mark.parametrize("cdtype,atol", [(torch.complex128, 1e-15), (torch.complex64, 1e-7)])
+def test_device_rotation_matrices_match_the_circuit_generator(cdtype, atol):
+    """qsv_batch_rotation_matrices: U and U^+ of every gate and set against the matrices
+    of circuits.ansatz_layers (RY, RZ, and X for the CNOTs)."""
+    from qip_gb300 import circuits
+
+    n, layers, B = 5, 2, 3
+    a = adjoint.Ansatz(n, layers)
+    th = numpy.random.default_rng(0).uniform(0, 6, (B, a.nparams))
+    U, Ud = adjoint.gate_matrices(a, torch.tensor(th, device="cuda"), cdtype)
+    U, Ud = U.cpu().numpy(), Ud.cpu().numpy()
+    for b in range(B):
+        dicts = circuits.ansatz_layers(n, layers, th[b])
+        for g, d in enumerate(dicts):
+            (key, m), = d.items()
+            want = m.m if getattr(m, "_kron_struct", None) == 2 else m
+            numpy.testing.assert_allclose(U[g, b].reshape(2, 2), want, atol=atol)
+            numpy.testing.assert_allclose(Ud[g, b].reshape(2, 2), numpy.conj(want).T, atol=atol)
