@@ -334,8 +334,12 @@ int qsv_adjoint_status(qsv_adjoint_plan* p);
  * object holds a gate table, a circuit table, per-qubit product-state feeds and the
  * output states of every circuit in device memory.  qsv_circuits_run replays one
  * persistent launch (captured once into a CUDA graph on the given, non-default
- * stream): one CTA per SM takes circuits from an atomic counter (in table order, so
- * put long circuits first); n <= 14 circuits run entirely in shared memory. */
+ * stream), in clusters of CS CTAs (one CTA per SM; CS = 6, QSV_CIRCUIT_CLUSTER = 1..8
+ * overrides).  The leading circuits of the table with n >= 14 + log2(2 CS) run one per
+ * cluster (the cluster's CTAs share each segment's chunks), the rest one per CTA, each
+ * group taken in table order from its own atomic counter (so put the largest streamed
+ * circuits first, then the rest longest first); n <= 14 circuits run entirely in shared
+ * memory. */
 typedef struct qsv_circuits qsv_circuits;
 /* Gate record (48 bytes).  kind 0 DENSE1: 2x2 complex64 m on q0; 1 PHASE1: |1> of q0 gets
  * phase (m[0], m[1]); 2 X on q0; 3 CX: target q0, control q1; 4 CSWAP: control q0, swap

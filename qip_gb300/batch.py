@@ -4,8 +4,9 @@ Each circuit is a list of ``kronselect_dot`` dictionaries on n qubits (3 <= n <=
 with a product-state input (one 2-vector per qubit).  The gates are encoded into the
 fixed records of ``include/qsv.h`` (``qsv_gate_rec``): dense single-qubit matrices,
 single-qubit phases, X, controlled X and controlled Swap — the gate set of the batched
-workload (H, X, Rm, CNOT, C(Swap), Haar 2x2).  Circuits are ordered longest first for
-the device work queue; results come back in the caller's order.
+workload (H, X, Rm, CNOT, C(Swap), Haar 2x2).  Circuits are ordered for the device work
+queues (the largest streamed ones first, each on a whole cluster of CTAs; then the rest
+longest first); results come back in the caller's order.
 """
 from __future__ import annotations
 
@@ -23,6 +24,7 @@ CIRC_DTYPE = numpy.dtype([("n", "<i4"), ("ngates", "<i4"), ("gate_offset", "<i8"
 assert GATE_DTYPE.itemsize == 48 and CIRC_DTYPE.itemsize == 32
 
 DENSE1, PHASE1, X, CX, CSWAP = 0, 1, 2, 3, 4
+SMEM_QUBITS = 14  # circuits up to this size run whole in one CTA's shared memory
 
 
 def encode_gates(mats_list: Sequence[dict]) -> numpy.ndarray:
@@ -69,7 +71,11 @@ class CircuitBatch:
         count = len(circuits)
         encoded = [encode_gates(c) for c in circuits]
         cost = [float(2 ** sizes[i]) * max(1, len(encoded[i])) for i in range(count)]
-        self.order = sorted(range(count), key=lambda i: -cost[i])  # device slot -> caller index
+        # Device slot -> caller index: streamed circuits (n > 14) first, largest n first
+        # (the library runs the leading ones with n >= 14 + log2(2 * cluster size) on a
+        # whole cluster each), then the rest longest first.
+        self.order = sorted(range(count), key=lambda i: (0, -sizes[i], -cost[i]) if sizes[i] > SMEM_QUBITS
+                            else (1, 0, -cost[i]))
         self.slot_of = {c: s for s, c in enumerate(self.order)}
         circs = numpy.zeros(count, dtype=CIRC_DTYPE)
         gate_chunks, feed_chunks = [], []
