@@ -265,10 +265,20 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr(const __grid_const
   const uint64_t cnt = rank < tps ? (tps - rank + nctas - 1) / nctas : 0;  // tiles per visited set
   const uint64_t nsg = (nsets - grp + ngr - 1) / ngr;                      // sets visited
   const uint64_t total = cnt * nsg;
-  auto tile_of = [&](uint64_t i) -> uint64_t {
-    const uint64_t si = i / cnt;
-    return ((grp + si * ngr) << a.tile_shift) + rank + (i - si * cnt) * nctas;
+  // A position in this CTA's sequence (set, tile within the set, index in the set's
+  // run), advanced without divisions.
+  struct Pos {
+    uint64_t set, local, li;
   };
+  auto advance = [&](Pos& p) {
+    p.local += nctas;
+    if (++p.li == cnt) {
+      p.li = 0;
+      p.local = rank;
+      p.set += ngr;
+    }
+  };
+  auto tile_of = [&](const Pos& p) -> uint64_t { return (p.set << a.tile_shift) + p.local; };
 
   const int it_t = tid & (AT - 1);
   const int it_j = tid >> 6;  // which 8 groups of the tile
@@ -361,14 +371,15 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr(const __grid_const
   bool pending = false;
   // Prologue: the first CORR_STAGES tiles in flight (one commit group per tile; empty
   // groups past the end keep the count uniform).
+  Pos cu{(uint64_t)grp, rank, 0}, pf = cu;  // the tile being multiplied; the next fetch
 #pragma unroll
   for (int k = 0; k < CORR_STAGES; ++k) {
-    if ((uint64_t)k < total) fetch(tile_of(k), k);
+    if ((uint64_t)k < total) fetch(tile_of(pf), k);
+    advance(pf);
     cp_async_commit();
   }
   int stage = 0;
   for (uint64_t i = 0; i < total; ++i) {
-    const uint64_t tile = tile_of(i);
     cp_async_wait<CORR_STAGES - 1>();  // this tile's group has landed (this thread's copies)
     __syncthreads();                   // ... and every other thread's
     write_ops(stage);
@@ -379,7 +390,8 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr(const __grid_const
     issue();
     pending = true;
     // The stage just consumed takes the tile CORR_STAGES ahead.
-    if (i + CORR_STAGES < total) fetch(tile_of(i + CORR_STAGES), stage);
+    if (i + CORR_STAGES < total) fetch(tile_of(pf), stage);
+    advance(pf);
     cp_async_commit();
     stage = stage + 1 == CORR_STAGES ? 0 : stage + 1;
     // One warp waits for the products; the others wait at the barrier (no polling).
@@ -404,7 +416,9 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr(const __grid_const
       for (int k = 0; k < 32; ++k) sum[k] += d[k];
     }
     tc_fence_before();
-    if ((i + 1) % cnt == 0) flush(tile >> a.tile_shift);
+    const uint64_t set = cu.set;
+    advance(cu);
+    if (cu.li == 0) flush(set);  // the next tile belongs to another set (or none is left)
   }
   cp_async_wait<0>();  // no copy may still target shared memory when the CTA exits
   __syncthreads();
