@@ -283,7 +283,7 @@ class GpuBackend(StateType):
         ``CythonBackend.kronselect_dot``, ``qip/backend.py:112-116``)."""
         if input_offset or output_offset:
             raise ValueError("GpuBackend holds the whole state: offsets must be 0")
-        ops = decompose(mats)
+        ops = decompose(mats, copy=False)  # read-only from here on
         for op in ops:
             if op.qmask >> self.n:  # (a negative index already failed building the mask)
                 bad = [q for q in sorted(op.qubits) if not 0 <= q < self.n]

@@ -226,13 +226,15 @@ _CACHE_MAX = 4096
 _cache: Dict[Any, List[GateOp]] = {}
 
 
-def decompose(mats: Mapping[Any, Any]) -> List[GateOp]:
+def decompose(mats: Mapping[Any, Any], copy: bool = True) -> List[GateOp]:
     """Turn one ``kronselect_dot`` dictionary into a list of GateOps (in order).
 
     Graph ops hand the same matrices to every run (the reference caches them per node,
     ``qip/operators.py:17-18``), so results are cached by content: the dictionary's keys
     and each matrix's dtype, shape and bytes.  A hit returns fresh copies of the cached
-    ops (callers own what they get; the matrix arrays are shared and never written)."""
+    ops (callers own what they get; the matrix arrays are shared and never written);
+    ``copy=False`` returns the cached ops themselves, for callers that only read them
+    (the backend's gate path)."""
     key = []
     for indices in mats:
         if type(indices) not in (tuple, int):
@@ -247,7 +249,7 @@ def decompose(mats: Mapping[Any, Any]) -> List[GateOp]:
         key = tuple(key)
         hit = _cache.get(key)
         if hit is not None:
-            return [_clone(op) for op in hit]
+            return [_clone(op) for op in hit] if copy else hit
     ops = _decompose(mats)
     if key is not None:
         if len(_cache) >= _CACHE_MAX:
@@ -261,7 +263,7 @@ def decompose(mats: Mapping[Any, Any]) -> List[GateOp]:
             op.finite = op.mat is None or bool(numpy.all(numpy.isfinite(op.mat)))
             op.shared = {}  # per-template data the copies share (the backend's call arguments)
         _cache[key] = ops
-        return [_clone(op) for op in ops]
+        return [_clone(op) for op in ops] if copy else ops
     return ops
 
 

@@ -268,11 +268,17 @@ class _Walk:
     def __init__(self, frontier, graphnodes, schedule):
         self.frontier = frontier
         self.graphnodes = graphnodes
-        self.schedule = schedule
+        # Nodes with the base feed_indices (register joins and cuts) do nothing but
+        # record (0, 0); the replay records that without the call.
+        base = PipelineObject.feed_indices
+        self.schedule = [(node, groups, type(node).feed_indices is base) for node, groups in schedule]
 
     def replay(self, state, n: int):
         classic = {}
-        for node, groups in self.schedule:
+        for node, groups, noop in self.schedule:
+            if noop and not TRACE:
+                classic[node] = 0
+                continue
             if TRACE:
                 _trace_lib().qsv_trace_push(type(node).__name__.encode())
             try:
