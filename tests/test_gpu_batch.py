@@ -89,3 +89,37 @@ def test_config4_list_seeded_subset_matches_oracle():
         assert lat.shape == (4096,) and numpy.all(lat > 0)
     finally:
         b.close()
+
+
+@pytest.mark.parametrize("cluster", ["1", "2", "4", "8"])
+def test_cluster_sizes_match_oracle(cluster, monkeypatch):
+    """Every cluster size (QSV_CIRCUIT_CLUSTER, read when the batch is created) gives the
+    oracle's states: large streamed circuits shared by a cluster's CTAs (n=20 down to the
+    size's threshold, one of them without gates), smaller streamed ones and shared-memory
+    ones one CTA each."""
+    import torch
+
+    from qip_gb300.circuits import random_circuit, random_product_feed
+
+    monkeypatch.setenv("QSV_CIRCUIT_CLUSTER", cluster)
+    rng = numpy.random.default_rng(int(cluster) + 100)
+    circs, feeds, sizes = [], [], []
+    for n, depth in ((20, 40), (19, 0), (18, 30), (17, 25), (16, 20), (15, 20), (12, 30), (8, 10)):
+        circs.append(random_circuit(rng, n, depth))
+        feeds.append(random_product_feed(rng, n))
+        sizes.append(n)
+    b = batch.CircuitBatch(circs, feeds, sizes)
+    stream = torch.cuda.Stream()
+    try:
+        for _ in range(2):
+            b.run(stream.cuda_stream)
+        stream.synchronize()
+        for i, (gl, f, n) in enumerate(zip(circs, feeds, sizes)):
+            want = sv.make_state(n, [[q] for q in range(n)], f)
+            for g in gl:
+                want = sv.kronselect_dot(g, want, n)
+            err = numpy.max(numpy.abs(b.state(i) - want))
+            assert err < 2e-5, (cluster, i, n, err)
+        assert numpy.all(b.latencies_ns() > 0)
+    finally:
+        b.close()
