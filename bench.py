@@ -399,7 +399,8 @@ def run_ours(args):
         s2.close()
         t5 = time.perf_counter()
         stage_log[keep_plans].append((t1 - t0, t2 - t1, t3 - t2, t4 - t3, t5 - t4,
-                                      s2.stats["readback_buffer_ms"] * 1e-3, s2.stats["readback_copy_ms"] * 1e-3))
+                                      s2.stats["readback_buffer_ms"] * 1e-3, s2.stats["readback_copy_ms"] * 1e-3,
+                                      float(s2.stats["readback_page_locked"])))
         return out
 
     e2e_steps = max(1, min(args.steps, 3))
@@ -511,6 +512,11 @@ def stage_summary(rows, ngates):
     med = [statistics.median(r[i] for r in rows) * 1e3 for i in range(len(names))]
     out = {k: round(v, 3) for k, v in zip(names, med)}
     out["submit_us_per_gate"] = round(med[1] * 1e3 / ngates, 2)
+    out["readback_page_locked_steps"] = int(sum(r[7] for r in rows))
+    out["readback_copy_ms_each"] = [round(r[6] * 1e3, 1) for r in rows]
+    from qip_gb300 import hostbuf
+
+    out["host_buffers"] = dict(hostbuf.counts)
     out["gc"] = "collector frozen over the setup objects; collection stays on"
     out["readback_note"] = "pooled page-locked array (no first-touch faults after warm-up)"
     return out

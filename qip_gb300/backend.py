@@ -545,6 +545,7 @@ class GpuBackend(StateType):
                     "get_state")
         self.stats["readback_buffer_ms"] = (t1 - t0) * 1e3
         self.stats["readback_copy_ms"] = (time.perf_counter() - t1) * 1e3
+        self.stats["readback_page_locked"] = hostbuf.is_pooled(out)
         return out
 
     def get_state_size(self) -> int:

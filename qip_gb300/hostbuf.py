@@ -24,6 +24,9 @@ POOL_PER_SIZE = 2
 
 _lock = threading.Lock()
 _free: Dict[int, List[int]] = {}
+# How each pinned request was served: a pooled buffer reused, a new buffer allocated, or
+# ordinary numpy memory because the page-locked allocation failed.
+counts = {"reused": 0, "allocated": 0, "alloc_failed": 0}
 
 
 class _PinnedOwner:
@@ -51,6 +54,14 @@ def _release(ptr: int, nbytes: int) -> None:
     nat.load().qsv_host_free(ctypes.c_void_p(ptr))
 
 
+def is_pooled(arr) -> bool:
+    """True when ``arr`` is a view of one of this pool's page-locked buffers."""
+    base = arr
+    while base is not None and not isinstance(base, _PinnedOwner):
+        base = getattr(base, "base", None)
+    return base is not None
+
+
 def enabled() -> bool:
     return os.environ.get("QSV_PINNED_READBACK", "1") != "0"
 
@@ -64,9 +75,13 @@ def empty(count: int, dtype) -> numpy.ndarray:
     with _lock:
         lst = _free.get(nbytes)
         ptr = lst.pop() if lst else None
+        if ptr is not None:
+            counts["reused"] += 1
     if ptr is None:
         p = ctypes.c_void_p()
         if nat.load().qsv_host_alloc(nbytes, ctypes.byref(p)) != nat.QSV_OK or not p.value:
+            counts["alloc_failed"] += 1
             return numpy.empty(count, dtype=dtype)
+        counts["allocated"] += 1
         ptr = p.value
     return numpy.asarray(_PinnedOwner(ptr, nbytes, (count,), dtype))
