@@ -85,9 +85,20 @@ struct FB {
 // rounds (lane bits whose group bit is above address bit 4 <-> c bits 0..j-1) restore
 // 32 consecutive amplitudes per store.  All addresses and operand offsets are sums of
 // per-bit contributions listed in the tables below.
+//
+// Prefix mode (6-qubit blocks whose targets include address bits 0, 1 and 2, so 8
+// consecutive t are adjacent amplitudes): the products run transposed, D^T = W A^T (W in
+// the MMA's A slot with its rows interleaved [Re t, Im t], the tile in the B slot), so
+// TMEM lane 2t / 2t+1 holds Re / Im of output target t and column b holds group b.  A
+// warp's lanes then cover 16 consecutive targets of one group: after one shfl.xor that
+// pairs Re with Im, each store instruction writes two whole 128-byte runs (groups b and
+// b+1), where the direct epilogue (one group per lane) would touch 32 lines.  Loads take
+// 32-byte runs of 4 targets, 4 lanes per 128-byte line and 8 groups per warp.
 constexpr int MODE_DIRECT = 0;
 constexpr int MODE_STAGED = 1;
 constexpr int MODE_SHUF = 2;
+constexpr int MODE_PREFIX = 3;
+constexpr int NUM_MODES = 4;
 
 struct BlockArgs {
   uint64_t ntiles;
@@ -135,6 +146,8 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   using P = FB<KQ>;
   constexpr bool STAGED = MODE == MODE_STAGED;
   constexpr bool SHUF = MODE == MODE_SHUF;
+  constexpr bool PREFIX = MODE == MODE_PREFIX;
+  static_assert(!PREFIX || KQ == 6, "the prefix mode is built for 6-qubit blocks");
   constexpr int SMEM_USED = STAGED ? P::SMEM : P::SMEM_DIRECT;
   constexpr int RAW = STAGED ? P::RAW_BYTES : 0;
   constexpr int R = P::T / 2;  // shuffle mode: amplitudes per thread
@@ -203,6 +216,16 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
 
   auto slot = [&](int e) -> int { return e ^ ((int)swz[e >> 4] << 1); };
   auto dep = [&](int e) -> uint64_t { return (uint64_t)(e & (FB_M - 1)) + dephi[e >> FB_BATCH_BITS]; };
+  // Item it of this thread: group b and target chunk tg (targets tg*8 .. tg*8+7); lanes
+  // take consecutive groups.
+  auto item_b = [&](int it) -> int { return (it * FB_THREADS + tid) & (FB_M - 1); };
+  auto item_tg = [&](int it) -> int { return (it * FB_THREADS + tid) >> FB_BATCH_BITS; };
+  // Prefix mode: quarter-items of 4 targets (one 32-byte load).  Quarter u of this thread
+  // is group ((warp*8 + lane/4) | (u&1)*64), targets 4*q4 .. 4*q4+3 with
+  // q4 = (lane&3) | (u>>1)*4: four lanes read one 128-byte run of a group (8 whole lines
+  // per warp load), and the 8-byte operand stores of a warp fill 16 distinct bank slots.
+  auto quarter_b = [&](int u) -> int { return ((warp << 3) | (lane >> 2)) | ((u & 1) << 6); };
+  auto quarter_t4 = [&](int u) -> int { return (lane & 3) | ((u >> 1) << 2); };
 
   // Staged: thread u-th pair holds elements e, e+1 with e = 2*(u*256 + tid) (adjacent
   // amplitudes).  Direct: item it holds (b, targets tg*8..tg*8+7).
@@ -243,12 +266,17 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         const int e = 2 * (u * FB_THREADS + tid);
         if (QSV_IN_BOUNDS(base + dep(e) + 1, lim)) buf[u] = __ldcs(reinterpret_cast<const float4*>(psi + base + dep(e)));
       }
+    } else if constexpr (PREFIX) {
+#pragma unroll
+      for (int u = 0; u < 2 * P::ITEMS; ++u) {
+        const uint64_t off = base + dep(eb[quarter_b(u)]) + dep(et[4 * quarter_t4(u)]);
+        if (QSV_IN_BOUNDS(off + 3, lim)) ld_v8(psi + off, &buf2[u >> 1][(u & 1) * 4]);
+      }
     } else if (a.vec == 4) {
 #pragma unroll
       for (int it = 0; it < P::ITEMS; ++it) {
-        const int item = it * FB_THREADS + tid;
-        const int b = item & (FB_M - 1);
-        const int tg = item >> FB_BATCH_BITS;
+        const int b = item_b(it);
+        const int tg = item_tg(it);
         const uint64_t rb = base + dep(eb[b]);
 #pragma unroll
         for (int j = 0; j < 8; j += 4)
@@ -343,11 +371,31 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
           *reinterpret_cast<uint4*>(sA_lo + off_im) = il;
         }
       }
+      if constexpr (PREFIX) {
   #pragma unroll
-      for (int it = 0; it < (SHUF ? 0 : P::ITEMS); ++it) {
-        const int item = it * FB_THREADS + tid;
-        const int b = item & (FB_M - 1);
-        const int tg = item >> FB_BATCH_BITS;
+        for (int u = 0; u < 2 * P::ITEMS; ++u) {
+          const int b = quarter_b(u), q4 = quarter_t4(u);
+          float re[4], im[4];
+  #pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            re[j] = buf2[u >> 1][(u & 1) * 4 + j].x;
+            im[j] = buf2[u >> 1][(u & 1) * 4 + j].y;
+          }
+          uint2 rh, rl, ih, il;
+          split4(re, rh, rl);
+          split4(im, ih, il);
+          const int off_re = (q4 >> 1) * P::A_LBO + b * 16 + (q4 & 1) * 8;
+          const int off_im = off_re + (P::T / 8) * P::A_LBO;
+          *reinterpret_cast<uint2*>(sA_hi + off_re) = rh;
+          *reinterpret_cast<uint2*>(sA_lo + off_re) = rl;
+          *reinterpret_cast<uint2*>(sA_hi + off_im) = ih;
+          *reinterpret_cast<uint2*>(sA_lo + off_im) = il;
+        }
+      }
+  #pragma unroll
+      for (int it = 0; it < ((SHUF || PREFIX) ? 0 : P::ITEMS); ++it) {
+        const int b = item_b(it);
+        const int tg = item_tg(it);
         const int eb_ = eb[b];
         float re[8], im[8];
   #pragma unroll
@@ -376,19 +424,23 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
       // rounds relative to the accumulator's current size, so the corrections' roundings
       // stay at their own (2^-8 smaller) scale and only the main pass's 8 adds round at
       // full scale (against 24 the other way round; the FP32 accumulation rounds towards
-      // zero, which otherwise shrinks the norm by ~1.5e-6 per block).
+      // zero, which otherwise shrinks the norm by ~1.5e-6 per block).  The prefix mode
+      // multiplies transposed: W in the first operand slot (M = KD = 128 rows), the
+      // tile in the second (N = 128 groups); the instruction descriptor is the same.
+      auto mma = [&](uint32_t tile_img, uint32_t w_img, int s, uint32_t accumulate) {
+        const uint64_t td = make_smem_desc(tile_img + s * 2 * P::A_LBO, P::A_LBO, 128);
+        const uint64_t wd = make_smem_desc(w_img + s * 2 * P::W_LBO, P::W_LBO, 128);
+        if constexpr (PREFIX)
+          tc_mma(acc, wd, td, idesc, accumulate);
+        else
+          tc_mma(acc, td, wd, idesc, accumulate);
+      };
 #pragma unroll
-      for (int s = 0; s < KSTEPS; ++s)
-        tc_mma(acc, make_smem_desc(a_hi + s * 2 * P::A_LBO, P::A_LBO, 128),
-               make_smem_desc(w_lo + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, s > 0 ? 1u : 0u);
+      for (int s = 0; s < KSTEPS; ++s) mma(a_hi, w_lo, s, s > 0 ? 1u : 0u);
 #pragma unroll
-      for (int s = 0; s < KSTEPS; ++s)
-        tc_mma(acc, make_smem_desc(a_lo + s * 2 * P::A_LBO, P::A_LBO, 128),
-               make_smem_desc(w_hi + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, 1u);
+      for (int s = 0; s < KSTEPS; ++s) mma(a_lo, w_hi, s, 1u);
 #pragma unroll
-      for (int s = 0; s < KSTEPS; ++s)
-        tc_mma(acc, make_smem_desc(a_hi + s * 2 * P::A_LBO, P::A_LBO, 128),
-               make_smem_desc(w_hi + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, 1u);
+      for (int s = 0; s < KSTEPS; ++s) mma(a_hi, w_hi, s, 1u);
       tc_commit(barrier);
     }
   };
@@ -431,6 +483,29 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   #pragma unroll
         for (int c = 0; c < CHS; ++c)
           if (QSV_IN_BOUNDS(tbase + st_lw + a.st_reg[c], lim)) __stcs(dst + a.st_reg[c], make_float2(re[c], im[c]));
+      } else if constexpr (PREFIX) {
+        // Lane row 32q + lane = component (lane & 1) of target t; warp half h reads
+        // groups 64h .. 64h+63.  Pairs of lanes swap halves: the even lane keeps group
+        // b and the odd lane group b+1, each with its (Re, Im).
+        const int q = warp & 3;
+        const int h = warp >> 2;
+        const bool odd = lane & 1;
+        const uint64_t ot = dep(et[(q * 32 + lane) >> 1]);
+        const uint32_t lane_addr = acc + ((uint32_t)(q * 32) << 16);
+  #pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 32) {
+          float col[32];
+          tmem_ld<32>(lane_addr + (uint32_t)(h * 64 + c0), col);
+          tmem_ld_wait();
+  #pragma unroll
+          for (int i = 0; i < 32; i += 2) {
+            const float got = __shfl_xor_sync(0xffffffffu, odd ? col[i] : col[i + 1], 1);
+            const int b = h * 64 + c0 + i + (odd ? 1 : 0);
+            const uint64_t idx = tbase + dep(eb[b]) + ot;
+            if (QSV_IN_BOUNDS(idx, lim))
+              __stcs(psi + idx, odd ? make_float2(got, col[i + 1]) : make_float2(col[i], got));
+          }
+        }
       } else {
         const int q = warp & 3;
         const int h = warp >> 2;
@@ -635,14 +710,15 @@ size_t image_bytes(int k) {
 
 // Builds the hi/lo bf16 images of W = [[Ur, -Ui], [Ui, Ur]] in the K-major canonical
 // layout: element (row nn, col kk) at (kk/8)*(KD*16) + nn*16 + (kk%8)*2.  Rows and
-// columns follow the kernel target order: U is read at (tperm[t'], tperm[t]).
-void build_image(int k, const double* U, const uint8_t* tperm, uint8_t* out) {
+// columns follow the kernel target order: U is read at (tperm[t'], tperm[t]).  With
+// interleaved rows (the prefix mode) row nn is component nn & 1 of output t' = nn >> 1.
+void build_image(int k, const double* U, const uint8_t* tperm, uint8_t* out, bool interleaved = false) {
   const int T = 1 << k, KD = 2 * T;
   uint16_t* hi = reinterpret_cast<uint16_t*>(out);
   uint16_t* lo = reinterpret_cast<uint16_t*>(out + (size_t)KD * KD * 2);
   for (int nn = 0; nn < KD; ++nn) {
-    const int tp = tperm[nn % T];
-    const bool out_im = nn >= T;
+    const int tp = tperm[interleaved ? nn >> 1 : nn % T];
+    const bool out_im = interleaved ? (nn & 1) != 0 : nn >= T;
     for (int kk = 0; kk < KD; ++kk) {
       const int t = tperm[kk % T];
       const bool in_im = kk >= T;
@@ -848,6 +924,7 @@ void tile_geometry(int k, const int* user_pos, BlockArgs& a, int forced_mode) {
   a.mode = rule;
   if (forced_mode == MODE_DIRECT || forced_mode == MODE_STAGED) a.mode = forced_mode;
   if (forced_mode == MODE_SHUF && jl >= 1 && jl <= k - 1) a.mode = MODE_SHUF;
+  if (forced_mode == MODE_PREFIX && k == 6 && L >= 3) a.mode = MODE_PREFIX;
   int batch[FB_BATCH_BITS];
   for (int p = 0, nb = 0; nb < FB_BATCH_BITS; ++p)
     if (!((tmask >> p) & 1ull)) batch[nb++] = p;
@@ -948,6 +1025,7 @@ int lookup_mode(int dev, int k, int low) {
 
 bool mode_applies(int k, int low, int mode) {
   if (mode == MODE_DIRECT || mode == MODE_STAGED) return true;
+  if (mode == MODE_PREFIX) return k == 6 && (low & 7) == 7;  // targets on address bits 0, 1, 2
   const int j = __builtin_popcount((unsigned)low & 0x1Fu);
   return mode == MODE_SHUF && j >= 1 && j <= k - 1;
 }
@@ -996,6 +1074,9 @@ int launch_block(qsv_state* s, const BlockArgs& a, float2* psi) {
   switch (a.mode) {
     case MODE_STAGED: return launch_block_variant<KQ, MODE_STAGED>(s, a, psi);
     case MODE_SHUF: return launch_block_variant<KQ, MODE_SHUF>(s, a, psi);
+    case MODE_PREFIX:
+      if constexpr (KQ == 6) return launch_block_variant<KQ, MODE_PREFIX>(s, a, psi);
+      return set_error(s, QSV_ERR_INVALID, "prefix mode on a %d-qubit block", KQ);
     default: return launch_block_variant<KQ, MODE_DIRECT>(s, a, psi);
   }
 }
@@ -1078,7 +1159,8 @@ extern "C" int qsv_plan_create(qsv_state* s, int nblocks, const int* ks, const i
   }
   std::vector<uint8_t> host(total);
   for (int i = 0; i < nblocks; ++i)
-    build_image(ks[i], mats_c128 + mat_offs[(size_t)i], p->args[(size_t)i].tperm, host.data() + img_off[(size_t)i]);
+    build_image(ks[i], mats_c128 + mat_offs[(size_t)i], p->args[(size_t)i].tperm, host.data() + img_off[(size_t)i],
+                p->args[(size_t)i].mode == MODE_PREFIX);
   if (cudaMalloc(&p->d_images, total) != cudaSuccess) {
     cudaGetLastError();
     delete p;
@@ -1172,7 +1254,8 @@ extern "C" int qsv_apply_blocks(qsv_state* s, int nblocks, const int* ks, const 
   }
   uint8_t* himg = static_cast<uint8_t*>(s->h_img[slot]);
   for (int i = 0; i < nblocks; ++i)
-    build_image(ks[i], mats_c128 + mat_offs[(size_t)i], args[(size_t)i].tperm, himg + img_off[(size_t)i]);
+    build_image(ks[i], mats_c128 + mat_offs[(size_t)i], args[(size_t)i].tperm, himg + img_off[(size_t)i],
+                args[(size_t)i].mode == MODE_PREFIX);
   QSV_CUDA(s, cudaMemcpyAsync(s->d_images, himg, total, cudaMemcpyHostToDevice, s->stream));
   QSV_CUDA(s, cudaEventRecord(s->img_ev[slot], s->stream));
   s->img_busy[slot] = true;
@@ -1211,7 +1294,10 @@ int fused_geom_create(int device, int n, int k, const int* qubits, FusedGeom** o
   g->a = BlockArgs{};
   g->a.k = k;
   g->a.ntiles = 1ull << (n - k - FB_BATCH_BITS);
-  tile_geometry(k, pos, g->a, lookup_mode(device, k, low));
+  // Batched launches take their images from k_adj_images (rows not interleaved): a
+  // class tuned to the prefix mode runs on the built-in rule here.
+  const int mode = lookup_mode(device, k, low);
+  tile_geometry(k, pos, g->a, mode == MODE_PREFIX ? -1 : mode);
   memcpy(tperm_out, g->a.tperm, 64);
   *out = g;
   return QSV_OK;
@@ -1265,7 +1351,7 @@ extern "C" int qsv_set_block_mode(qsv_state* s, int k, int low_mask, int mode) {
   QSV_CHECK_HANDLE(s);
   if (k < 4 || k > 6 || low_mask < 0 || low_mask >= (1 << FB_BATCH_BITS) || __builtin_popcount(low_mask) > k)
     return set_error(s, QSV_ERR_INVALID, "bad placement class k=%d low_mask=%d", k, low_mask);
-  if (mode < -1 || mode > MODE_SHUF) return set_error(s, QSV_ERR_INVALID, "bad access mode %d", mode);
+  if (mode < -1 || mode >= NUM_MODES) return set_error(s, QSV_ERR_INVALID, "bad access mode %d", mode);
   std::lock_guard<std::mutex> lk(g_mode_mu);
   if (mode < 0) {
     g_modes.erase(mode_key(s->device, k, low_mask));
@@ -1300,7 +1386,8 @@ extern "C" int qsv_tune_blocks(qsv_state* s, int count, const int* ks, const int
   const size_t ibytes = image_bytes(6);
   std::vector<uint8_t> himg(ibytes);
   std::vector<double> ident;
-  if (cudaMalloc(&scratch, sbytes) != cudaSuccess || cudaMalloc(&dimg, 3 * ibytes) != cudaSuccess) {
+  // Identity images for k = 4, 5, 6 and the interleaved k = 6 image of the prefix mode.
+  if (cudaMalloc(&scratch, sbytes) != cudaSuccess || cudaMalloc(&dimg, 4 * ibytes) != cudaSuccess) {
     cudaGetLastError();
     rc = set_error(s, QSV_ERR_OOM, "tuning scratch allocation failed");
   }
@@ -1317,6 +1404,11 @@ extern "C" int qsv_tune_blocks(qsv_state* s, int count, const int* ks, const int
     build_image(k, ident.data(), idperm, himg.data());
     if (cudaMemcpy(dimg + (k - 4) * ibytes, himg.data(), image_bytes(k), cudaMemcpyHostToDevice) != cudaSuccess)
       rc = set_error(s, QSV_ERR_CUDA, "tuning image upload failed");
+    if (k == 6 && !rc) {
+      build_image(k, ident.data(), idperm, himg.data(), true);
+      if (cudaMemcpy(dimg + 3 * ibytes, himg.data(), image_bytes(k), cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = set_error(s, QSV_ERR_CUDA, "tuning image upload failed");
+    }
   }
   for (int i = 0; i < count && !rc; ++i) {
     const int k = ks[i], low = low_masks[i];
@@ -1327,8 +1419,8 @@ extern "C" int qsv_tune_blocks(qsv_state* s, int count, const int* ks, const int
     std::sort(tpos, tpos + k, [](int x, int y) { return x > y; });
     double best = -1.0;
     int best_mode = -1;
-    for (int mode = 0; mode < 3 && !rc; ++mode) {
-      out_ms[3 * i + mode] = -1.0;
+    for (int mode = 0; mode < NUM_MODES && !rc; ++mode) {
+      out_ms[NUM_MODES * i + mode] = -1.0;
       if (!mode_applies(k, low, mode)) continue;
       BlockArgs a{};
       a.k = k;
@@ -1336,7 +1428,7 @@ extern "C" int qsv_tune_blocks(qsv_state* s, int count, const int* ks, const int
       tile_geometry(k, tpos, a, mode);
       if (a.mode != mode) continue;
       a.flag = s->d_flag;
-      a.wimg = reinterpret_cast<const uint4*>(dimg + (k - 4) * ibytes);
+      a.wimg = reinterpret_cast<const uint4*>(dimg + (mode == MODE_PREFIX ? 3 : k - 4) * ibytes);
       rc = launch_args_on(s, a, scratch);
       if (!rc && cudaEventRecord(e0, s->stream) != cudaSuccess) rc = set_error(s, QSV_ERR_CUDA, "event record");
       for (int r = 0; r < reps && !rc; ++r) rc = launch_args_on(s, a, scratch);
@@ -1346,7 +1438,7 @@ extern "C" int qsv_tune_blocks(qsv_state* s, int count, const int* ks, const int
         rc = set_error(s, QSV_ERR_CUDA, "tuning timing failed");
       if (rc) break;
       const double per = (double)ms / reps;
-      out_ms[3 * i + mode] = per;
+      out_ms[NUM_MODES * i + mode] = per;
       if (best < 0.0 || per < best) {
         best = per;
         best_mode = mode;

@@ -165,4 +165,17 @@ __device__ __forceinline__ void split8(const float* x, uint4& hi, uint4& lo) {
   lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
+// The same for 4 floats (two bf16 pairs per half).
+__device__ __forceinline__ void split4(const float* x, uint2& hi, uint2& lo) {
+  uint32_t h[2], l[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    h[i] = pack_bf16(x[2 * i], x[2 * i + 1]);
+    const float h0 = __uint_as_float(h[i] << 16), h1 = __uint_as_float(h[i] & 0xffff0000u);
+    l[i] = pack_bf16(x[2 * i] - h0, x[2 * i + 1] - h1);
+  }
+  hi = make_uint2(h[0], h[1]);
+  lo = make_uint2(l[0], l[1]);
+}
+
 }  // namespace

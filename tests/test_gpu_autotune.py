@@ -8,7 +8,7 @@ import pytest
 
 import statevector as sv
 from qip_gb300 import GpuBackend, _native as nat, circuits, gates
-from qip_gb300.autotune import Autotuner, placement_class
+from qip_gb300.autotune import MODES, Autotuner, placement_class
 from qip_gb300.fusion import Block
 
 pytestmark = pytest.mark.gpu
@@ -16,13 +16,13 @@ pytestmark = pytest.mark.gpu
 C64 = numpy.complex64
 
 CLASSES = [(6, 0b0000000), (6, 0b1100000), (6, 0b0000011), (6, 0b0011000), (6, 0b0000110), (6, 0b1110000),
-           (6, 0b0011110), (6, 0b0111111), (6, 0b0001111), (5, 0b0001010), (5, 0b0011101), (4, 0b0011100),
-           (4, 0b0011110)]
+           (6, 0b0011110), (6, 0b0111111), (6, 0b0001111), (6, 0b0000111), (6, 0b1011111), (5, 0b0001010),
+           (5, 0b0011101), (5, 0b0000111), (4, 0b0011100), (4, 0b0011110)]
 
 
 def applicable(k, low):
     j = bin(low & 0x1F).count("1")
-    return [0, 1] + ([2] if 1 <= j <= k - 1 else [])
+    return [0, 1] + ([2] if 1 <= j <= k - 1 else []) + ([3] if k == 6 and low & 7 == 7 else [])
 
 
 def block_qubits(n, k, low):
@@ -70,6 +70,10 @@ def test_block_mode_arguments_are_checked():
         nat.check(lib.qsv_set_block_mode(st.handle, 3, 0, 0), st.handle, "set_block_mode")
     with pytest.raises(ValueError):
         nat.check(lib.qsv_set_block_mode(st.handle, 6, 0, 5), st.handle, "set_block_mode")
+    with pytest.raises(ValueError):
+        nat.check(lib.qsv_set_block_mode(st.handle, 6, 0b0000011, 3), st.handle, "set_block_mode")  # bit 2 free
+    with pytest.raises(ValueError):
+        nat.check(lib.qsv_set_block_mode(st.handle, 5, 0b0000111, 3), st.handle, "set_block_mode")  # k = 5
     st.close()
 
 
@@ -83,7 +87,7 @@ def test_tuner_records_the_fastest_mode_and_state_is_untouched():
     assert numpy.array_equal(st.get_state(), v)
     for k, low in CLASSES:
         times, best = tuner.measured(n, k, low)
-        ok = [m for m in range(3) if times[m] >= 0]
+        ok = [m for m in range(len(MODES)) if times[m] >= 0]
         assert sorted(ok) == applicable(k, low)
         assert best == min(ok, key=lambda m: times[m])
         assert tuner.block_ms(n, k, low) == times[best]

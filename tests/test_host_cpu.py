@@ -267,14 +267,14 @@ def test_incremental_plan_equals_full_plan():
 
 
 def _synthetic_tuner(cost):
-    from qip_gb300.autotune import Autotuner
+    from qip_gb300.autotune import MODES, Autotuner
 
     t = Autotuner()
     for k in (4, 5, 6):
         for low in range(128):
             if bin(low).count("1") <= k:
                 ms = cost(k, low)
-                t._ms[(20, k, low)] = ([ms, ms * 1.5, -1.0], 0)
+                t._ms[(20, k, low)] = ([ms, ms * 1.5] + [-1.0] * (len(MODES) - 2), 0)
     return t
 
 
