@@ -186,9 +186,11 @@ int qsv_block_matrices(int nblocks, const int* block_k, const int* block_qubits,
  * low_mask set <-> a target on address bit p, p < 7 (targets on higher bits do not
  * change how a tile is read).  Modes: 0 direct, 1 staged (shared-memory transpose),
  * 2 shuffle (warp exchanges; needs 1..k-1 targets on bits 0..4), 3 prefix (transposed
- * products; k = 6 with targets on bits 0, 1 and 2).  Choices are kept per device for
- * the life of the process and used by qsv_apply_blocks / qsv_plan_create (batched
- * adjoint launches use the built-in rule for classes tuned to the prefix mode).
+ * products; k = 6 with targets on bits 0, 1 and 2).  Without a recorded choice a class
+ * takes the built-in rule: direct when its low targets are bits 0..L-1 with L <= 2,
+ * prefix for k = 6 with L >= 4, else shuffle (or staged).  Choices are kept per device
+ * for the life of the process and used by qsv_apply_blocks / qsv_plan_create and the
+ * tensor-core adjoint.
  *
  * qsv_tune_blocks times every applicable mode of each class (reps launches after one
  * warm-up) on a zeroed scratch state of min(n, 26) qubits (the caller's state is not

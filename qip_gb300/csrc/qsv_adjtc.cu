@@ -57,6 +57,7 @@ struct AdjGate {
 
 struct AdjBlockDev {
   int first_gate, ngates;
+  int interleaved;     // W image rows interleaved [Re t', Im t'] (the block kernel's prefix mode)
   uint64_t dept[AT];   // address offset of local index t
   int tpos[AK];        // the block's bit positions, ascending (a group index gets zeros there)
   uint8_t tperm[64];   // fused kernel's target order -> local index
@@ -100,6 +101,7 @@ __global__ void __launch_bounds__(A_THREADS)
   __shared__ uint8_t tperm[64];
   const int tid = threadIdx.x;
   const int set = blockIdx.x;
+  const bool inter = blk->interleaved != 0;
   for (int i = tid; i < AT * AT; i += A_THREADS) U[i / AT][i % AT] = make_float2((i / AT) == (i % AT) ? 1.f : 0.f, 0.f);
   if (tid < 64) tperm[tid] = blk->tperm[tid];
   __syncthreads();
@@ -144,8 +146,8 @@ __global__ void __launch_bounds__(A_THREADS)
   // Items (nn, kk/8): 8 consecutive kk are one 16-byte row of a core matrix.
   for (int item = tid; item < AKD * (AKD / 8); item += A_THREADS) {
     const int nn = item % AKD, k8 = item / AKD;
-    const int tp = tperm[nn % AT];
-    const bool out_im = nn >= AT;
+    const int tp = tperm[inter ? nn >> 1 : nn % AT];
+    const bool out_im = inter ? (nn & 1) != 0 : nn >= AT;
     uint16_t h[8], l[8];
     for (int q = 0; q < 8; ++q) {
       const int kk = k8 * 8 + q;
@@ -596,6 +598,7 @@ extern "C" int qsv_adjoint_plan_create(int n, int nblocks, const int* block_qubi
     }
     p->geom.push_back(g);
     memcpy(B.tperm, tperm, 64);
+    B.interleaved = fused_geom_interleaved(g) ? 1 : 0;
     B.first_gate = gofs;
     B.ngates = block_ngates[b];
     for (int i = 0; i < block_ngates[b]; ++i) {

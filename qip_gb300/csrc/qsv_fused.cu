@@ -914,13 +914,17 @@ void tile_geometry(int k, const int* user_pos, BlockArgs& a, int forced_mode) {
   // stay coalesced only when those targets are the address prefix 0..L-1 with L <= 2
   // (L == j; t's lowest bits are exactly those, as tpos is in descending bit order, so
   // t..t+vec-1 are adjacent amplitudes and a warp reads 32 x vec contiguous
-  // amplitudes; a longer prefix spreads the lanes 2^L amplitudes apart).  Otherwise the
-  // shuffle mode handles up to k-1 of them and the staged mode the rest.
+  // amplitudes; a longer prefix spreads the lanes 2^L amplitudes apart).  A 6-qubit block
+  // with a prefix of 4 or more runs transposed (prefix mode; measured faster there than
+  // the direct and shuffle modes, and slower at L = 3).  Otherwise the shuffle mode
+  // handles up to k-1 of them and the staged mode the rest.
   int L = 0;
   while (L < k && tpos[k - 1 - L] == L) ++L;
   const int jl = __builtin_popcountll(tmask & 0x1Full);
   a.vec = L >= 2 ? 4 : (L == 1 ? 2 : 1);
-  const int rule = (jl == L && L <= 2) ? MODE_DIRECT : (jl <= k - 1 ? MODE_SHUF : MODE_STAGED);
+  const int rule = (jl == L && L <= 2) ? MODE_DIRECT
+                   : (k == 6 && L >= 4) ? MODE_PREFIX
+                                        : (jl <= k - 1 ? MODE_SHUF : MODE_STAGED);
   a.mode = rule;
   if (forced_mode == MODE_DIRECT || forced_mode == MODE_STAGED) a.mode = forced_mode;
   if (forced_mode == MODE_SHUF && jl >= 1 && jl <= k - 1) a.mode = MODE_SHUF;
@@ -1294,16 +1298,15 @@ int fused_geom_create(int device, int n, int k, const int* qubits, FusedGeom** o
   g->a = BlockArgs{};
   g->a.k = k;
   g->a.ntiles = 1ull << (n - k - FB_BATCH_BITS);
-  // Batched launches take their images from k_adj_images (rows not interleaved): a
-  // class tuned to the prefix mode runs on the built-in rule here.
-  const int mode = lookup_mode(device, k, low);
-  tile_geometry(k, pos, g->a, mode == MODE_PREFIX ? -1 : mode);
+  tile_geometry(k, pos, g->a, lookup_mode(device, k, low));
   memcpy(tperm_out, g->a.tperm, 64);
   *out = g;
   return QSV_OK;
 }
 
 void fused_geom_destroy(FusedGeom* g) { delete g; }
+
+bool fused_geom_interleaved(const FusedGeom* g) { return g->a.mode == MODE_PREFIX; }
 
 int fused_geom_launch_sets(const FusedGeom* g, float2* psi, int nsets, int n, const void* images,
                            size_t img_stride, int* flag, cudaStream_t stream, int sm_count) {
@@ -1324,7 +1327,7 @@ int fused_geom_launch_sets(const FusedGeom* g, float2* psi, int nsets, int n, co
     break;
     QSV_FB_CASE(4, MODE_DIRECT) QSV_FB_CASE(4, MODE_STAGED) QSV_FB_CASE(4, MODE_SHUF)
     QSV_FB_CASE(5, MODE_DIRECT) QSV_FB_CASE(5, MODE_STAGED) QSV_FB_CASE(5, MODE_SHUF)
-    QSV_FB_CASE(6, MODE_DIRECT) QSV_FB_CASE(6, MODE_STAGED) QSV_FB_CASE(6, MODE_SHUF)
+    QSV_FB_CASE(6, MODE_DIRECT) QSV_FB_CASE(6, MODE_STAGED) QSV_FB_CASE(6, MODE_SHUF) QSV_FB_CASE(6, MODE_PREFIX)
 #undef QSV_FB_CASE
     default: return QSV_ERR_INVALID;
   }

@@ -77,6 +77,9 @@ struct FusedGeom;
 size_t fused_image_bytes(int k);
 int fused_geom_create(int device, int n, int k, const int* qubits, FusedGeom** out, uint8_t* tperm_out);
 void fused_geom_destroy(FusedGeom* g);
+// True when the geometry's launches want W images with interleaved rows (row nn =
+// component nn & 1 of output nn >> 1, the prefix access mode).
+bool fused_geom_interleaved(const FusedGeom* g);
 // One launch over nsets states of 2^n complex64 amplitudes (psi); state s uses the W
 // image at images + s * img_stride.  A bounded wait that gives up sets *flag.
 int fused_geom_launch_sets(const FusedGeom* g, float2* psi, int nsets, int n, const void* images,

@@ -262,7 +262,7 @@ def test_tensor_core_block_matches_oracle(k):
 
 BLOCK_PLACEMENTS = [  # target bit positions below bit 7 (the rest sit at the top bits)
     (6, ()), (6, (5, 6)), (6, (0,)), (6, (0, 1)),  # direct
-    (6, (0, 1, 2, 3, 4, 5)), (6, (0, 1, 2, 3)),  # shuffle (prefix longer than 2)
+    (6, (0, 1, 2, 3, 4, 5)), (6, (0, 1, 2, 3)),  # prefix (transposed products; a prefix of 4 or more)
     (6, (4,)), (6, (3, 4)), (6, (1, 2)), (6, (0, 2)), (6, (4, 5, 6)), (6, (1, 2, 3, 4)),  # shuffle
     (6, (0, 1, 4, 5, 6)), (6, (2, 3, 4, 5, 6)), (5, (1, 3)), (5, (0, 2, 3, 4)), (4, (2, 3, 4)),
     (4, (1, 2, 3, 4)), (4, (0, 2, 3, 4)),  # staged (all four targets below bit 5, not a prefix)
@@ -271,7 +271,7 @@ BLOCK_PLACEMENTS = [  # target bit positions below bit 7 (the rest sit at the to
 
 @pytest.mark.parametrize("k,low", BLOCK_PLACEMENTS)
 def test_tensor_core_block_modes_match_oracle(k, low):
-    """Each access mode of the tensor-core block kernel (direct, shuffle, staged), with
+    """Each access mode of the tensor-core block kernel (direct, shuffle, staged, prefix), with
     the block's qubits in ascending, descending and shuffled matrix order."""
     n = 15
     rng = numpy.random.default_rng(100 * k + len(low))
