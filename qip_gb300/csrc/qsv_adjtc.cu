@@ -15,7 +15,7 @@
 //     Q_{j-1} = U_j^+ Q_j U_j,
 // over the block's gates j = m..1 (g runs over the 2^(n-6) groups of the other qubits,
 // A_j = U_m..U_{j+1}, psi_j = A_j^+ psi_out, lambda_j = A_j^+ lambda_out, so the sum
-// over groups is Tr(A_j P_j A_j^+ X) = Tr(P_j Q_j)).  k_adj_corr computes X as a real
+// over groups is Tr(A_j P_j A_j^+ X) = Tr(P_j Q_j)).  k_adj_corr_d computes X as a real
 // GEMM on the tensor cores (K = the groups), k_adj_walk walks Q through the block's gates
 // in FP64 and writes the gradients, then psi and lambda are un-computed by U^+ with two
 // more fused-block launches.  Every block's gradients cost one correlation pass and two
@@ -42,12 +42,8 @@ constexpr int AKD = 2 * AT;         // 128: [Re | Im]
 constexpr int A_THREADS = 256;
 constexpr int CORR_K = 64;          // groups per correlation tile (the GEMM's K)
 constexpr int CORR_OP_BYTES = AKD * CORR_K * 2;  // one bf16 operand image (16 KiB)
-constexpr int CORR_RAW_BYTES = 2 * AT * CORR_K * 8;  // one tile of psi and lambda, complex64 (64 KiB)
-constexpr int CORR_STAGES = 2;                        // tiles in flight ahead of the one multiplied
 constexpr int CORR_GROUPS = 8;                        // sets read concurrently
-constexpr int CORR_THREADS = 512;                     // 16 warps: one (t, 8 groups) run per thread
-// A hi/lo, B hi/lo, the raw stages, then the mbarrier, the TMEM slot and the abort flag.
-constexpr int CORR_SMEM = 4 * CORR_OP_BYTES + CORR_STAGES * CORR_RAW_BYTES + 64;
+constexpr int CORR_THREADS = 512;                     // 16 warps: four 4-group runs per thread
 constexpr int GATE_RY = 0, GATE_RZ = 1, GATE_CNOT = 2;
 
 // A gate of a block: kind, local target bit, local control bit (-1), parameter index.
@@ -186,13 +182,9 @@ __global__ void __launch_bounds__(A_THREADS)
 // at one time read neighbouring memory, as the fused block kernel does; a CTA then meets
 // every set once and flushes once per set.
 //
-// Loads: a tile is, for each state (psi, lambda) and local index t, a row of 64 groups
-// (512 contiguous bytes when the block has no target among address bits 0..5).  A warp
-// copies whole rows with cp.async (lane l: groups 2l, 2l+1, 16 bytes; 8-byte halves when
-// address bit 0 is a target), into a ring of CORR_STAGES raw tiles, CORR_STAGES tiles
-// ahead of the tile being multiplied.  Row (state, t) sits at ((state * 64 + t) * 512)
-// bytes with 16-byte chunk c at position c ^ (t & 7), so the transposing reads below (8
-// groups of one t per thread, consecutive t across lanes) hit distinct bank quads.
+// Loads: a tile is, for each state (psi, lambda) and local index t, 64 groups; threads
+// read aligned 32-byte runs straight into registers (k_adj_corr_d below, one variant per
+// role of address bits 0 and 1).
 //
 // Order: the CTAs form CORR_GROUPS groups; group q takes sets q, q + CORR_GROUPS, ... and
 // its CTAs stride through each set's tiles together, so concurrent reads stay close in
@@ -209,24 +201,39 @@ struct CorrArgs {
   const AdjBlockDev* blk;
 };
 
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async8(uint32_t dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+// The correlation kernel.  Each thread loads 4 aligned 32-byte runs (4 consecutive
+// amplitudes) of a tile into registers and writes 4 runs (state, t, groups 4*g4 ..
+// 4*g4+3) into the operand images as 8-byte chunks.  There is no staging buffer: an
+// earlier version that staged tiles through shared memory with cp.async moved three
+// times the shared bytes.  The next tile's loads are issued while the products run.
+//  LM = 0, no target on address bits 0, 1: a 32-byte run is 4 groups of one t.  Warp w
+//    takes state w/8, t = 8*(w%8) + lane/4, run g4 = lane%4 + 4u (u = 0..3): 128
+//    contiguous bytes per t and load.
+//  LM = 1, targets on address bits 0 and 1 (t bits 0, 1): a run is 4 targets of one
+//    group.  Loads: lane bits 0, 1 = group bits 0, 1, lane bits 2, 3 = t bits 2, 3, lane
+//    bit 4 = group bit 2, warp bits 0, 1 = t bits 4, 5, warp bit 2 = group bit 3, warp bit
+//    3 = state, u = group bits 4, 5 (4 lanes read 128 contiguous bytes for every such
+//    placement).  A 4 x 4 transpose over lane bits 0, 1 (two shfl.xor rounds) then
+//    gives each thread 4 groups of one t per run: t = lane%16 + 16*(w%4),
+//    g4 = lane/16 + 2*((w/4)%2) + 4u.
+//  LM = 2 / 3, one target and one group bit on address bits 0, 1 (LM = 2: t bit 0 on
+//    address bit 0; LM = 3: group bit 0 there): a run is 2 targets x 2 groups.  Loads:
+//    lane bit 0 = group bit 1, lane bits 1, 2 = t bits 1, 2, lane bit 3 = group bit 2, lane
+//    bit 4 = t bit 3, warp bits 0, 1 = t bits 4, 5, warp bit 2 = group bit 3, u = group
+//    bits 4, 5.  After putting group bit 0 in register bit 0 (LM = 2 swaps registers 1
+//    and 2), one shfl.xor round over lane bit 0 trades t bit 0 for group bit 1.
+// Every mode's 8-byte operand stores of a warp fill 16 distinct bank slots.
+// A hi/lo, B hi/lo, then the mbarrier, the TMEM slot and the abort flag.
+constexpr int CORRD_SMEM = 4 * CORR_OP_BYTES + 64;
 
-__global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr(const __grid_constant__ CorrArgs a) {
+template <int LM>
+__global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr_d(const __grid_constant__ CorrArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sA_hi = smem;
   uint8_t* sA_lo = smem + CORR_OP_BYTES;
   uint8_t* sB_hi = smem + 2 * CORR_OP_BYTES;
   uint8_t* sB_lo = smem + 3 * CORR_OP_BYTES;
-  uint8_t* raw = smem + 4 * CORR_OP_BYTES;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(raw + CORR_STAGES * CORR_RAW_BYTES);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + 4 * CORR_OP_BYTES);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
   __shared__ uint64_t dept[AT];
@@ -249,13 +256,8 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr(const __grid_const
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const bool pairs = tpos[0] > 0;  // groups 2l, 2l+1 are adjacent amplitudes
-  // Address offsets of this lane's groups 2l and 2l+1 within a tile (the tile's first
-  // group is a multiple of 64, so its offset adds).
-  const uint64_t dlane0 = qsv_insert_zeros((uint64_t)(2 * lane), tpos, AK);
-  const uint64_t dlane1 = qsv_insert_zeros((uint64_t)(2 * lane + 1), tpos, AK);
 
-  // This CTA's tiles: group q of the CTAs, rank within the group.
+  // This CTA's tiles: group grp of the CTAs, rank within the group.
   const uint64_t nsets = a.ntiles >> a.tile_shift;
   const uint64_t tps = 1ull << a.tile_shift;
   uint64_t ngr64 = nsets < (uint64_t)gridDim.x ? nsets : (uint64_t)gridDim.x;
@@ -264,11 +266,9 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr(const __grid_const
   const int grp = blockIdx.x % ngr;
   const uint64_t rank = blockIdx.x / ngr;
   const uint64_t nctas = (gridDim.x - grp + ngr - 1) / ngr;
-  const uint64_t cnt = rank < tps ? (tps - rank + nctas - 1) / nctas : 0;  // tiles per visited set
-  const uint64_t nsg = (nsets - grp + ngr - 1) / ngr;                      // sets visited
+  const uint64_t cnt = rank < tps ? (tps - rank + nctas - 1) / nctas : 0;
+  const uint64_t nsg = (nsets - grp + ngr - 1) / ngr;
   const uint64_t total = cnt * nsg;
-  // A position in this CTA's sequence (set, tile within the set, index in the set's
-  // run), advanced without divisions.
   struct Pos {
     uint64_t set, local, li;
   };
@@ -282,66 +282,118 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr(const __grid_const
   };
   auto tile_of = [&](const Pos& p) -> uint64_t { return (p.set << a.tile_shift) + p.local; };
 
-  const int it_t = tid & (AT - 1);
-  const int it_j = tid >> 6;  // which 8 groups of the tile
-  const uint64_t lim = a.set_amps * nsets;
-  const uint32_t raw_u32 = smem_u32(raw);
-  // Queue this warp's rows (state, t) = rows warp, warp + 8, ... of tile `tile` into `stage`.
-  auto fetch = [&](uint64_t tile, int stage) {
+  const int state = warp >> 3;
+  const float2* src = state ? a.lam : a.psi;
+  // The run each thread writes: local index t, run g4_of(u).
+  const int t = LM == 0   ? ((warp & 7) << 3) | (lane >> 2)
+                : LM == 1 ? (lane & 15) | ((warp & 3) << 4)
+                          : (lane & 7) | (((lane >> 4) & 1) << 3) | ((warp & 3) << 4);
+  auto g4_of = [&](int u) -> int {
+    return LM == 0   ? (lane & 3) | (u << 2)
+           : LM == 1 ? (lane >> 4) | (((warp >> 2) & 1) << 1) | (u << 2)
+                     : ((lane >> 3) & 1) | (((warp >> 2) & 1) << 1) | (u << 2);
+  };
+  // Address offset of load u within a tile: local index and group of its first amplitude.
+  uint64_t off[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    int tl, gl;
+    if (LM == 0) {
+      tl = t;
+      gl = 4 * g4_of(u);
+    } else if (LM == 1) {
+      tl = (lane & 12) | ((warp & 3) << 4);
+      gl = (lane & 3) | (((lane >> 4) & 1) << 2) | (((warp >> 2) & 1) << 3) | (u << 4);
+    } else {
+      tl = (lane & 6) | (((lane >> 4) & 1) << 3) | ((warp & 3) << 4);
+      gl = ((lane & 1) << 1) | (((lane >> 3) & 1) << 2) | (((warp >> 2) & 1) << 3) | (u << 4);
+    }
+    off[u] = dept[tl] + qsv_insert_zeros((uint64_t)gl, tpos, AK);
+  }
+  [[maybe_unused]] const uint64_t lim = a.set_amps * nsets;
+  float2 buf[4][4];
+  auto load = [&](uint64_t tile) {
     const uint64_t set = tile >> a.tile_shift;
-    const uint64_t gbase = qsv_insert_zeros((tile & (tps - 1)) << 6, tpos, AK);
-#pragma unroll 4
-    for (int r = warp; r < 2 * AT; r += CORR_THREADS / 32) {
-      const int state = r >> 6, t = r & (AT - 1);
-      const uint64_t idx = set * a.set_amps + dept[t] + gbase;  // the row's first amplitude
-      const float2* src = (state ? a.lam : a.psi) + idx;
-      const uint32_t dst = raw_u32 + (uint32_t)stage * CORR_RAW_BYTES + (uint32_t)(r * 512) +
-                           (uint32_t)((lane ^ (t & 7)) * 16);
-      if (pairs) {
-        if (QSV_IN_BOUNDS(idx + dlane0 + 1, lim)) cp_async16(dst, src + dlane0);
-      } else {
-        if (QSV_IN_BOUNDS(idx + dlane0, lim)) cp_async8(dst, src + dlane0);
-        if (QSV_IN_BOUNDS(idx + dlane1, lim)) cp_async8(dst + 8, src + dlane1);
+    const uint64_t row = set * a.set_amps + qsv_insert_zeros((tile & (tps - 1)) << 6, tpos, AK);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (QSV_IN_BOUNDS(row + off[u] + 3, lim)) ld_v8(src + row + off[u], buf[u]);
+  };
+  constexpr int LBO = AKD * 16;  // K-step between core matrices (both operands: 128 rows)
+  auto write_ops = [&]() {
+    uint8_t* hi = state ? sB_hi : sA_hi;
+    uint8_t* lo = state ? sB_lo : sA_lo;
+    if constexpr (LM == 1) {
+      // buf[u][j]: t bits 0, 1 = j, group bits 0, 1 = lane bits 0, 1.  Swap the two roles.
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        const bool up = (lane >> b) & 1;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            if (j & (1 << b)) continue;
+            const int j1 = j | (1 << b);
+            const float2 send = up ? buf[u][j] : buf[u][j1];
+            float2 got;
+            got.x = __shfl_xor_sync(0xffffffffu, send.x, 1 << b);
+            got.y = __shfl_xor_sync(0xffffffffu, send.y, 1 << b);
+            if (up)
+              buf[u][j] = got;
+            else
+              buf[u][j1] = got;
+          }
+      }
+    } else if constexpr (LM >= 2) {
+      // Register bit 0 = group bit 0, bit 1 = t bit 0 (LM = 2 loads them the other way
+      // round); then trade t bit 0 (register bit 1) for group bit 1 (lane bit 0).
+      const bool up = lane & 1;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if constexpr (LM == 2) {
+          const float2 x = buf[u][1];
+          buf[u][1] = buf[u][2];
+          buf[u][2] = x;
+        }
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const float2 send = up ? buf[u][j] : buf[u][j + 2];
+          float2 got;
+          got.x = __shfl_xor_sync(0xffffffffu, send.x, 1);
+          got.y = __shfl_xor_sync(0xffffffffu, send.y, 1);
+          if (up)
+            buf[u][j] = got;
+          else
+            buf[u][j + 2] = got;
+        }
       }
     }
-  };
-  // Split this thread's runs (t, 8 groups) of stage `stage` into the bf16 operand images.
-  auto write_ops = [&](int stage) {
-    {
-      const int j = it_j;
-      const uint32_t off_re = (uint32_t)j * (AKD * 16) + (uint32_t)it_t * 16;
-      const uint32_t off_im = off_re + AT * 16;
 #pragma unroll
-      for (int state = 0; state < 2; ++state) {
-        const uint8_t* row = raw + stage * CORR_RAW_BYTES + (state * AT + it_t) * 512;
-        float re[8], im[8];
+    for (int u = 0; u < 4; ++u) {
+      const int g4 = g4_of(u);
+      float re[4], im[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const float4 v = *reinterpret_cast<const float4*>(row + (((4 * j + k) ^ (it_t & 7)) * 16));
-          re[2 * k] = v.x;
-          im[2 * k] = v.y;
-          re[2 * k + 1] = v.z;
-          im[2 * k + 1] = v.w;
-        }
-        uint4 rh, rl, ih, il;
-        split8(re, rh, rl);
-        split8(im, ih, il);
-        uint8_t* hi = state ? sB_hi : sA_hi;
-        uint8_t* lo = state ? sB_lo : sA_lo;
-        *reinterpret_cast<uint4*>(hi + off_re) = rh;
-        *reinterpret_cast<uint4*>(lo + off_re) = rl;
-        *reinterpret_cast<uint4*>(hi + off_im) = ih;
-        *reinterpret_cast<uint4*>(lo + off_im) = il;
+      for (int j = 0; j < 4; ++j) {
+        re[j] = buf[u][j].x;
+        im[j] = buf[u][j].y;
       }
+      uint2 rh, rl, ih, il;
+      split4(re, rh, rl);
+      split4(im, ih, il);
+      // Row t (Re) / AT + t (Im), K = groups 4*g4 .. 4*g4+3 of the tile.
+      const uint32_t off_re = (uint32_t)(g4 >> 1) * LBO + (uint32_t)t * 16 + (uint32_t)(g4 & 1) * 8;
+      const uint32_t off_im = off_re + AT * 16;
+      *reinterpret_cast<uint2*>(hi + off_re) = rh;
+      *reinterpret_cast<uint2*>(lo + off_re) = rl;
+      *reinterpret_cast<uint2*>(hi + off_im) = ih;
+      *reinterpret_cast<uint2*>(lo + off_im) = il;
     }
   };
   constexpr uint32_t idesc = make_idesc(AKD, AKD);
-  constexpr int LBO = AKD * 16;  // K-step between core matrices (both operands: 128 rows)
   auto issue = [&]() {
     if (tid == 0) {
       const uint32_t ah = smem_u32(sA_hi), al = smem_u32(sA_lo), bh = smem_u32(sB_hi), bl = smem_u32(sB_lo);
       constexpr int KSTEPS = CORR_K / 16;
-      // Corrections first, main product last (see the fused block kernel).
 #pragma unroll
       for (int s = 0; s < KSTEPS; ++s)
         tc_mma(tmem, make_smem_desc(ah + s * 2 * LBO, LBO, 128), make_smem_desc(bl + s * 2 * LBO, LBO, 128), idesc,
@@ -355,7 +407,6 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr(const __grid_const
       tc_commit(smem_u32(mbar));
     }
   };
-  // This thread's TMEM quadrant (rows 32*q + lane) and column quarter h (32 columns).
   const int q = warp & 3, h = warp >> 2;
   const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 32);
   float sum[32];
@@ -371,32 +422,19 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr(const __grid_const
   };
   uint32_t phase = 0;
   bool pending = false;
-  // Prologue: the first CORR_STAGES tiles in flight (one commit group per tile; empty
-  // groups past the end keep the count uniform).
-  Pos cu{(uint64_t)grp, rank, 0}, pf = cu;  // the tile being multiplied; the next fetch
-#pragma unroll
-  for (int k = 0; k < CORR_STAGES; ++k) {
-    if ((uint64_t)k < total) fetch(tile_of(pf), k);
-    advance(pf);
-    cp_async_commit();
-  }
-  int stage = 0;
+  Pos cu{(uint64_t)grp, rank, 0}, pf = cu;
+  if (total > 0) load(tile_of(pf));
+  advance(pf);
   for (uint64_t i = 0; i < total; ++i) {
-    cp_async_wait<CORR_STAGES - 1>();  // this tile's group has landed (this thread's copies)
-    __syncthreads();                   // ... and every other thread's
-    write_ops(stage);
+    write_ops();
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     issue();
     pending = true;
-    // The stage just consumed takes the tile CORR_STAGES ahead.
-    if (i + CORR_STAGES < total) fetch(tile_of(pf), stage);
+    if (i + 1 < total) load(tile_of(pf));  // the next tile, while the products run
     advance(pf);
-    cp_async_commit();
-    stage = stage + 1 == CORR_STAGES ? 0 : stage + 1;
-    // One warp waits for the products; the others wait at the barrier (no polling).
     if (warp == 0) {
       const bool done = mbar_wait_bounded(smem_u32(mbar), phase);
       if (!done && lane == 0) atomicExch(abort_flag, 1);
@@ -410,19 +448,19 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr(const __grid_const
       phase ^= 1u;
       break;
     }
-    {
-      float d[32];
-      tmem_ld<32>(taddr, d);
+#pragma unroll
+    for (int c = 0; c < 32; c += 16) {
+      float d[16];
+      tmem_ld<16>(taddr + (uint32_t)c, d);
       tmem_ld_wait();
 #pragma unroll
-      for (int k = 0; k < 32; ++k) sum[k] += d[k];
+      for (int k = 0; k < 16; ++k) sum[c + k] += d[k];
     }
     tc_fence_before();
     const uint64_t set = cu.set;
     advance(cu);
-    if (cu.li == 0) flush(set);  // the next tile belongs to another set (or none is left)
+    if (cu.li == 0) flush(set);
   }
-  cp_async_wait<0>();  // no copy may still target shared memory when the CTA exits
   __syncthreads();
   if (*abort_flag) {
     if (pending) mbar_wait_bounded(smem_u32(mbar), phase);
@@ -539,6 +577,9 @@ struct qsv_adjoint_plan {
   int ngates = 0;
   int max_param = -1;
   std::vector<FusedGeom*> geom;
+  // Correlation kernel of block b: k_adj_corr_d<kind>, by the roles of address bits 0, 1
+  // (0: both group bits, 1: both target bits, 2: target, group, 3: group, target).
+  std::vector<char> corr_kind;
   AdjBlockDev* d_blocks = nullptr;
   AdjGate* d_gates = nullptr;
   int* d_flag = nullptr;
@@ -597,6 +638,7 @@ extern "C" int qsv_adjoint_plan_create(int n, int nblocks, const int* block_qubi
       return set_error(nullptr, QSV_ERR_INVALID, "block %d: no tile geometry", b);
     }
     p->geom.push_back(g);
+    p->corr_kind.push_back(B.tpos[0] >= 2 ? 0 : B.tpos[0] == 1 ? 3 : B.tpos[1] == 1 ? 1 : 2);
     memcpy(B.tperm, tperm, 64);
     B.interleaved = fused_geom_interleaved(g) ? 1 : 0;
     B.first_gate = gofs;
@@ -636,7 +678,10 @@ extern "C" int qsv_adjoint_plan_create(int n, int nblocks, const int* block_qubi
   }
   static bool configured = false;
   if (!configured) {
-    cudaFuncSetAttribute(k_adj_corr, cudaFuncAttributeMaxDynamicSharedMemorySize, CORR_SMEM);
+    cudaFuncSetAttribute(k_adj_corr_d<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, CORRD_SMEM);
+    cudaFuncSetAttribute(k_adj_corr_d<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, CORRD_SMEM);
+    cudaFuncSetAttribute(k_adj_corr_d<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, CORRD_SMEM);
+    cudaFuncSetAttribute(k_adj_corr_d<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, CORRD_SMEM);
     cudaFuncSetAttribute(k_adj_walk, cudaFuncAttributeMaxDynamicSharedMemorySize, AT * AT * (int)sizeof(double2));
     configured = true;
   }
@@ -724,14 +769,22 @@ extern "C" int qsv_adjoint_backward(qsv_adjoint_plan* p, void* psi, void* lam, i
   ca.n = p->n;
   ca.set_amps = 1ull << p->n;
   ca.flag = p->d_flag;
-  int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adj_corr, CORR_THREADS, CORR_SMEM);
-  per_sm = std::max(1, std::min(per_sm, 4));  // 128 TMEM columns each
-  uint64_t grid = (uint64_t)std::max(1, p->sm_count) * per_sm;
-  if (grid > ca.ntiles) grid = ca.ntiles;
+  auto grid_of = [&](const void* fn, int smem) -> unsigned {
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, CORR_THREADS, smem);
+    per_sm = std::max(1, std::min(per_sm, 4));  // 128 TMEM columns each
+    uint64_t grid = (uint64_t)std::max(1, p->sm_count) * per_sm;
+    return (unsigned)std::min<uint64_t>(grid, ca.ntiles);
+  };
+  const unsigned grid_direct = grid_of((const void*)k_adj_corr_d<0>, CORRD_SMEM);
   for (int b = p->nblocks - 1; b >= 0; --b) {
     ca.blk = p->d_blocks + b;
-    k_adj_corr<<<(unsigned)grid, CORR_THREADS, CORR_SMEM, st>>>(ca);
+    switch (p->corr_kind[(size_t)b]) {
+      case 0: k_adj_corr_d<0><<<grid_direct, CORR_THREADS, CORRD_SMEM, st>>>(ca); break;
+      case 1: k_adj_corr_d<1><<<grid_direct, CORR_THREADS, CORRD_SMEM, st>>>(ca); break;
+      case 2: k_adj_corr_d<2><<<grid_direct, CORR_THREADS, CORRD_SMEM, st>>>(ca); break;
+      default: k_adj_corr_d<3><<<grid_direct, CORR_THREADS, CORRD_SMEM, st>>>(ca); break;
+    }
     rc = check_stream_launch("adjoint correlation");
     if (rc) return rc;
     k_adj_walk<<<nsets, A_THREADS, AT * AT * sizeof(double2), st>>>(p->d_blocks + b, p->d_gates, thetas, nparams,
