@@ -205,7 +205,10 @@ struct CorrArgs {
 // amplitudes) of a tile into registers and writes 4 runs (state, t, groups 4*g4 ..
 // 4*g4+3) into the operand images as 8-byte chunks.  There is no staging buffer: an
 // earlier version that staged tiles through shared memory with cp.async moved three
-// times the shared bytes.  The next tile's loads are issued while the products run.
+// times the shared bytes.  Two tiles live in registers: tile i+2's loads are issued while
+// tile i's products run, so every tile's reads have a whole iteration to land.  The
+// running sums sit in TMEM columns 128..255 next to the products (added in registers,
+// round to nearest, and stored back), which leaves the registers for the second tile.
 //  LM = 0, no target on address bits 0, 1: a 32-byte run is 4 groups of one t.  Warp w
 //    takes state w/8, t = 8*(w%8) + lane/4, run g4 = lane%4 + 4u (u = 0..3): 128
 //    contiguous bytes per t and load.
@@ -248,7 +251,7 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr_d(const __grid_con
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"((uint32_t)AKD)
+                 "r"((uint32_t)(2 * AKD))
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -311,8 +314,8 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr_d(const __grid_con
     off[u] = dept[tl] + qsv_insert_zeros((uint64_t)gl, tpos, AK);
   }
   [[maybe_unused]] const uint64_t lim = a.set_amps * nsets;
-  float2 buf[4][4];
-  auto load = [&](uint64_t tile) {
+  float2 buf0[4][4], buf1[4][4];
+  auto load = [&](uint64_t tile, float2 (&buf)[4][4]) {
     const uint64_t set = tile >> a.tile_shift;
     const uint64_t row = set * a.set_amps + qsv_insert_zeros((tile & (tps - 1)) << 6, tpos, AK);
 #pragma unroll
@@ -320,7 +323,7 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr_d(const __grid_con
       if (QSV_IN_BOUNDS(row + off[u] + 3, lim)) ld_v8(src + row + off[u], buf[u]);
   };
   constexpr int LBO = AKD * 16;  // K-step between core matrices (both operands: 128 rows)
-  auto write_ops = [&]() {
+  auto write_ops = [&](float2 (&buf)[4][4]) {
     uint8_t* hi = state ? sB_hi : sA_hi;
     uint8_t* lo = state ? sB_lo : sA_lo;
     if constexpr (LM == 1) {
@@ -407,33 +410,50 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr_d(const __grid_con
       tc_commit(smem_u32(mbar));
     }
   };
+  // This thread's TMEM lane (row 32q + lane) and 32 columns: the tile's products at
+  // taddr, the running sums AKD columns further.
   const int q = warp & 3, h = warp >> 2;
   const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 32);
-  float sum[32];
+  const uint32_t saddr = taddr + AKD;
+  auto zero_sums = [&]() {
+    float z[16];
 #pragma unroll
-  for (int i = 0; i < 32; ++i) sum[i] = 0.f;
+    for (int k = 0; k < 16; ++k) z[k] = 0.f;
+    tmem_st16(saddr, z);
+    tmem_st16(saddr + 16, z);
+    tmem_st_wait();
+  };
   auto flush = [&](uint64_t set) {
     double* dst = a.corr + set * (uint64_t)(AKD * AKD) + (uint64_t)(q * 32 + lane) * AKD + h * 32;
 #pragma unroll
-    for (int i = 0; i < 32; ++i) {
-      if (sum[i] != 0.f) atomicAdd(dst + i, (double)sum[i]);
-      sum[i] = 0.f;
+    for (int c = 0; c < 32; c += 16) {
+      float sv[16];
+      tmem_ld<16>(saddr + (uint32_t)c, sv);
+      tmem_ld_wait();
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+        if (sv[k] != 0.f) atomicAdd(dst + c + k, (double)sv[k]);
     }
+    zero_sums();
   };
   uint32_t phase = 0;
   bool pending = false;
   Pos cu{(uint64_t)grp, rank, 0}, pf = cu;
-  if (total > 0) load(tile_of(pf));
+  if (total > 0) load(tile_of(pf), buf0);
   advance(pf);
-  for (uint64_t i = 0; i < total; ++i) {
-    write_ops();
+  if (total > 1) load(tile_of(pf), buf1);
+  advance(pf);
+  zero_sums();
+  // Tile i (in buf, loaded an iteration or two ago); buf then takes tile i + 2.
+  auto step = [&](uint64_t i, float2 (&buf)[4][4]) -> bool {
+    write_ops(buf);
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     issue();
     pending = true;
-    if (i + 1 < total) load(tile_of(pf));  // the next tile, while the products run
+    if (i + 2 < total) load(tile_of(pf), buf);
     advance(pf);
     if (warp == 0) {
       const bool done = mbar_wait_bounded(smem_u32(mbar), phase);
@@ -446,20 +466,29 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr_d(const __grid_con
     if (*abort_flag) {
       pending = true;
       phase ^= 1u;
-      break;
+      return false;
     }
 #pragma unroll
     for (int c = 0; c < 32; c += 16) {
-      float d[16];
+      float d[16], sv[16];
       tmem_ld<16>(taddr + (uint32_t)c, d);
+      tmem_ld<16>(saddr + (uint32_t)c, sv);
       tmem_ld_wait();
 #pragma unroll
-      for (int k = 0; k < 16; ++k) sum[c + k] += d[k];
+      for (int k = 0; k < 16; ++k) sv[k] += d[k];
+      tmem_st16(saddr + (uint32_t)c, sv);
     }
+    tmem_st_wait();
     tc_fence_before();
     const uint64_t set = cu.set;
     advance(cu);
     if (cu.li == 0) flush(set);
+    return true;
+  };
+  for (uint64_t i = 0; i < total;) {
+    if (!step(i, buf0) || ++i >= total) break;
+    if (!step(i, buf1)) break;
+    ++i;
   }
   __syncthreads();
   if (*abort_flag) {
@@ -470,7 +499,8 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr_d(const __grid_con
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)AKD) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(2 * AKD))
+                 : "memory");
   }
 }
 
@@ -772,7 +802,7 @@ extern "C" int qsv_adjoint_backward(qsv_adjoint_plan* p, void* psi, void* lam, i
   auto grid_of = [&](const void* fn, int smem) -> unsigned {
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, CORR_THREADS, smem);
-    per_sm = std::max(1, std::min(per_sm, 4));  // 128 TMEM columns each
+    per_sm = std::max(1, std::min(per_sm, 2));  // 256 TMEM columns each
     uint64_t grid = (uint64_t)std::max(1, p->sm_count) * per_sm;
     return (unsigned)std::min<uint64_t>(grid, ca.ntiles);
   };
