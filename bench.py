@@ -403,7 +403,9 @@ def run_ours(args):
                                       float(s2.stats["readback_page_locked"])))
         return out
 
-    e2e_steps = max(1, min(args.steps, 3))
+    # Every timed step counts (up to 10): a single slow readback (host memory shared with
+    # other work on the machine) then moves the mean less.
+    e2e_steps = max(1, min(args.steps, 10))
     # Warm-up holds two results at once, as the timed loop does (the previous step's
     # array is alive while the next one runs): both page-locked readback buffers exist
     # before timing starts.

@@ -132,6 +132,7 @@ struct BlockArgs {
   uint64_t set_tiles;
   uint64_t set_amps;
   uint64_t img_stride;
+  int reverse;          // visit the tiles from the last one down (one state only)
 };
 
 // MODE_DIRECT: each thread loads (b, 8 targets) items straight from global memory and
@@ -570,7 +571,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   uint64_t base = 0;
   // Amplitude offset of a tile: its state's start plus the tile's zero-inserted index.
   auto tile_base = [&](uint64_t t) -> uint64_t {
-    if (!a.set_tiles) return qsv_insert_zeros(t, a.ptile, P::EBITS);
+    if (!a.set_tiles) return qsv_insert_zeros(a.reverse ? a.ntiles - 1 - t : t, a.ptile, P::EBITS);
     const uint64_t st = t >> set_shift;
     return st * a.set_amps + qsv_insert_zeros(t - (st << set_shift), a.ptile, P::EBITS);
   };
@@ -1103,7 +1104,13 @@ int launch_args_on(qsv_state* s, const BlockArgs& a, float2* psi) {
   }
 }
 
-int launch_args(qsv_state* s, const BlockArgs& a) {
+// Consecutive launches on a state alternate the tile order (serpentine): each starts
+// with the tiles the previous one wrote last, part of which is still in L2 (measured
+// 0.2-0.5% per step on the brickwork plan; normal-priority stores instead of streaming
+// ones, to keep more of them there, measured 3.5% slower).
+int launch_args(qsv_state* s, const BlockArgs& args) {
+  BlockArgs a = args;
+  a.reverse = (int)(s->block_launches++ & 1);
   return launch_args_on(s, a, (float2*)s->d_amp);
 }
 

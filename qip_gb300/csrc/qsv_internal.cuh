@@ -34,6 +34,9 @@ struct qsv_state {
   // Fault injection for tests (qsv_inject_block_stall): the limit of the stalled wait of
   // the next fused-block launch, 0 when not armed.
   uint64_t inject_stall_ns = 0;
+  // Fused-block launches on this state so far: consecutive launches visit the tiles in
+  // opposite orders (the next one starts on what the last one wrote, still in L2).
+  uint64_t block_launches = 0;
   // Fused-block matrix images: a ring of pinned host staging slots (a slot is reused
   // only after its upload completed, so the host rarely waits for queued kernels) and
   // one device buffer (stream order keeps uploads behind the kernels reading it).
