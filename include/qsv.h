@@ -186,15 +186,18 @@ int qsv_block_matrices(int nblocks, const int* block_k, const int* block_qubits,
  * low_mask set <-> a target on address bit p, p < 7 (targets on higher bits do not
  * change how a tile is read).  Modes: 0 direct, 1 staged (shared-memory transpose),
  * 2 shuffle (warp exchanges; needs 1..k-1 targets on bits 0..4), 3 prefix (transposed
- * products; k = 6 with targets on bits 0, 1 and 2).  Without a recorded choice a class
+ * products; k = 6 with targets on bits 0, 1 and 2), 4 pair1 / 5 pair2 (transposed
+ * products; k = 6, bit 0 / bits 0 and 1 not targets, the next 4 bits targets).  Without a
+ * recorded choice a class
  * takes the built-in rule: direct when its low targets are bits 0..L-1 with L <= 2,
- * prefix for k = 6 with L >= 4, else shuffle (or staged).  Choices are kept per device
+ * prefix for k = 6 with L >= 4, pair1 / pair2 where they apply, else shuffle (or
+ * staged).  Choices are kept per device
  * for the life of the process and used by qsv_apply_blocks / qsv_plan_create and the
  * tensor-core adjoint.
  *
  * qsv_tune_blocks times every applicable mode of each class (reps launches after one
  * warm-up) on a zeroed scratch state of min(n, 26) qubits (the caller's state is not
- * touched), writes out_ms[4*i + mode] (-1 where a mode does not apply) and out_mode[i],
+ * touched), writes out_ms[6*i + mode] (-1 where a mode does not apply) and out_mode[i],
  * and records the fastest.  Synchronises the handle's stream.
  * qsv_set_block_mode pins a mode for a class (mode -1 restores the built-in rule). */
 int qsv_tune_blocks(qsv_state* s, int count, const int* ks, const int* low_masks, int reps,

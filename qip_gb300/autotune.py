@@ -1,8 +1,8 @@
 """Measured choices for the fused-block path: fusion width and tile access mode.
 
-The tensor-core block kernel reads and writes a tile in one of four access modes
-(direct, staged through shared memory, warp shuffles, transposed products for targets on
-the lowest address bits; ``include/qsv.h``).  Which one
+The tensor-core block kernel reads and writes a tile in one of six access modes
+(direct, staged through shared memory, warp shuffles, and three with transposed products
+for targets on or just above the lowest address bits; ``include/qsv.h``).  Which one
 is fastest depends on where the block's targets sit among the low address bits, so it
 is measured: ``qsv_tune_blocks`` times every applicable mode on a scratch state for
 each placement class a plan uses, and the library keeps the fastest per device.
@@ -39,7 +39,7 @@ from .gates import GateOp
 
 SCRATCH_QUBITS = 26  # the library tunes on min(n, 26) qubits
 BATCH_BITS = 7       # a tile's group bits: targets below this change the access pattern
-MODES = ("direct", "staged", "shuffle", "prefix")
+MODES = ("direct", "staged", "shuffle", "prefix", "pair1", "pair2")
 
 
 def placement_class(qubits: Sequence[int], n: int) -> Tuple[int, int]:

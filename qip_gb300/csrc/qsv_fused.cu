@@ -98,7 +98,15 @@ constexpr int MODE_DIRECT = 0;
 constexpr int MODE_STAGED = 1;
 constexpr int MODE_SHUF = 2;
 constexpr int MODE_PREFIX = 3;
-constexpr int NUM_MODES = 4;
+// Pair modes (6-qubit blocks whose lowest targets are a run of 4 on address bits m..m+3
+// above m = 1 or 2 group bits): the prefix mode's transposed products and epilogue (each
+// store instruction then writes one run of 32 (m = 1) or two half-sector runs (m = 2)),
+// with loads of 32-byte runs that hold 2 groups x 2 targets (m = 1) or 4 groups x 1
+// target (m = 2), turned into runs of 4 targets of one group by lane exchanges: a
+// register swap and one shfl.xor round (m = 1) or a 4 x 4 transpose (m = 2).
+constexpr int MODE_PAIR1 = 4;
+constexpr int MODE_PAIR2 = 5;
+constexpr int NUM_MODES = 6;
 
 struct BlockArgs {
   uint64_t ntiles;
@@ -148,7 +156,9 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   constexpr bool STAGED = MODE == MODE_STAGED;
   constexpr bool SHUF = MODE == MODE_SHUF;
   constexpr bool PREFIX = MODE == MODE_PREFIX;
-  static_assert(!PREFIX || KQ == 6, "the prefix mode is built for 6-qubit blocks");
+  constexpr int PAIR = MODE == MODE_PAIR1 ? 1 : (MODE == MODE_PAIR2 ? 2 : 0);  // group bits below the targets
+  constexpr bool TRANS = PREFIX || PAIR > 0;  // transposed products and epilogue
+  static_assert(!TRANS || KQ == 6, "the prefix and pair modes are built for 6-qubit blocks");
   constexpr int SMEM_USED = STAGED ? P::SMEM : P::SMEM_DIRECT;
   constexpr int RAW = STAGED ? P::RAW_BYTES : 0;
   constexpr int R = P::T / 2;  // shuffle mode: amplitudes per thread
@@ -227,6 +237,26 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   // per warp load), and the 8-byte operand stores of a warp fill 16 distinct bank slots.
   auto quarter_b = [&](int u) -> int { return ((warp << 3) | (lane >> 2)) | ((u & 1) << 6); };
   auto quarter_t4 = [&](int u) -> int { return (lane & 3) | ((u >> 1) << 2); };
+  // Pair modes: load u of this thread starts at group pair_lb(u), target pair_lt(u) (the
+  // run's other amplitudes differ in the group bits below the targets, and for m = 1 in
+  // target bit 0); after the exchanges the thread holds group pair_b(u), targets
+  // 4*pair_q4(u) .. +3.  With l = lane bits, w = warp:
+  //   m = 1: loads t bits 1, 2, 3 = l0, l1, l2; b bits 1, 2 = l3, l4; b bits 3..5 = w;
+  //          t bits 4, 5 = u bits 0, 1; b bit 6 = u bit 2.  Held: b bit 0 = l0.
+  //   m = 2: loads t bits 0, 1, 2 = l0, l1, l2; b bits 2, 3 = l3, l4; b bits 4..6 = w;
+  //          t bits 3..5 = u.  Held: b bits 0, 1 = l0, l1.
+  auto lb = [&](int i) -> int { return (lane >> i) & 1; };
+  auto pair_lb = [&](int u) -> int {
+    return PAIR == 1 ? (lb(3) << 1) | (lb(4) << 2) | (warp << 3) | ((u >> 2) << 6) : (lb(3) << 2) | (lb(4) << 3) | (warp << 4);
+  };
+  auto pair_lt = [&](int u) -> int {
+    return PAIR == 1 ? (lb(0) << 1) | (lb(1) << 2) | (lb(2) << 3) | ((u & 3) << 4) : lb(0) | (lb(1) << 1) | (lb(2) << 2) | (u << 3);
+  };
+  auto pair_b = [&](int u) -> int {
+    return PAIR == 1 ? lb(0) | (lb(3) << 1) | (lb(4) << 2) | (warp << 3) | ((u >> 2) << 6)
+                     : lb(0) | (lb(1) << 1) | (lb(3) << 2) | (lb(4) << 3) | (warp << 4);
+  };
+  auto pair_q4 = [&](int u) -> int { return PAIR == 1 ? lb(1) | (lb(2) << 1) | ((u & 3) << 2) : lb(2) | (u << 1); };
 
   // Staged: thread u-th pair holds elements e, e+1 with e = 2*(u*256 + tid) (adjacent
   // amplitudes).  Direct: item it holds (b, targets tg*8..tg*8+7).
@@ -271,6 +301,12 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
 #pragma unroll
       for (int u = 0; u < 2 * P::ITEMS; ++u) {
         const uint64_t off = base + dep(eb[quarter_b(u)]) + dep(et[4 * quarter_t4(u)]);
+        if (QSV_IN_BOUNDS(off + 3, lim)) ld_v8(psi + off, &buf2[u >> 1][(u & 1) * 4]);
+      }
+    } else if constexpr (PAIR > 0) {
+#pragma unroll
+      for (int u = 0; u < 2 * P::ITEMS; ++u) {
+        const uint64_t off = base + dep(eb[pair_lb(u)]) + dep(et[pair_lt(u)]);
         if (QSV_IN_BOUNDS(off + 3, lim)) ld_v8(psi + off, &buf2[u >> 1][(u & 1) * 4]);
       }
     } else if (a.vec == 4) {
@@ -372,10 +408,57 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
           *reinterpret_cast<uint4*>(sA_lo + off_im) = il;
         }
       }
-      if constexpr (PREFIX) {
+      if constexpr (PAIR == 1) {
+        // Register bit 0 = group bit 0, bit 1 = target bit 0: swap them, then trade
+        // register bit 1 (group bit 0) for lane bit 0 (target bit 1).
+        const bool up = lane & 1;
   #pragma unroll
         for (int u = 0; u < 2 * P::ITEMS; ++u) {
-          const int b = quarter_b(u), q4 = quarter_t4(u);
+          float2* r = &buf2[u >> 1][(u & 1) * 4];
+          const float2 x = r[1];
+          r[1] = r[2];
+          r[2] = x;
+  #pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            const float2 send = up ? r[j] : r[j + 2];
+            float2 got;
+            got.x = __shfl_xor_sync(0xffffffffu, send.x, 1);
+            got.y = __shfl_xor_sync(0xffffffffu, send.y, 1);
+            if (up)
+              r[j] = got;
+            else
+              r[j + 2] = got;
+          }
+        }
+      } else if constexpr (PAIR == 2) {
+        // Register bits 0, 1 = group bits 0, 1; lane bits 0, 1 = target bits 0, 1:
+        // transpose the 4 x 4 blocks (two shfl.xor rounds).
+  #pragma unroll
+        for (int bb = 0; bb < 2; ++bb) {
+          const bool up = (lane >> bb) & 1;
+  #pragma unroll
+          for (int u = 0; u < 2 * P::ITEMS; ++u) {
+            float2* r = &buf2[u >> 1][(u & 1) * 4];
+  #pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              if (j & (1 << bb)) continue;
+              const int j1 = j | (1 << bb);
+              const float2 send = up ? r[j] : r[j1];
+              float2 got;
+              got.x = __shfl_xor_sync(0xffffffffu, send.x, 1 << bb);
+              got.y = __shfl_xor_sync(0xffffffffu, send.y, 1 << bb);
+              if (up)
+                r[j] = got;
+              else
+                r[j1] = got;
+            }
+          }
+        }
+      }
+      if constexpr (TRANS) {
+  #pragma unroll
+        for (int u = 0; u < 2 * P::ITEMS; ++u) {
+          const int b = PAIR ? pair_b(u) : quarter_b(u), q4 = PAIR ? pair_q4(u) : quarter_t4(u);
           float re[4], im[4];
   #pragma unroll
           for (int j = 0; j < 4; ++j) {
@@ -394,7 +477,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         }
       }
   #pragma unroll
-      for (int it = 0; it < ((SHUF || PREFIX) ? 0 : P::ITEMS); ++it) {
+      for (int it = 0; it < ((SHUF || TRANS) ? 0 : P::ITEMS); ++it) {
         const int b = item_b(it);
         const int tg = item_tg(it);
         const int eb_ = eb[b];
@@ -431,7 +514,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
       auto mma = [&](uint32_t tile_img, uint32_t w_img, int s, uint32_t accumulate) {
         const uint64_t td = make_smem_desc(tile_img + s * 2 * P::A_LBO, P::A_LBO, 128);
         const uint64_t wd = make_smem_desc(w_img + s * 2 * P::W_LBO, P::W_LBO, 128);
-        if constexpr (PREFIX)
+        if constexpr (TRANS)
           tc_mma(acc, wd, td, idesc, accumulate);
         else
           tc_mma(acc, td, wd, idesc, accumulate);
@@ -484,7 +567,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   #pragma unroll
         for (int c = 0; c < CHS; ++c)
           if (QSV_IN_BOUNDS(tbase + st_lw + a.st_reg[c], lim)) __stcs(dst + a.st_reg[c], make_float2(re[c], im[c]));
-      } else if constexpr (PREFIX) {
+      } else if constexpr (TRANS) {
         // Lane row 32q + lane = component (lane & 1) of target t; warp half h reads
         // groups 64h .. 64h+63.  Pairs of lanes swap halves: the even lane keeps group
         // b and the odd lane group b+1, each with its (Re, Im).
@@ -690,6 +773,9 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
 }
 
 // ---- host: W images ---------------------------------------------------------------------
+// The transposed modes (prefix, pair) take W with interleaved rows.
+bool uses_interleaved_image(int mode) { return mode == MODE_PREFIX || mode == MODE_PAIR1 || mode == MODE_PAIR2; }
+
 uint16_t f32_to_bf16_rn(float f) {
   uint32_t u;
   memcpy(&u, &f, 4);
@@ -923,13 +1009,20 @@ void tile_geometry(int k, const int* user_pos, BlockArgs& a, int forced_mode) {
   while (L < k && tpos[k - 1 - L] == L) ++L;
   const int jl = __builtin_popcountll(tmask & 0x1Full);
   a.vec = L >= 2 ? 4 : (L == 1 ? 2 : 1);
+  // A 6-qubit block whose targets include the run of 4 just above 1 or 2 group bits takes
+  // the pair modes (measured faster than shuffle for every such class).
+  const bool run1 = k == 6 && tpos[k - 1] == 1 && (tmask & 0x1Eull) == 0x1Eull;
+  const bool run2 = k == 6 && tpos[k - 1] == 2 && (tmask & 0x3Cull) == 0x3Cull;
   const int rule = (jl == L && L <= 2) ? MODE_DIRECT
                    : (k == 6 && L >= 4) ? MODE_PREFIX
+                   : run1               ? MODE_PAIR1
+                   : run2               ? MODE_PAIR2
                                         : (jl <= k - 1 ? MODE_SHUF : MODE_STAGED);
   a.mode = rule;
   if (forced_mode == MODE_DIRECT || forced_mode == MODE_STAGED) a.mode = forced_mode;
   if (forced_mode == MODE_SHUF && jl >= 1 && jl <= k - 1) a.mode = MODE_SHUF;
   if (forced_mode == MODE_PREFIX && k == 6 && L >= 3) a.mode = MODE_PREFIX;
+  if ((forced_mode == MODE_PAIR1 && run1) || (forced_mode == MODE_PAIR2 && run2)) a.mode = forced_mode;
   int batch[FB_BATCH_BITS];
   for (int p = 0, nb = 0; nb < FB_BATCH_BITS; ++p)
     if (!((tmask >> p) & 1ull)) batch[nb++] = p;
@@ -1031,6 +1124,8 @@ int lookup_mode(int dev, int k, int low) {
 bool mode_applies(int k, int low, int mode) {
   if (mode == MODE_DIRECT || mode == MODE_STAGED) return true;
   if (mode == MODE_PREFIX) return k == 6 && (low & 7) == 7;  // targets on address bits 0, 1, 2
+  if (mode == MODE_PAIR1) return k == 6 && (low & 0x1F) == 0x1E;  // bit 0 a group bit, bits 1..4 targets
+  if (mode == MODE_PAIR2) return k == 6 && (low & 0x3F) == 0x3C;  // bits 0, 1 group bits, bits 2..5 targets
   const int j = __builtin_popcount((unsigned)low & 0x1Fu);
   return mode == MODE_SHUF && j >= 1 && j <= k - 1;
 }
@@ -1082,6 +1177,12 @@ int launch_block(qsv_state* s, const BlockArgs& a, float2* psi) {
     case MODE_PREFIX:
       if constexpr (KQ == 6) return launch_block_variant<KQ, MODE_PREFIX>(s, a, psi);
       return set_error(s, QSV_ERR_INVALID, "prefix mode on a %d-qubit block", KQ);
+    case MODE_PAIR1:
+      if constexpr (KQ == 6) return launch_block_variant<KQ, MODE_PAIR1>(s, a, psi);
+      return set_error(s, QSV_ERR_INVALID, "pair mode on a %d-qubit block", KQ);
+    case MODE_PAIR2:
+      if constexpr (KQ == 6) return launch_block_variant<KQ, MODE_PAIR2>(s, a, psi);
+      return set_error(s, QSV_ERR_INVALID, "pair mode on a %d-qubit block", KQ);
     default: return launch_block_variant<KQ, MODE_DIRECT>(s, a, psi);
   }
 }
@@ -1171,7 +1272,7 @@ extern "C" int qsv_plan_create(qsv_state* s, int nblocks, const int* ks, const i
   std::vector<uint8_t> host(total);
   for (int i = 0; i < nblocks; ++i)
     build_image(ks[i], mats_c128 + mat_offs[(size_t)i], p->args[(size_t)i].tperm, host.data() + img_off[(size_t)i],
-                p->args[(size_t)i].mode == MODE_PREFIX);
+                uses_interleaved_image(p->args[(size_t)i].mode));
   if (cudaMalloc(&p->d_images, total) != cudaSuccess) {
     cudaGetLastError();
     delete p;
@@ -1266,7 +1367,7 @@ extern "C" int qsv_apply_blocks(qsv_state* s, int nblocks, const int* ks, const 
   uint8_t* himg = static_cast<uint8_t*>(s->h_img[slot]);
   for (int i = 0; i < nblocks; ++i)
     build_image(ks[i], mats_c128 + mat_offs[(size_t)i], args[(size_t)i].tperm, himg + img_off[(size_t)i],
-                args[(size_t)i].mode == MODE_PREFIX);
+                uses_interleaved_image(args[(size_t)i].mode));
   QSV_CUDA(s, cudaMemcpyAsync(s->d_images, himg, total, cudaMemcpyHostToDevice, s->stream));
   QSV_CUDA(s, cudaEventRecord(s->img_ev[slot], s->stream));
   s->img_busy[slot] = true;
@@ -1313,7 +1414,7 @@ int fused_geom_create(int device, int n, int k, const int* qubits, FusedGeom** o
 
 void fused_geom_destroy(FusedGeom* g) { delete g; }
 
-bool fused_geom_interleaved(const FusedGeom* g) { return g->a.mode == MODE_PREFIX; }
+bool fused_geom_interleaved(const FusedGeom* g) { return uses_interleaved_image(g->a.mode); }
 
 int fused_geom_launch_sets(const FusedGeom* g, float2* psi, int nsets, int n, const void* images,
                            size_t img_stride, int* flag, cudaStream_t stream, int sm_count) {
@@ -1327,14 +1428,15 @@ int fused_geom_launch_sets(const FusedGeom* g, float2* psi, int nsets, int n, co
   a.wait_ns = FB_WAIT_NS;
   a.stall_first = 0;
   cudaError_t e;
-  switch (a.k * 4 + a.mode) {
+  switch (a.k * 8 + a.mode) {
 #define QSV_FB_CASE(KQ, MODE) \
-  case KQ * 4 + MODE:         \
+  case KQ * 8 + MODE:         \
     e = launch_fb<KQ, MODE>(a, psi, stream, sm_count); \
     break;
     QSV_FB_CASE(4, MODE_DIRECT) QSV_FB_CASE(4, MODE_STAGED) QSV_FB_CASE(4, MODE_SHUF)
     QSV_FB_CASE(5, MODE_DIRECT) QSV_FB_CASE(5, MODE_STAGED) QSV_FB_CASE(5, MODE_SHUF)
     QSV_FB_CASE(6, MODE_DIRECT) QSV_FB_CASE(6, MODE_STAGED) QSV_FB_CASE(6, MODE_SHUF) QSV_FB_CASE(6, MODE_PREFIX)
+    QSV_FB_CASE(6, MODE_PAIR1) QSV_FB_CASE(6, MODE_PAIR2)
 #undef QSV_FB_CASE
     default: return QSV_ERR_INVALID;
   }
@@ -1438,7 +1540,7 @@ extern "C" int qsv_tune_blocks(qsv_state* s, int count, const int* ks, const int
       tile_geometry(k, tpos, a, mode);
       if (a.mode != mode) continue;
       a.flag = s->d_flag;
-      a.wimg = reinterpret_cast<const uint4*>(dimg + (mode == MODE_PREFIX ? 3 : k - 4) * ibytes);
+      a.wimg = reinterpret_cast<const uint4*>(dimg + (uses_interleaved_image(mode) ? 3 : k - 4) * ibytes);
       rc = launch_args_on(s, a, scratch);
       if (!rc && cudaEventRecord(e0, s->stream) != cudaSuccess) rc = set_error(s, QSV_ERR_CUDA, "event record");
       for (int r = 0; r < reps && !rc; ++r) rc = launch_args_on(s, a, scratch);

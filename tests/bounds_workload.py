@@ -53,7 +53,8 @@ def block_modes(rng):
     n = 22
     lib = nat.load()
     for k, low, mode in ((6, 0b0000000, 0), (6, 0b0000001, 0), (6, 0b0000011, 0), (6, 0b0011000, 2),
-                         (6, 0b0111111, 2), (6, 0b0111111, 3), (6, 0b0000111, 3), (6, 0b0011000, 1),
+                         (6, 0b0111111, 2), (6, 0b0111111, 3), (6, 0b0000111, 3), (6, 0b1111110, 4),
+                         (6, 0b1111100, 5), (6, 0b0011000, 1),
                          (5, 0b0011110, 1), (4, 0b0000000, 0)):
         bits = [b for b in range(7) if (low >> b) & 1]
         bits += [n - 1 - i for i in range(k - len(bits))]

@@ -16,13 +16,15 @@ pytestmark = pytest.mark.gpu
 C64 = numpy.complex64
 
 CLASSES = [(6, 0b0000000), (6, 0b1100000), (6, 0b0000011), (6, 0b0011000), (6, 0b0000110), (6, 0b1110000),
-           (6, 0b0011110), (6, 0b0111111), (6, 0b0001111), (6, 0b0000111), (6, 0b1011111), (5, 0b0001010),
+           (6, 0b0011110), (6, 0b0111111), (6, 0b0001111), (6, 0b0000111), (6, 0b1011111), (6, 0b1111110),
+           (6, 0b0111100), (6, 0b1111100), (6, 0b1011110), (5, 0b0001010),
            (5, 0b0011101), (5, 0b0000111), (4, 0b0011100), (4, 0b0011110)]
 
 
 def applicable(k, low):
     j = bin(low & 0x1F).count("1")
-    return [0, 1] + ([2] if 1 <= j <= k - 1 else []) + ([3] if k == 6 and low & 7 == 7 else [])
+    return ([0, 1] + ([2] if 1 <= j <= k - 1 else []) + ([3] if k == 6 and low & 7 == 7 else [])
+            + ([4] if k == 6 and low & 0x1F == 0x1E else []) + ([5] if k == 6 and low & 0x3F == 0x3C else []))
 
 
 def block_qubits(n, k, low):
@@ -74,6 +76,10 @@ def test_block_mode_arguments_are_checked():
         nat.check(lib.qsv_set_block_mode(st.handle, 6, 0b0000011, 3), st.handle, "set_block_mode")  # bit 2 free
     with pytest.raises(ValueError):
         nat.check(lib.qsv_set_block_mode(st.handle, 5, 0b0000111, 3), st.handle, "set_block_mode")  # k = 5
+    with pytest.raises(ValueError):
+        nat.check(lib.qsv_set_block_mode(st.handle, 6, 0b0011111, 4), st.handle, "set_block_mode")  # bit 0 a target
+    with pytest.raises(ValueError):
+        nat.check(lib.qsv_set_block_mode(st.handle, 6, 0b0011100, 5), st.handle, "set_block_mode")  # bit 5 free
     st.close()
 
 
