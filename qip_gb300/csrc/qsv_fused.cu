@@ -1013,10 +1013,15 @@ void tile_geometry(int k, const int* user_pos, BlockArgs& a, int forced_mode) {
   // the pair modes (measured faster than shuffle for every such class).
   const bool run1 = k == 6 && tpos[k - 1] == 1 && (tmask & 0x1Eull) == 0x1Eull;
   const bool run2 = k == 6 && tpos[k - 1] == 2 && (tmask & 0x3Cull) == 0x3Cull;
-  const int rule = (jl == L && L <= 2) ? MODE_DIRECT
+  // Direct also wins (or ties) for a prefix of 3 and whenever no target sits on address
+  // bits 0..2 (measured at n=26 for k = 4, 5, 6: e.g. bits 4..6 0.183 ms against 0.195
+  // shuffle, bits 0..2 0.190 against 0.201 prefix and 0.227 shuffle).
+  const bool low3_free = tpos[k - 1] >= 3;
+  const int rule = (jl == L && L <= 3) ? MODE_DIRECT
                    : (k == 6 && L >= 4) ? MODE_PREFIX
                    : run1               ? MODE_PAIR1
                    : run2               ? MODE_PAIR2
+                   : low3_free          ? MODE_DIRECT
                                         : (jl <= k - 1 ? MODE_SHUF : MODE_STAGED);
   a.mode = rule;
   if (forced_mode == MODE_DIRECT || forced_mode == MODE_STAGED) a.mode = forced_mode;
