@@ -41,6 +41,8 @@ def infidelity(a, b):
 
 @pytest.mark.parametrize("k,low", CLASSES)
 def test_every_access_mode_matches_oracle(k, low):
+    """Two blocks of the class in a row: consecutive launches on a state visit the tiles
+    in opposite orders, so both orders are checked in every mode."""
     n = 15
     rng = numpy.random.default_rng(k * 1000 + low)
     lib = nat.load()
@@ -48,16 +50,18 @@ def test_every_access_mode_matches_oracle(k, low):
         qubits = block_qubits(n, k, low)
         rng.shuffle(qubits)
         u = numpy.linalg.qr(rng.standard_normal((2 ** k, 2 ** k)) + 1j * rng.standard_normal((2 ** k, 2 ** k)))[0]
+        u2 = numpy.linalg.qr(rng.standard_normal((2 ** k, 2 ** k)) + 1j * rng.standard_normal((2 ** k, 2 ** k)))[0]
         v = (rng.standard_normal(2 ** n) + 1j * rng.standard_normal(2 ** n)) / numpy.sqrt(2 ** (n + 1))
         st = GpuBackend.make_state(n, [list(range(n))], [v], statetype=C64, fusion=True, autotune=False)
         try:
             nat.check(lib.qsv_set_block_mode(st.handle, k, low, mode), st.handle, "set_block_mode")
             st.apply_blocks([Block(tuple(qubits), u, 1, 1.0)])
+            st.apply_blocks([Block(tuple(qubits), u2, 1, 1.0)])
             got = st.get_state()
         finally:
             lib.qsv_set_block_mode(st.handle, k, low, -1)
             st.close()
-        want = sv.apply_on(v, n, qubits, u)
+        want = sv.apply_on(sv.apply_on(v, n, qubits, u), n, qubits, u2)
         err = numpy.max(numpy.abs(got - want)) / numpy.max(numpy.abs(want))
         assert err < 5e-5, (k, low, mode, err)
         assert infidelity(got, want) < 1e-8
