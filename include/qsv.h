@@ -187,11 +187,12 @@ int qsv_block_matrices(int nblocks, const int* block_k, const int* block_qubits,
  * change how a tile is read).  Modes: 0 direct, 1 staged (shared-memory transpose),
  * 2 shuffle (warp exchanges; needs 1..k-1 targets on bits 0..4), 3 prefix (transposed
  * products; k = 6 with targets on bits 0, 1 and 2), 4 pair1 / 5 pair2 (transposed
- * products; k = 6, bit 0 / bits 0 and 1 not targets, the next 4 bits targets).  Without a
+ * products; k = 6 with the lowest target on bit 1 / bit 2).  Without a
  * recorded choice a class
  * takes the built-in rule: direct when its low targets are bits 0..L-1 with L <= 3,
- * prefix for k = 6 with L >= 4, pair1 / pair2 where they apply, direct when no target
- * sits on bits 0..2, else shuffle (or staged).  Choices are kept per device
+ * prefix for k = 6 with L >= 4, pair1 / pair2 when the lowest target is on bit 1 / 2
+ * and at least 3 of bits 1..4 / 2..5 are targets, direct when no target sits on bits
+ * 0..2, else shuffle (or staged).  Choices are kept per device
  * for the life of the process and used by qsv_apply_blocks / qsv_plan_create and the
  * tensor-core adjoint.
  *

@@ -1009,10 +1009,11 @@ void tile_geometry(int k, const int* user_pos, BlockArgs& a, int forced_mode) {
   while (L < k && tpos[k - 1 - L] == L) ++L;
   const int jl = __builtin_popcountll(tmask & 0x1Full);
   a.vec = L >= 2 ? 4 : (L == 1 ? 2 : 1);
-  // A 6-qubit block whose targets include the run of 4 just above 1 or 2 group bits takes
-  // the pair modes (measured faster than shuffle for every such class).
-  const bool run1 = k == 6 && tpos[k - 1] == 1 && (tmask & 0x1Eull) == 0x1Eull;
-  const bool run2 = k == 6 && tpos[k - 1] == 2 && (tmask & 0x3Cull) == 0x3Cull;
+  // A 6-qubit block whose lowest target sits on bit 1 (2) takes pair1 (pair2) when at
+  // least 3 of bits 1..4 (2..5) are targets: measured faster than shuffle for every such
+  // class, and slower with fewer (the store runs break up).
+  const bool run1 = k == 6 && tpos[k - 1] == 1 && __builtin_popcountll(tmask & 0x1Eull) >= 3;
+  const bool run2 = k == 6 && tpos[k - 1] == 2 && __builtin_popcountll(tmask & 0x3Cull) >= 3;
   // Direct also wins (or ties) for a prefix of 3 and whenever no target sits on address
   // bits 0..2 (measured at n=26 for k = 4, 5, 6: e.g. bits 4..6 0.183 ms against 0.195
   // shuffle, bits 0..2 0.190 against 0.201 prefix and 0.227 shuffle).
@@ -1027,7 +1028,11 @@ void tile_geometry(int k, const int* user_pos, BlockArgs& a, int forced_mode) {
   if (forced_mode == MODE_DIRECT || forced_mode == MODE_STAGED) a.mode = forced_mode;
   if (forced_mode == MODE_SHUF && jl >= 1 && jl <= k - 1) a.mode = MODE_SHUF;
   if (forced_mode == MODE_PREFIX && k == 6 && L >= 3) a.mode = MODE_PREFIX;
-  if ((forced_mode == MODE_PAIR1 && run1) || (forced_mode == MODE_PAIR2 && run2)) a.mode = forced_mode;
+  // Any placement with the lowest target on bit 1 (pair1) or 2 (pair2) is correct in the
+  // pair modes; the run of 4 only decides how whole the store runs are.
+  if ((forced_mode == MODE_PAIR1 && k == 6 && tpos[k - 1] == 1) ||
+      (forced_mode == MODE_PAIR2 && k == 6 && tpos[k - 1] == 2))
+    a.mode = forced_mode;
   int batch[FB_BATCH_BITS];
   for (int p = 0, nb = 0; nb < FB_BATCH_BITS; ++p)
     if (!((tmask >> p) & 1ull)) batch[nb++] = p;
@@ -1129,8 +1134,8 @@ int lookup_mode(int dev, int k, int low) {
 bool mode_applies(int k, int low, int mode) {
   if (mode == MODE_DIRECT || mode == MODE_STAGED) return true;
   if (mode == MODE_PREFIX) return k == 6 && (low & 7) == 7;  // targets on address bits 0, 1, 2
-  if (mode == MODE_PAIR1) return k == 6 && (low & 0x1F) == 0x1E;  // bit 0 a group bit, bits 1..4 targets
-  if (mode == MODE_PAIR2) return k == 6 && (low & 0x3F) == 0x3C;  // bits 0, 1 group bits, bits 2..5 targets
+  if (mode == MODE_PAIR1) return k == 6 && (low & 3) == 2;  // lowest target on bit 1
+  if (mode == MODE_PAIR2) return k == 6 && (low & 7) == 4;  // lowest target on bit 2
   const int j = __builtin_popcount((unsigned)low & 0x1Fu);
   return mode == MODE_SHUF && j >= 1 && j <= k - 1;
 }

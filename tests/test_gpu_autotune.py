@@ -24,7 +24,7 @@ CLASSES = [(6, 0b0000000), (6, 0b1100000), (6, 0b0000011), (6, 0b0011000), (6, 0
 def applicable(k, low):
     j = bin(low & 0x1F).count("1")
     return ([0, 1] + ([2] if 1 <= j <= k - 1 else []) + ([3] if k == 6 and low & 7 == 7 else [])
-            + ([4] if k == 6 and low & 0x1F == 0x1E else []) + ([5] if k == 6 and low & 0x3F == 0x3C else []))
+            + ([4] if k == 6 and low & 3 == 2 else []) + ([5] if k == 6 and low & 7 == 4 else []))
 
 
 def block_qubits(n, k, low):
@@ -83,7 +83,7 @@ def test_block_mode_arguments_are_checked():
     with pytest.raises(ValueError):
         nat.check(lib.qsv_set_block_mode(st.handle, 6, 0b0011111, 4), st.handle, "set_block_mode")  # bit 0 a target
     with pytest.raises(ValueError):
-        nat.check(lib.qsv_set_block_mode(st.handle, 6, 0b0011100, 5), st.handle, "set_block_mode")  # bit 5 free
+        nat.check(lib.qsv_set_block_mode(st.handle, 6, 0b0011110, 5), st.handle, "set_block_mode")  # bit 1 a target
     st.close()
 
 
