@@ -809,6 +809,21 @@ extern "C" int qsv_adjoint_backward(qsv_adjoint_plan* p, void* psi, void* lam, i
   const unsigned grid_direct = grid_of((const void*)k_adj_corr_d<0>, CORRD_SMEM);
   for (int b = p->nblocks - 1; b >= 0; --b) {
     ca.blk = p->d_blocks + b;
+    if (fused_geom_backward_ok(p->geom[(size_t)b])) {
+      // One pass: U^+ images, then un-compute and correlation together, then the walk.
+      k_adj_images<true><<<nsets, A_THREADS, 0, st>>>(p->d_blocks + b, p->d_gates, thetas, nparams, images,
+                                                     image_stride());
+      rc = check_stream_launch("adjoint images");
+      if (rc) return rc;
+      rc = fused_geom_launch_backward(p->geom[(size_t)b], states[0], states[1], corr, nsets, p->n, images,
+                                      image_stride(), p->d_flag, st, p->sm_count);
+      if (rc) return set_error(nullptr, rc, "adjoint backward launch failed");
+      k_adj_walk<<<nsets, A_THREADS, AT * AT * sizeof(double2), st>>>(p->d_blocks + b, p->d_gates, thetas, nparams,
+                                                                      corr, grads, grad_stride);
+      rc = check_stream_launch("adjoint walk");
+      if (rc) return rc;
+      continue;
+    }
     switch (p->corr_kind[(size_t)b]) {
       case 0: k_adj_corr_d<0><<<grid_direct, CORR_THREADS, CORRD_SMEM, st>>>(ca); break;
       case 1: k_adj_corr_d<1><<<grid_direct, CORR_THREADS, CORRD_SMEM, st>>>(ca); break;

@@ -772,6 +772,306 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   }
 }
 
+// ---- the tensor-core adjoint's fused backward pass --------------------------------------
+// One launch per block over all parameter sets, for blocks with no target on address
+// bits 0..4 (the direct geometry with 8-byte lanes).  Per tile (128 groups x 64 targets of
+// one set) it loads psi and lambda, writes both bf16 operand images and issues three
+// product sets on the tensor cores: psi U^+ and lambda U^+ (the un-compute, written back
+// in place) and the correlation D[m][n] = sum_g psi[g][m] lambda[g][n] over the tile's 128
+// groups, with both images read MN-major (the same bytes: a K-major image of rows g is
+// an MN-major operand with K = g; core matrices 128 bytes apart along K, 2048 along MN).
+// The correlation's running sums stay in TMEM (columns 384..511) and are flushed with
+// FP64 atomics into corr[set][m][n] when a CTA leaves a set; the CTAs form 8 groups that
+// stride through their sets together (as k_adj_corr_d).  512 threads: two (b, 8 targets)
+// items per thread and state, both states of the next tile loaded while the products run.
+// psi and lambda are read once and written once per block instead of read twice and
+// written once (correlation kernel + two block launches).
+struct AdjBackArgs {
+  float2* psi;
+  float2* lam;
+  double* corr;        // [nsets][128][128], accumulated into
+  const uint8_t* wimg;  // U^+ image of set s at wimg + s * img_stride
+  uint64_t img_stride;
+  uint64_t set_amps;    // 2^n
+  uint64_t nsets;
+  int* flag;
+};
+
+constexpr int AB_THREADS = 512;
+constexpr int AB_GROUPS = 8;
+// psi and lambda images (hi, lo), W (hi, lo), eb, et, dephi, then the mbarrier, the TMEM
+// slot and the abort flag.
+constexpr int AB_SMEM = 4 * FB<6>::A_BYTES + 2 * FB<6>::W_BYTES + FB_M * 2 + 64 * 2 + 64 * 8 + 64;
+
+__global__ void __launch_bounds__(AB_THREADS, 1)
+    k_adj_back(const __grid_constant__ BlockArgs g, const __grid_constant__ AdjBackArgs a) {
+  using P = FB<6>;
+  constexpr int ITEMS = (FB_M * (P::T / 8)) / AB_THREADS;  // 2
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sP_hi = smem;
+  uint8_t* sP_lo = smem + P::A_BYTES;
+  uint8_t* sL_hi = smem + 2 * P::A_BYTES;
+  uint8_t* sL_lo = smem + 3 * P::A_BYTES;
+  uint8_t* sW_hi = smem + 4 * P::A_BYTES;
+  uint8_t* sW_lo = sW_hi + P::W_BYTES;
+  uint16_t* eb = reinterpret_cast<uint16_t*>(sW_lo + P::W_BYTES);
+  uint16_t* et = eb + FB_M;
+  uint64_t* dephi = reinterpret_cast<uint64_t*>(et + P::T);
+  uint64_t* mbar = dephi + P::T;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+  int* abort_flag = reinterpret_cast<int*>(tslot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int i = tid; i < FB_M; i += AB_THREADS) eb[i] = g.eb[i];
+  for (int i = tid; i < P::T; i += AB_THREADS) {
+    et[i] = g.et[i];
+    dephi[i] = g.dephi[i];
+  }
+  if (tid == 0) {
+    mbar_init(smem_u32(mbar), 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(512u)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const uint32_t accP = tmem, accL = tmem + 128, accC = tmem + 256, sums = tmem + 384;
+  auto dep = [&](int e) -> uint64_t { return (uint64_t)(e & (FB_M - 1)) + dephi[e >> FB_BATCH_BITS]; };
+
+  // This CTA's tiles: group grp of the CTAs takes sets grp, grp + ngr, ...; within a set
+  // its CTAs stride through the tiles together.
+  const uint64_t tps = g.ntiles;  // tiles per set
+  uint64_t ngr64 = a.nsets < (uint64_t)gridDim.x ? a.nsets : (uint64_t)gridDim.x;
+  if (ngr64 > (uint64_t)AB_GROUPS) ngr64 = AB_GROUPS;
+  const int ngr = (int)ngr64;
+  const int grp = blockIdx.x % ngr;
+  const uint64_t rank = blockIdx.x / ngr;
+  const uint64_t nctas = (gridDim.x - grp + ngr - 1) / ngr;
+  const uint64_t cnt = rank < tps ? (tps - rank + nctas - 1) / nctas : 0;
+  const uint64_t nsg = (a.nsets - grp + ngr - 1) / ngr;
+  const uint64_t total = cnt * nsg;
+  struct Pos {
+    uint64_t set, local, li;
+  };
+  auto advance = [&](Pos& p) {
+    p.local += nctas;
+    if (++p.li == cnt) {
+      p.li = 0;
+      p.local = rank;
+      p.set += ngr;
+    }
+  };
+  auto tile_base = [&](const Pos& p) -> uint64_t {
+    return p.set * a.set_amps + qsv_insert_zeros(p.local, g.ptile, P::EBITS);
+  };
+  [[maybe_unused]] const uint64_t lim = a.set_amps * a.nsets;
+  float2 bp[ITEMS][8], bl[ITEMS][8];
+  auto load = [&](uint64_t base) {
+#pragma unroll
+    for (int it = 0; it < ITEMS; ++it) {
+      const int item = it * AB_THREADS + tid;
+      const uint64_t rb = base + dep(eb[item & (FB_M - 1)]);
+      const int tg = item >> FB_BATCH_BITS;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const uint64_t idx = rb + dep(et[tg * 8 + j]);
+        if (QSV_IN_BOUNDS(idx, lim)) {
+          bp[it][j] = __ldcs(a.psi + idx);
+          bl[it][j] = __ldcs(a.lam + idx);
+        }
+      }
+    }
+  };
+  auto write_image = [&](const float2 (&buf)[ITEMS][8], uint8_t* hi, uint8_t* lo) {
+#pragma unroll
+    for (int it = 0; it < ITEMS; ++it) {
+      const int item = it * AB_THREADS + tid;
+      const int b = item & (FB_M - 1);
+      const int tg = item >> FB_BATCH_BITS;
+      float re[8], im[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        re[j] = buf[it][j].x;
+        im[j] = buf[it][j].y;
+      }
+      uint4 rh, rl, ih, il;
+      split8(re, rh, rl);
+      split8(im, ih, il);
+      const int off_re = tg * P::A_LBO + b * 16;
+      const int off_im = (P::T / 8 + tg) * P::A_LBO + b * 16;
+      *reinterpret_cast<uint4*>(hi + off_re) = rh;
+      *reinterpret_cast<uint4*>(lo + off_re) = rl;
+      *reinterpret_cast<uint4*>(hi + off_im) = ih;
+      *reinterpret_cast<uint4*>(lo + off_im) = il;
+    }
+  };
+  uint64_t cur_set = ~0ull;
+  auto load_w = [&](uint64_t set) {
+    const uint4* src = reinterpret_cast<const uint4*>(a.wimg + set * a.img_stride);
+    uint4* dst = reinterpret_cast<uint4*>(sW_hi);
+    constexpr int NV = (2 * P::W_BYTES) / 16;
+    for (int i = tid; i < NV; i += AB_THREADS) dst[i] = src[i];
+  };
+  constexpr uint32_t idesc = make_idesc(FB_M, P::KD);
+  // Correlation: both operands MN-major (transpose bits 15, 16), K = the tile's groups.
+  constexpr uint32_t idesc_c = make_idesc(P::KD, P::KD) | (1u << 15) | (1u << 16);
+  auto issue = [&]() {
+    if (tid != 0) return;
+    const uint32_t ph = smem_u32(sP_hi), pl = smem_u32(sP_lo), lh = smem_u32(sL_hi), ll = smem_u32(sL_lo);
+    const uint32_t wh = smem_u32(sW_hi), wl = smem_u32(sW_lo);
+    constexpr int KS = P::KD / 16;  // 8 steps of 16 components (block products)
+    auto blk = [&](uint32_t acc, uint32_t xh, uint32_t xl) {
+      // Corrections first, main pass last (as in k_block_tc).
+#pragma unroll
+      for (int s = 0; s < KS; ++s)
+        tc_mma(acc, make_smem_desc(xh + s * 2 * P::A_LBO, P::A_LBO, 128),
+               make_smem_desc(wl + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, s > 0 ? 1u : 0u);
+#pragma unroll
+      for (int s = 0; s < KS; ++s)
+        tc_mma(acc, make_smem_desc(xl + s * 2 * P::A_LBO, P::A_LBO, 128),
+               make_smem_desc(wh + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, 1u);
+#pragma unroll
+      for (int s = 0; s < KS; ++s)
+        tc_mma(acc, make_smem_desc(xh + s * 2 * P::A_LBO, P::A_LBO, 128),
+               make_smem_desc(wh + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, 1u);
+    };
+    blk(accP, ph, pl);
+    blk(accL, lh, ll);
+    constexpr int GS = FB_M / 16;  // 8 steps of 16 groups (correlation)
+    auto mn = [&](uint32_t base, int s) { return make_smem_desc(base + s * 256, 128, P::A_LBO); };
+#pragma unroll
+    for (int s = 0; s < GS; ++s) tc_mma(accC, mn(ph, s), mn(ll, s), idesc_c, s > 0 ? 1u : 0u);
+#pragma unroll
+    for (int s = 0; s < GS; ++s) tc_mma(accC, mn(pl, s), mn(lh, s), idesc_c, 1u);
+#pragma unroll
+    for (int s = 0; s < GS; ++s) tc_mma(accC, mn(ph, s), mn(lh, s), idesc_c, 1u);
+    tc_commit(smem_u32(mbar));
+  };
+  // Epilogue of a block product: warp w reads TMEM lanes 32*(w%4).. (groups) and target
+  // columns [16*(w/4), +16), and stores them over the state.
+  const int q = warp & 3, h = warp >> 2;
+  const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+  auto store = [&](uint32_t acc, float2* dst, uint64_t base) {
+    const int b = q * 32 + lane;
+    const uint64_t rb = base + dep(eb[b]);
+    const int t0 = h * 16;
+    float re[16], im[16];
+    tmem_ld<16>(acc + lane_off + (uint32_t)t0, re);
+    tmem_ld<16>(acc + lane_off + (uint32_t)(P::T + t0), im);
+    tmem_ld_wait();
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const uint64_t idx = rb + dep(et[t0 + j]);
+      if (QSV_IN_BOUNDS(idx, lim)) __stcs(dst + idx, make_float2(re[j], im[j]));
+    }
+  };
+  // Correlation: thread (lane row 32q + lane, columns 32h ..) adds its 32 entries.
+  const uint32_t c_off = lane_off + (uint32_t)(h * 32);
+  auto zero_sums = [&]() {
+    float z[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) z[k] = 0.f;
+    tmem_st16(sums + c_off, z);
+    tmem_st16(sums + c_off + 16, z);
+    tmem_st_wait();
+  };
+  auto add_corr = [&]() {
+#pragma unroll
+    for (int c = 0; c < 32; c += 16) {
+      float d[16], sv[16];
+      tmem_ld<16>(accC + c_off + (uint32_t)c, d);
+      tmem_ld<16>(sums + c_off + (uint32_t)c, sv);
+      tmem_ld_wait();
+#pragma unroll
+      for (int k = 0; k < 16; ++k) sv[k] += d[k];
+      tmem_st16(sums + c_off + (uint32_t)c, sv);
+    }
+    tmem_st_wait();
+  };
+  auto flush = [&](uint64_t set) {
+    double* dst = a.corr + set * (uint64_t)(P::KD * P::KD) + (uint64_t)(q * 32 + lane) * P::KD + h * 32;
+#pragma unroll
+    for (int c = 0; c < 32; c += 16) {
+      float sv[16];
+      tmem_ld<16>(sums + c_off + (uint32_t)c, sv);
+      tmem_ld_wait();
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+        if (sv[k] != 0.f) atomicAdd(dst + c + k, (double)sv[k]);
+    }
+    zero_sums();
+  };
+
+  zero_sums();
+  uint32_t phase = 0;
+  bool pending = false;
+  Pos cu{(uint64_t)grp, rank, 0}, pf = cu;
+  uint64_t base = 0;
+  if (total > 0) {
+    base = tile_base(pf);
+    load(base);
+  }
+  advance(pf);
+  for (uint64_t i = 0; i < total; ++i) {
+    if (cu.set != cur_set) {  // no products in flight here
+      cur_set = cu.set;
+      load_w(cur_set);
+    }
+    write_image(bp, sP_hi, sP_lo);
+    write_image(bl, sL_hi, sL_lo);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    issue();
+    pending = true;
+    uint64_t next_base = 0;
+    if (i + 1 < total) {
+      next_base = tile_base(pf);
+      load(next_base);
+    }
+    advance(pf);
+    if (warp == 0) {
+      const bool done = mbar_wait_bounded(smem_u32(mbar), phase);
+      if (!done && lane == 0) atomicExch(abort_flag, 1);
+    }
+    phase ^= 1u;
+    pending = false;
+    __syncthreads();
+    tc_fence_after();
+    if (*abort_flag) {
+      pending = true;
+      phase ^= 1u;
+      break;
+    }
+    store(accP, a.psi, base);
+    store(accL, a.lam, base);
+    add_corr();
+    tc_fence_before();
+    const uint64_t set = cu.set;
+    advance(cu);
+    if (cu.li == 0) flush(set);
+    base = next_base;
+  }
+  __syncthreads();
+  if (*abort_flag) {
+    if (pending) mbar_wait_bounded(smem_u32(mbar), phase);
+    if (tid == 0) atomicExch(a.flag, 3);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u) : "memory");
+  }
+}
+
 // ---- host: W images ---------------------------------------------------------------------
 // The transposed modes (prefix, pair) take W with interleaved rows.
 bool uses_interleaved_image(int mode) { return mode == MODE_PREFIX || mode == MODE_PAIR1 || mode == MODE_PAIR2; }
@@ -1394,6 +1694,7 @@ extern "C" int qsv_apply_blocks(qsv_state* s, int nblocks, const int* ks, const 
 namespace qsv {
 struct FusedGeom {
   BlockArgs a;
+  int low;  // targets among address bits 0..6
 };
 
 size_t fused_image_bytes(int k) { return image_bytes(k); }
@@ -1416,6 +1717,7 @@ int fused_geom_create(int device, int n, int k, const int* qubits, FusedGeom** o
   g->a = BlockArgs{};
   g->a.k = k;
   g->a.ntiles = 1ull << (n - k - FB_BATCH_BITS);
+  g->low = low;
   tile_geometry(k, pos, g->a, lookup_mode(device, k, low));
   memcpy(tperm_out, g->a.tperm, 64);
   *out = g;
@@ -1425,6 +1727,38 @@ int fused_geom_create(int device, int n, int k, const int* qubits, FusedGeom** o
 void fused_geom_destroy(FusedGeom* g) { delete g; }
 
 bool fused_geom_interleaved(const FusedGeom* g) { return uses_interleaved_image(g->a.mode); }
+
+bool fused_geom_backward_ok(const FusedGeom* g) {
+  return g->a.k == 6 && g->a.mode == MODE_DIRECT && g->a.vec == 1 && (g->low & 0x1F) == 0;
+}
+
+int fused_geom_launch_backward(const FusedGeom* geom, float2* psi, float2* lam, double* corr, int nsets, int n,
+                               const void* images, size_t img_stride, int* flag, cudaStream_t stream, int sm_count) {
+  if (!fused_geom_backward_ok(geom)) return QSV_ERR_UNSUPPORTED;
+  static bool configured = false;
+  if (!configured) {
+    if (cudaFuncSetAttribute(k_adj_back, cudaFuncAttributeMaxDynamicSharedMemorySize, AB_SMEM) != cudaSuccess)
+      return QSV_ERR_CUDA;
+    configured = true;
+  }
+  AdjBackArgs a{};
+  a.psi = psi;
+  a.lam = lam;
+  a.corr = corr;
+  a.wimg = static_cast<const uint8_t*>(images);
+  a.img_stride = img_stride;
+  a.set_amps = 1ull << n;
+  a.nsets = (uint64_t)nsets;
+  a.flag = flag;
+  // One CTA per SM (shared memory, all 512 TMEM columns).
+  uint64_t grid = (uint64_t)std::max(1, sm_count);
+  const uint64_t work = geom->a.ntiles * (uint64_t)nsets;
+  if (grid > work) grid = work;
+  k_adj_back<<<(unsigned)grid, AB_THREADS, AB_SMEM, stream>>>(geom->a, a);
+  if (cudaGetLastError() != cudaSuccess) return QSV_ERR_CUDA;
+  count_launch();
+  return QSV_OK;
+}
 
 int fused_geom_launch_sets(const FusedGeom* g, float2* psi, int nsets, int n, const void* images,
                            size_t img_stride, int* flag, cudaStream_t stream, int sm_count) {
