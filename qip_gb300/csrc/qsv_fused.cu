@@ -773,8 +773,8 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
 }
 
 // ---- the tensor-core adjoint's fused backward pass --------------------------------------
-// One launch per block over all parameter sets, for blocks with no target on address
-// bits 0..4 (the direct geometry with 8-byte lanes).  Per tile (128 groups x 64 targets of
+// One launch per block over all parameter sets, for blocks in the direct geometry with
+// 8-byte lanes (no target on address bits 0, 1).  Per tile (128 groups x 64 targets of
 // one set) it loads psi and lambda, writes both bf16 operand images and issues three
 // product sets on the tensor cores: psi U^+ and lambda U^+ (the un-compute, written back
 // in place) and the correlation D[m][n] = sum_g psi[g][m] lambda[g][n] over the tile's 128
@@ -1729,7 +1729,7 @@ void fused_geom_destroy(FusedGeom* g) { delete g; }
 bool fused_geom_interleaved(const FusedGeom* g) { return uses_interleaved_image(g->a.mode); }
 
 bool fused_geom_backward_ok(const FusedGeom* g) {
-  return g->a.k == 6 && g->a.mode == MODE_DIRECT && g->a.vec == 1 && (g->low & 0x1F) == 0;
+  return g->a.k == 6 && g->a.mode == MODE_DIRECT && g->a.vec == 1;
 }
 
 int fused_geom_launch_backward(const FusedGeom* geom, float2* psi, float2* lam, double* corr, int nsets, int n,
