@@ -773,8 +773,8 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
 }
 
 // ---- the tensor-core adjoint's fused backward pass --------------------------------------
-// One launch per block over all parameter sets, for blocks in the direct geometry with
-// 8-byte lanes (no target on address bits 0, 1).  Per tile (128 groups x 64 targets of
+// One launch per block over all parameter sets, for blocks in the direct geometry (8-,
+// 16- or 32-byte lanes as the block's low targets allow).  Per tile (128 groups x 64 targets of
 // one set) it loads psi and lambda, writes both bf16 operand images and issues three
 // product sets on the tensor cores: psi U^+ and lambda U^+ (the un-compute, written back
 // in place) and the correlation D[m][n] = sum_g psi[g][m] lambda[g][n] over the tile's 128
@@ -878,12 +878,35 @@ __global__ void __launch_bounds__(AB_THREADS, 1)
       const int item = it * AB_THREADS + tid;
       const uint64_t rb = base + dep(eb[item & (FB_M - 1)]);
       const int tg = item >> FB_BATCH_BITS;
+      if (g.vec == 4) {  // targets t..t+3 adjacent: 32-byte loads
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const uint64_t idx = rb + dep(et[tg * 8 + j]);
-        if (QSV_IN_BOUNDS(idx, lim)) {
-          bp[it][j] = __ldcs(a.psi + idx);
-          bl[it][j] = __ldcs(a.lam + idx);
+        for (int j = 0; j < 8; j += 4) {
+          const uint64_t idx = rb + dep(et[tg * 8 + j]);
+          if (QSV_IN_BOUNDS(idx + 3, lim)) {
+            ld_v8(a.psi + idx, &bp[it][j]);
+            ld_v8(a.lam + idx, &bl[it][j]);
+          }
+        }
+      } else if (g.vec == 2) {  // t, t+1 adjacent: 16-byte loads
+#pragma unroll
+        for (int j = 0; j < 8; j += 2) {
+          const uint64_t idx = rb + dep(et[tg * 8 + j]);
+          if (!QSV_IN_BOUNDS(idx + 1, lim)) continue;
+          const float4 vp = __ldcs(reinterpret_cast<const float4*>(a.psi + idx));
+          const float4 vl = __ldcs(reinterpret_cast<const float4*>(a.lam + idx));
+          bp[it][j] = make_float2(vp.x, vp.y);
+          bp[it][j + 1] = make_float2(vp.z, vp.w);
+          bl[it][j] = make_float2(vl.x, vl.y);
+          bl[it][j + 1] = make_float2(vl.z, vl.w);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const uint64_t idx = rb + dep(et[tg * 8 + j]);
+          if (QSV_IN_BOUNDS(idx, lim)) {
+            bp[it][j] = __ldcs(a.psi + idx);
+            bl[it][j] = __ldcs(a.lam + idx);
+          }
         }
       }
     }
@@ -965,10 +988,25 @@ __global__ void __launch_bounds__(AB_THREADS, 1)
     tmem_ld<16>(acc + lane_off + (uint32_t)t0, re);
     tmem_ld<16>(acc + lane_off + (uint32_t)(P::T + t0), im);
     tmem_ld_wait();
+    if (g.vec == 4) {
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      const uint64_t idx = rb + dep(et[t0 + j]);
-      if (QSV_IN_BOUNDS(idx, lim)) __stcs(dst + idx, make_float2(re[j], im[j]));
+      for (int j = 0; j < 16; j += 4) {
+        const uint64_t idx = rb + dep(et[t0 + j]);
+        if (QSV_IN_BOUNDS(idx + 3, lim)) st_v8(dst + idx, &re[j], &im[j]);
+      }
+    } else if (g.vec == 2) {
+#pragma unroll
+      for (int j = 0; j < 16; j += 2) {
+        const uint64_t idx = rb + dep(et[t0 + j]);
+        if (QSV_IN_BOUNDS(idx + 1, lim))
+          __stcs(reinterpret_cast<float4*>(dst + idx), make_float4(re[j], im[j], re[j + 1], im[j + 1]));
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const uint64_t idx = rb + dep(et[t0 + j]);
+        if (QSV_IN_BOUNDS(idx, lim)) __stcs(dst + idx, make_float2(re[j], im[j]));
+      }
     }
   };
   // Correlation: thread (lane row 32q + lane, columns 32h ..) adds its 32 entries.
@@ -1728,9 +1766,7 @@ void fused_geom_destroy(FusedGeom* g) { delete g; }
 
 bool fused_geom_interleaved(const FusedGeom* g) { return uses_interleaved_image(g->a.mode); }
 
-bool fused_geom_backward_ok(const FusedGeom* g) {
-  return g->a.k == 6 && g->a.mode == MODE_DIRECT && g->a.vec == 1;
-}
+bool fused_geom_backward_ok(const FusedGeom* g) { return g->a.k == 6 && g->a.mode == MODE_DIRECT; }
 
 int fused_geom_launch_backward(const FusedGeom* geom, float2* psi, float2* lam, double* corr, int nsets, int n,
                                const void* images, size_t img_stride, int* flag, cudaStream_t stream, int sm_count) {
