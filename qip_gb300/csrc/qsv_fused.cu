@@ -773,8 +773,8 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
 }
 
 // ---- the tensor-core adjoint's fused backward pass --------------------------------------
-// One launch per block over all parameter sets, for blocks in the direct geometry (8-,
-// 16- or 32-byte lanes as the block's low targets allow).  Per tile (128 groups x 64 targets of
+// One launch per block over all parameter sets, for blocks in the direct, prefix and pair
+// geometries.  Per tile (128 groups x 64 targets of
 // one set) it loads psi and lambda, writes both bf16 operand images and issues three
 // product sets on the tensor cores: psi U^+ and lambda U^+ (the un-compute, written back
 // in place) and the correlation D[m][n] = sum_g psi[g][m] lambda[g][n] over the tile's 128
@@ -803,10 +803,19 @@ constexpr int AB_GROUPS = 8;
 // slot and the abort flag.
 constexpr int AB_SMEM = 4 * FB<6>::A_BYTES + 2 * FB<6>::W_BYTES + FB_M * 2 + 64 * 2 + 64 * 8 + 64;
 
+// MODE: the block's access mode (direct, prefix, pair1, pair2; the last three multiply
+// transposed and take interleaved W images, as in k_block_tc).  Loads in the transposed
+// modes: 4 runs of 32 bytes per thread and state with the k_block_tc mappings spread over
+// 16 warps (prefix: group ((w%8)*8 + lane/4) | (w/8)*64, targets 4*((lane%4) + 4u) ..;
+// pair1: the k_block_tc pair1 roles with group bit 6 on warp bit 3; pair2: target bit 5 on
+// warp bit 3), exchanged as there.
+template <int MODE>
 __global__ void __launch_bounds__(AB_THREADS, 1)
     k_adj_back(const __grid_constant__ BlockArgs g, const __grid_constant__ AdjBackArgs a) {
   using P = FB<6>;
-  constexpr int ITEMS = (FB_M * (P::T / 8)) / AB_THREADS;  // 2
+  constexpr bool TRANS = MODE != MODE_DIRECT;
+  constexpr int PAIR = MODE == MODE_PAIR1 ? 1 : (MODE == MODE_PAIR2 ? 2 : 0);
+  constexpr int ITEMS = (FB_M * (P::T / 8)) / AB_THREADS;  // 2 (direct: (b, 8 targets) items)
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sP_hi = smem;
   uint8_t* sP_lo = smem + P::A_BYTES;
@@ -871,67 +880,166 @@ __global__ void __launch_bounds__(AB_THREADS, 1)
     return p.set * a.set_amps + qsv_insert_zeros(p.local, g.ptile, P::EBITS);
   };
   [[maybe_unused]] const uint64_t lim = a.set_amps * a.nsets;
-  float2 bp[ITEMS][8], bl[ITEMS][8];
+  // Transposed modes: load u's first group / target and the run held after the exchange.
+  auto lb = [&](int i) -> int { return (lane >> i) & 1; };
+  auto ld_b = [&](int u) -> int {
+    return PAIR == 0 ? (((warp & 7) << 3) | (lane >> 2) | ((warp >> 3) << 6))
+           : PAIR == 1 ? (lb(3) << 1) | (lb(4) << 2) | ((warp & 7) << 3) | ((warp >> 3) << 6)
+                       : (lb(3) << 2) | (lb(4) << 3) | ((warp & 7) << 4);
+  };
+  auto ld_t = [&](int u) -> int {
+    return PAIR == 0 ? 4 * ((lane & 3) | (u << 2))
+           : PAIR == 1 ? (lb(0) << 1) | (lb(1) << 2) | (lb(2) << 3) | (u << 4)
+                       : lb(0) | (lb(1) << 1) | (lb(2) << 2) | (u << 3) | ((warp >> 3) << 5);
+  };
+  auto held_b = [&](int u) -> int {
+    return PAIR == 0 ? ld_b(u)
+           : PAIR == 1 ? lb(0) | (lb(3) << 1) | (lb(4) << 2) | ((warp & 7) << 3) | ((warp >> 3) << 6)
+                       : lb(0) | (lb(1) << 1) | (lb(3) << 2) | (lb(4) << 3) | ((warp & 7) << 4);
+  };
+  auto held_q4 = [&](int u) -> int {
+    return PAIR == 0 ? (lane & 3) | (u << 2) : PAIR == 1 ? lb(1) | (lb(2) << 1) | (u << 2) : lb(2) | (u << 1) | ((warp >> 3) << 3);
+  };
+  float2 bp[16], bl[16];  // direct: item it, target j at [8*it + j]; transposed: run u, j at [4*u + j]
   auto load = [&](uint64_t base) {
+    if constexpr (TRANS) {
 #pragma unroll
-    for (int it = 0; it < ITEMS; ++it) {
-      const int item = it * AB_THREADS + tid;
-      const uint64_t rb = base + dep(eb[item & (FB_M - 1)]);
-      const int tg = item >> FB_BATCH_BITS;
-      if (g.vec == 4) {  // targets t..t+3 adjacent: 32-byte loads
+      for (int u = 0; u < 4; ++u) {
+        const uint64_t idx = base + dep(eb[ld_b(u)]) + dep(et[ld_t(u)]);
+        if (QSV_IN_BOUNDS(idx + 3, lim)) {
+          ld_v8(a.psi + idx, &bp[4 * u]);
+          ld_v8(a.lam + idx, &bl[4 * u]);
+        }
+      }
+    } else {
 #pragma unroll
-        for (int j = 0; j < 8; j += 4) {
-          const uint64_t idx = rb + dep(et[tg * 8 + j]);
-          if (QSV_IN_BOUNDS(idx + 3, lim)) {
-            ld_v8(a.psi + idx, &bp[it][j]);
-            ld_v8(a.lam + idx, &bl[it][j]);
+      for (int it = 0; it < ITEMS; ++it) {
+        const int item = it * AB_THREADS + tid;
+        const uint64_t rb = base + dep(eb[item & (FB_M - 1)]);
+        const int tg = item >> FB_BATCH_BITS;
+        if (g.vec == 4) {  // targets t..t+3 adjacent: 32-byte loads
+#pragma unroll
+          for (int j = 0; j < 8; j += 4) {
+            const uint64_t idx = rb + dep(et[tg * 8 + j]);
+            if (QSV_IN_BOUNDS(idx + 3, lim)) {
+              ld_v8(a.psi + idx, &bp[8 * it + j]);
+              ld_v8(a.lam + idx, &bl[8 * it + j]);
+            }
           }
-        }
-      } else if (g.vec == 2) {  // t, t+1 adjacent: 16-byte loads
+        } else if (g.vec == 2) {  // t, t+1 adjacent: 16-byte loads
 #pragma unroll
-        for (int j = 0; j < 8; j += 2) {
-          const uint64_t idx = rb + dep(et[tg * 8 + j]);
-          if (!QSV_IN_BOUNDS(idx + 1, lim)) continue;
-          const float4 vp = __ldcs(reinterpret_cast<const float4*>(a.psi + idx));
-          const float4 vl = __ldcs(reinterpret_cast<const float4*>(a.lam + idx));
-          bp[it][j] = make_float2(vp.x, vp.y);
-          bp[it][j + 1] = make_float2(vp.z, vp.w);
-          bl[it][j] = make_float2(vl.x, vl.y);
-          bl[it][j + 1] = make_float2(vl.z, vl.w);
-        }
-      } else {
+          for (int j = 0; j < 8; j += 2) {
+            const uint64_t idx = rb + dep(et[tg * 8 + j]);
+            if (!QSV_IN_BOUNDS(idx + 1, lim)) continue;
+            const float4 vp = __ldcs(reinterpret_cast<const float4*>(a.psi + idx));
+            const float4 vl = __ldcs(reinterpret_cast<const float4*>(a.lam + idx));
+            bp[8 * it + j] = make_float2(vp.x, vp.y);
+            bp[8 * it + j + 1] = make_float2(vp.z, vp.w);
+            bl[8 * it + j] = make_float2(vl.x, vl.y);
+            bl[8 * it + j + 1] = make_float2(vl.z, vl.w);
+          }
+        } else {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const uint64_t idx = rb + dep(et[tg * 8 + j]);
-          if (QSV_IN_BOUNDS(idx, lim)) {
-            bp[it][j] = __ldcs(a.psi + idx);
-            bl[it][j] = __ldcs(a.lam + idx);
+          for (int j = 0; j < 8; ++j) {
+            const uint64_t idx = rb + dep(et[tg * 8 + j]);
+            if (QSV_IN_BOUNDS(idx, lim)) {
+              bp[8 * it + j] = __ldcs(a.psi + idx);
+              bl[8 * it + j] = __ldcs(a.lam + idx);
+            }
           }
         }
       }
     }
   };
-  auto write_image = [&](const float2 (&buf)[ITEMS][8], uint8_t* hi, uint8_t* lo) {
+  // Pair modes: turn the loaded runs into runs of 4 targets of one group (as k_block_tc).
+  auto exchange = [&](float2* r) {
+    if constexpr (PAIR == 1) {
+      const bool up = lane & 1;
 #pragma unroll
-    for (int it = 0; it < ITEMS; ++it) {
-      const int item = it * AB_THREADS + tid;
-      const int b = item & (FB_M - 1);
-      const int tg = item >> FB_BATCH_BITS;
-      float re[8], im[8];
+      for (int u = 0; u < 4; ++u) {
+        float2* x = r + 4 * u;
+        const float2 y = x[1];
+        x[1] = x[2];
+        x[2] = y;
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        re[j] = buf[it][j].x;
-        im[j] = buf[it][j].y;
+        for (int j = 0; j < 2; ++j) {
+          const float2 send = up ? x[j] : x[j + 2];
+          float2 got;
+          got.x = __shfl_xor_sync(0xffffffffu, send.x, 1);
+          got.y = __shfl_xor_sync(0xffffffffu, send.y, 1);
+          if (up)
+            x[j] = got;
+          else
+            x[j + 2] = got;
+        }
       }
-      uint4 rh, rl, ih, il;
-      split8(re, rh, rl);
-      split8(im, ih, il);
-      const int off_re = tg * P::A_LBO + b * 16;
-      const int off_im = (P::T / 8 + tg) * P::A_LBO + b * 16;
-      *reinterpret_cast<uint4*>(hi + off_re) = rh;
-      *reinterpret_cast<uint4*>(lo + off_re) = rl;
-      *reinterpret_cast<uint4*>(hi + off_im) = ih;
-      *reinterpret_cast<uint4*>(lo + off_im) = il;
+    } else if constexpr (PAIR == 2) {
+#pragma unroll
+      for (int bb = 0; bb < 2; ++bb) {
+        const bool up = (lane >> bb) & 1;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          float2* x = r + 4 * u;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            if (j & (1 << bb)) continue;
+            const int j1 = j | (1 << bb);
+            const float2 send = up ? x[j] : x[j1];
+            float2 got;
+            got.x = __shfl_xor_sync(0xffffffffu, send.x, 1 << bb);
+            got.y = __shfl_xor_sync(0xffffffffu, send.y, 1 << bb);
+            if (up)
+              x[j] = got;
+            else
+              x[j1] = got;
+          }
+        }
+      }
+    }
+  };
+  auto write_image = [&](const float2* buf, uint8_t* hi, uint8_t* lo) {
+    if constexpr (TRANS) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int b = held_b(u), q4 = held_q4(u);
+        float re[4], im[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          re[j] = buf[4 * u + j].x;
+          im[j] = buf[4 * u + j].y;
+        }
+        uint2 rh, rl, ih, il;
+        split4(re, rh, rl);
+        split4(im, ih, il);
+        const int off_re = (q4 >> 1) * P::A_LBO + b * 16 + (q4 & 1) * 8;
+        const int off_im = off_re + (P::T / 8) * P::A_LBO;
+        *reinterpret_cast<uint2*>(hi + off_re) = rh;
+        *reinterpret_cast<uint2*>(lo + off_re) = rl;
+        *reinterpret_cast<uint2*>(hi + off_im) = ih;
+        *reinterpret_cast<uint2*>(lo + off_im) = il;
+      }
+    } else {
+#pragma unroll
+      for (int it = 0; it < ITEMS; ++it) {
+        const int item = it * AB_THREADS + tid;
+        const int b = item & (FB_M - 1);
+        const int tg = item >> FB_BATCH_BITS;
+        float re[8], im[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          re[j] = buf[8 * it + j].x;
+          im[j] = buf[8 * it + j].y;
+        }
+        uint4 rh, rl, ih, il;
+        split8(re, rh, rl);
+        split8(im, ih, il);
+        const int off_re = tg * P::A_LBO + b * 16;
+        const int off_im = (P::T / 8 + tg) * P::A_LBO + b * 16;
+        *reinterpret_cast<uint4*>(hi + off_re) = rh;
+        *reinterpret_cast<uint4*>(lo + off_re) = rl;
+        *reinterpret_cast<uint4*>(hi + off_im) = ih;
+        *reinterpret_cast<uint4*>(lo + off_im) = il;
+      }
     }
   };
   uint64_t cur_set = ~0ull;
@@ -950,19 +1058,21 @@ __global__ void __launch_bounds__(AB_THREADS, 1)
     const uint32_t wh = smem_u32(sW_hi), wl = smem_u32(sW_lo);
     constexpr int KS = P::KD / 16;  // 8 steps of 16 components (block products)
     auto blk = [&](uint32_t acc, uint32_t xh, uint32_t xl) {
+      auto mma = [&](uint32_t x, uint32_t w, int s, uint32_t accumulate) {
+        const uint64_t td = make_smem_desc(x + s * 2 * P::A_LBO, P::A_LBO, 128);
+        const uint64_t wd = make_smem_desc(w + s * 2 * P::W_LBO, P::W_LBO, 128);
+        if constexpr (TRANS)
+          tc_mma(acc, wd, td, idesc, accumulate);
+        else
+          tc_mma(acc, td, wd, idesc, accumulate);
+      };
       // Corrections first, main pass last (as in k_block_tc).
 #pragma unroll
-      for (int s = 0; s < KS; ++s)
-        tc_mma(acc, make_smem_desc(xh + s * 2 * P::A_LBO, P::A_LBO, 128),
-               make_smem_desc(wl + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, s > 0 ? 1u : 0u);
+      for (int s = 0; s < KS; ++s) mma(xh, wl, s, s > 0 ? 1u : 0u);
 #pragma unroll
-      for (int s = 0; s < KS; ++s)
-        tc_mma(acc, make_smem_desc(xl + s * 2 * P::A_LBO, P::A_LBO, 128),
-               make_smem_desc(wh + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, 1u);
+      for (int s = 0; s < KS; ++s) mma(xl, wh, s, 1u);
 #pragma unroll
-      for (int s = 0; s < KS; ++s)
-        tc_mma(acc, make_smem_desc(xh + s * 2 * P::A_LBO, P::A_LBO, 128),
-               make_smem_desc(wh + s * 2 * P::W_LBO, P::W_LBO, 128), idesc, 1u);
+      for (int s = 0; s < KS; ++s) mma(xh, wh, s, 1u);
     };
     blk(accP, ph, pl);
     blk(accL, lh, ll);
@@ -976,36 +1086,53 @@ __global__ void __launch_bounds__(AB_THREADS, 1)
     for (int s = 0; s < GS; ++s) tc_mma(accC, mn(ph, s), mn(lh, s), idesc_c, 1u);
     tc_commit(smem_u32(mbar));
   };
-  // Epilogue of a block product: warp w reads TMEM lanes 32*(w%4).. (groups) and target
-  // columns [16*(w/4), +16), and stores them over the state.
   const int q = warp & 3, h = warp >> 2;
   const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+  // Epilogue of a block product.  Direct: warp w reads TMEM lanes 32*(w%4).. (groups) and
+  // target columns [16*(w/4), +16).  Transposed: lane row 32q + lane is component lane%2
+  // of target (32q + lane)/2 and warp quarter h reads groups [32h, 32h + 32); lane pairs
+  // swap halves so the even lane keeps group b and the odd lane group b+1.
   auto store = [&](uint32_t acc, float2* dst, uint64_t base) {
-    const int b = q * 32 + lane;
-    const uint64_t rb = base + dep(eb[b]);
-    const int t0 = h * 16;
-    float re[16], im[16];
-    tmem_ld<16>(acc + lane_off + (uint32_t)t0, re);
-    tmem_ld<16>(acc + lane_off + (uint32_t)(P::T + t0), im);
-    tmem_ld_wait();
-    if (g.vec == 4) {
+    if constexpr (TRANS) {
+      const bool odd = lane & 1;
+      const uint64_t ot = dep(et[(q * 32 + lane) >> 1]);
+      float col[32];
+      tmem_ld<32>(acc + lane_off + (uint32_t)(h * 32), col);
+      tmem_ld_wait();
 #pragma unroll
-      for (int j = 0; j < 16; j += 4) {
-        const uint64_t idx = rb + dep(et[t0 + j]);
-        if (QSV_IN_BOUNDS(idx + 3, lim)) st_v8(dst + idx, &re[j], &im[j]);
-      }
-    } else if (g.vec == 2) {
-#pragma unroll
-      for (int j = 0; j < 16; j += 2) {
-        const uint64_t idx = rb + dep(et[t0 + j]);
-        if (QSV_IN_BOUNDS(idx + 1, lim))
-          __stcs(reinterpret_cast<float4*>(dst + idx), make_float4(re[j], im[j], re[j + 1], im[j + 1]));
+      for (int i = 0; i < 32; i += 2) {
+        const float got = __shfl_xor_sync(0xffffffffu, odd ? col[i] : col[i + 1], 1);
+        const int b = h * 32 + i + (odd ? 1 : 0);
+        const uint64_t idx = base + dep(eb[b]) + ot;
+        if (QSV_IN_BOUNDS(idx, lim)) __stcs(dst + idx, odd ? make_float2(got, col[i + 1]) : make_float2(col[i], got));
       }
     } else {
+      const int b = q * 32 + lane;
+      const uint64_t rb = base + dep(eb[b]);
+      const int t0 = h * 16;
+      float re[16], im[16];
+      tmem_ld<16>(acc + lane_off + (uint32_t)t0, re);
+      tmem_ld<16>(acc + lane_off + (uint32_t)(P::T + t0), im);
+      tmem_ld_wait();
+      if (g.vec == 4) {
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const uint64_t idx = rb + dep(et[t0 + j]);
-        if (QSV_IN_BOUNDS(idx, lim)) __stcs(dst + idx, make_float2(re[j], im[j]));
+        for (int j = 0; j < 16; j += 4) {
+          const uint64_t idx = rb + dep(et[t0 + j]);
+          if (QSV_IN_BOUNDS(idx + 3, lim)) st_v8(dst + idx, &re[j], &im[j]);
+        }
+      } else if (g.vec == 2) {
+#pragma unroll
+        for (int j = 0; j < 16; j += 2) {
+          const uint64_t idx = rb + dep(et[t0 + j]);
+          if (QSV_IN_BOUNDS(idx + 1, lim))
+            __stcs(reinterpret_cast<float4*>(dst + idx), make_float4(re[j], im[j], re[j + 1], im[j + 1]));
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const uint64_t idx = rb + dep(et[t0 + j]);
+          if (QSV_IN_BOUNDS(idx, lim)) __stcs(dst + idx, make_float2(re[j], im[j]));
+        }
       }
     }
   };
@@ -1061,6 +1188,8 @@ __global__ void __launch_bounds__(AB_THREADS, 1)
       cur_set = cu.set;
       load_w(cur_set);
     }
+    exchange(bp);
+    exchange(bl);
     write_image(bp, sP_hi, sP_lo);
     write_image(bl, sL_hi, sL_lo);
     fence_async_smem();
@@ -1766,17 +1895,26 @@ void fused_geom_destroy(FusedGeom* g) { delete g; }
 
 bool fused_geom_interleaved(const FusedGeom* g) { return uses_interleaved_image(g->a.mode); }
 
-bool fused_geom_backward_ok(const FusedGeom* g) { return g->a.k == 6 && g->a.mode == MODE_DIRECT; }
+bool fused_geom_backward_ok(const FusedGeom* g) {
+  const int m = g->a.mode;
+  return g->a.k == 6 && (m == MODE_DIRECT || m == MODE_PREFIX || m == MODE_PAIR1 || m == MODE_PAIR2);
+}
+
+template <int MODE>
+cudaError_t launch_adj_back(const BlockArgs& g, const AdjBackArgs& a, unsigned grid, cudaStream_t stream) {
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_adj_back<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, AB_SMEM);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  k_adj_back<MODE><<<grid, AB_THREADS, AB_SMEM, stream>>>(g, a);
+  return cudaGetLastError();
+}
 
 int fused_geom_launch_backward(const FusedGeom* geom, float2* psi, float2* lam, double* corr, int nsets, int n,
                                const void* images, size_t img_stride, int* flag, cudaStream_t stream, int sm_count) {
   if (!fused_geom_backward_ok(geom)) return QSV_ERR_UNSUPPORTED;
-  static bool configured = false;
-  if (!configured) {
-    if (cudaFuncSetAttribute(k_adj_back, cudaFuncAttributeMaxDynamicSharedMemorySize, AB_SMEM) != cudaSuccess)
-      return QSV_ERR_CUDA;
-    configured = true;
-  }
   AdjBackArgs a{};
   a.psi = psi;
   a.lam = lam;
@@ -1790,8 +1928,14 @@ int fused_geom_launch_backward(const FusedGeom* geom, float2* psi, float2* lam, 
   uint64_t grid = (uint64_t)std::max(1, sm_count);
   const uint64_t work = geom->a.ntiles * (uint64_t)nsets;
   if (grid > work) grid = work;
-  k_adj_back<<<(unsigned)grid, AB_THREADS, AB_SMEM, stream>>>(geom->a, a);
-  if (cudaGetLastError() != cudaSuccess) return QSV_ERR_CUDA;
+  cudaError_t e;
+  switch (geom->a.mode) {
+    case MODE_PREFIX: e = launch_adj_back<MODE_PREFIX>(geom->a, a, (unsigned)grid, stream); break;
+    case MODE_PAIR1: e = launch_adj_back<MODE_PAIR1>(geom->a, a, (unsigned)grid, stream); break;
+    case MODE_PAIR2: e = launch_adj_back<MODE_PAIR2>(geom->a, a, (unsigned)grid, stream); break;
+    default: e = launch_adj_back<MODE_DIRECT>(geom->a, a, (unsigned)grid, stream); break;
+  }
+  if (e != cudaSuccess) return QSV_ERR_CUDA;
   count_launch();
   return QSV_OK;
 }

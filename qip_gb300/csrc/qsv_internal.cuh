@@ -90,7 +90,7 @@ int fused_geom_launch_sets(const FusedGeom* g, float2* psi, int nsets, int n, co
 // The adjoint's fused backward pass for one block (k_adj_back): un-computes psi and lambda
 // in place with the U^+ images and adds the block's correlation into corr
 // ([nsets][128][128] FP64).  Only for geometries where fused_geom_backward_ok holds
-// (6 qubits in the direct access mode); QSV_ERR_UNSUPPORTED otherwise.
+// (6 qubits in the direct, prefix or pair access modes); QSV_ERR_UNSUPPORTED otherwise.
 bool fused_geom_backward_ok(const FusedGeom* g);
 int fused_geom_launch_backward(const FusedGeom* g, float2* psi, float2* lam, double* corr, int nsets, int n,
                                const void* images, size_t img_stride, int* flag, cudaStream_t stream, int sm_count);
