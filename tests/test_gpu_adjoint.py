@@ -78,6 +78,38 @@ def test_tensor_core_adjoint_matches_fp64_path(n, layers, B):
     numpy.testing.assert_allclose(g1.cpu().numpy(), g0.cpu().numpy(), atol=5e-5)
 
 
+def test_tensor_core_adjoint_three_launch_backward():
+    """Blocks whose placement class is pinned to the shuffle mode take the backward path
+    of correlation kernel + walk + two block launches (the fused pass covers the direct,
+    prefix and pair modes); gradients against the complex128 segment kernels."""
+    from qip_gb300 import GpuBackend, _native as nat
+
+    n, layers, B = 15, 3, 3
+    a = adjoint.Ansatz(n, layers)
+    lows = set()
+    for qs, _ in adjoint.block_partition(a):
+        low = sum(1 << (n - 1 - q) for q in qs if n - 1 - q < 7)
+        if len(qs) == 6 and 1 <= bin(low & 0x1F).count("1") <= 5:
+            lows.add(low)
+    assert lows
+    lib = nat.load()
+    st = GpuBackend.make_state(13, [], [], statetype=numpy.complex64, fusion=True, autotune=False)
+    adjoint._TC_PLANS.pop((n, layers), None)
+    try:
+        for low in lows:
+            nat.check(lib.qsv_set_block_mode(st.handle, 6, low, 2), st.handle, "set_block_mode")
+        th = torch.tensor(numpy.random.default_rng(7).uniform(0, 2 * numpy.pi, (B, a.nparams)), device="cuda")
+        e1, g1 = adjoint.energy_and_grad(th, a, torch.complex64, "tensor")
+        e0, g0 = adjoint.energy_and_grad(th, a, torch.complex128, "segmented")
+    finally:
+        for low in lows:
+            lib.qsv_set_block_mode(st.handle, 6, low, -1)
+        adjoint._TC_PLANS.pop((n, layers), None)
+        st.close()
+    numpy.testing.assert_allclose(e1.cpu().numpy(), e0.cpu().numpy(), atol=1e-5)
+    numpy.testing.assert_allclose(g1.cpu().numpy(), g0.cpu().numpy(), atol=5e-5)
+
+
 def test_tensor_core_adjoint_upstream_gradient_and_defaults():
     """complex64 at n >= 13 takes the tensor cores by default; the upstream gradient
     scales each set's row; a set with weight 0 gets zeros."""
