@@ -15,11 +15,13 @@
 //     Q_{j-1} = U_j^+ Q_j U_j,
 // over the block's gates j = m..1 (g runs over the 2^(n-6) groups of the other qubits,
 // A_j = U_m..U_{j+1}, psi_j = A_j^+ psi_out, lambda_j = A_j^+ lambda_out, so the sum
-// over groups is Tr(A_j P_j A_j^+ X) = Tr(P_j Q_j)).  k_adj_corr_d computes X as a real
-// GEMM on the tensor cores (K = the groups), k_adj_walk walks Q through the block's gates
-// in FP64 and writes the gradients, then psi and lambda are un-computed by U^+ with two
-// more fused-block launches.  Every block's gradients cost one correlation pass and two
-// block passes instead of a pass per gate.
+// over groups is Tr(A_j P_j A_j^+ X) = Tr(P_j Q_j)).  For blocks in the direct, prefix
+// and pair access modes one launch (k_adj_back, qsv_fused.cu) un-computes psi and lambda
+// with U^+ and computes X on the tensor cores from the same operand images; for the
+// others k_adj_corr_d computes X as a real GEMM (K = the groups) and two fused-block
+// launches un-compute psi and lambda.  k_adj_walk then walks Q through the block's gates
+// in FP64 and writes the gradients.  Every block's gradients cost one pass over psi and
+// lambda instead of a pass per gate.
 //
 // Local index convention: a block's qubits q_0 < ... < q_5; bit 5-j of a local index
 // (matrix row/column, X's indices) is qubit q_j, whose address bit is n-1-q_j.
