@@ -856,7 +856,8 @@ def measure_adjoint(args):
         "forward_s": tf, "backward_s": tb, "backward_over_forward": tb / tf,
         "grad_components_per_s": B * a.nparams / (tf + tb),
         "method": "tensor cores: 6-qubit blocks, per-set block images, correlation GEMM + FP64 walk per block",
-        "blocks": len(adjoint.tensor_core_plan(a).blocks), "cuda_core_segmented": seg,
+        "blocks": len(adjoint.tensor_core_plan(a).blocks),
+        "fused_backward_blocks": adjoint.tensor_core_plan(a).fused_blocks, "cuda_core_segmented": seg,
         "max_abs_grad": float(g.abs().max()),
         "fd_checked_angles": idx, "max_abs_err_vs_fd_c128": max(errs),
         "cpu_baseline": None, "cpu_baseline_note": "the reference has no gradient code (qip/backend.py:14-65)",

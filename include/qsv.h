@@ -320,7 +320,10 @@ int qsv_batch_segment_adjoint(void* psi, void* lam, int nsets, int n, int dtype,
  * qsv_adjoint_backward: psi = the final states, lam = H psi; for the blocks in reverse,
  * one tensor-core correlation X = sum_g psi[g] lam[g]^+ over the other qubits gives every
  * gradient of the block (dE/dtheta_j = Im Tr(P_j Q_j), Q walked through the block's gates
- * in FP64), added to grads[s * grad_stride + p]; then psi, lam <- U^+ psi, U^+ lam.
+ * in FP64), added to grads[s * grad_stride + p]; then psi, lam <- U^+ psi, U^+ lam.  For
+ * blocks in the direct, prefix and pair access modes the correlation and both un-computes
+ * are one pass over psi and lam; qsv_adjoint_plan_fused_blocks writes how many blocks of
+ * the plan take it to *out (the others use three passes).
  * scratch: caller-owned device memory of qsv_adjoint_scratch_bytes (per-set images and
  * correlations); psi, lam and scratch 256-byte aligned; work queued on `stream`.
  * qsv_adjoint_status synchronises and reports a bounded device wait that gave up
@@ -330,6 +333,7 @@ int qsv_adjoint_plan_create(int n, int nblocks, const int* block_qubits, const i
                             const int* gates, qsv_adjoint_plan** out);
 int qsv_adjoint_plan_destroy(qsv_adjoint_plan* p);
 size_t qsv_adjoint_scratch_bytes(const qsv_adjoint_plan* p, int nsets);
+int qsv_adjoint_plan_fused_blocks(const qsv_adjoint_plan* p, int* out);
 int qsv_adjoint_forward(qsv_adjoint_plan* p, void* psi, int nsets, const double* thetas, int nparams,
                         void* scratch, size_t scratch_bytes, void* stream);
 int qsv_adjoint_backward(qsv_adjoint_plan* p, void* psi, void* lam, int nsets, const double* thetas,

@@ -84,6 +84,7 @@ SIGNATURES = {
                                                ctypes.c_void_p, ctypes.c_void_p]),
     "qsv_adjoint_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "qsv_adjoint_scratch_bytes": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int]),
+    "qsv_adjoint_plan_fused_blocks": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
     "qsv_adjoint_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "qsv_adjoint_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,

@@ -296,6 +296,10 @@ class TensorCorePlan:
                "adjoint_plan_create")
         self.handle = h
         self.nparams = ansatz.nparams
+        fused = ctypes.c_int()
+        _check(lib.qsv_adjoint_plan_fused_blocks(h, ctypes.byref(fused)), "adjoint_plan_fused_blocks")
+        # Blocks whose backward is one pass (correlation and both un-computes together).
+        self.fused_blocks = fused.value
 
     def scratch(self, nsets: int, device) -> torch.Tensor:
         nbytes = int(nat.load().qsv_adjoint_scratch_bytes(self.handle, nsets))

@@ -844,6 +844,14 @@ extern "C" int qsv_adjoint_backward(qsv_adjoint_plan* p, void* psi, void* lam, i
   return QSV_OK;
 }
 
+extern "C" int qsv_adjoint_plan_fused_blocks(const qsv_adjoint_plan* p, int* out) {
+  if (!p || !out) return set_error(nullptr, QSV_ERR_INVALID, "null plan or output");
+  int count = 0;
+  for (FusedGeom* g : p->geom) count += fused_geom_backward_ok(g) ? 1 : 0;
+  *out = count;
+  return QSV_OK;
+}
+
 extern "C" int qsv_adjoint_status(qsv_adjoint_plan* p) {
   if (!p) return set_error(nullptr, QSV_ERR_INVALID, "null plan");
   int flag = 0;

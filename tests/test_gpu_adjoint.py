@@ -73,7 +73,8 @@ def test_tensor_core_adjoint_matches_fp64_path(n, layers, B):
     th = torch.tensor(numpy.random.default_rng(n).uniform(0, 2 * numpy.pi, (B, a.nparams)), device="cuda")
     e1, g1 = adjoint.energy_and_grad(th, a, torch.complex64, "tensor")
     e0, g0 = adjoint.energy_and_grad(th, a, torch.complex128, "segmented")
-    assert len(adjoint.tensor_core_plan(a).blocks) > 1
+    plan = adjoint.tensor_core_plan(a)
+    assert len(plan.blocks) > 1 and plan.fused_blocks > 0  # the one-pass backward is in use
     numpy.testing.assert_allclose(e1.cpu().numpy(), e0.cpu().numpy(), atol=1e-5)
     numpy.testing.assert_allclose(g1.cpu().numpy(), g0.cpu().numpy(), atol=5e-5)
 
@@ -101,6 +102,8 @@ def test_tensor_core_adjoint_three_launch_backward():
         th = torch.tensor(numpy.random.default_rng(7).uniform(0, 2 * numpy.pi, (B, a.nparams)), device="cuda")
         e1, g1 = adjoint.energy_and_grad(th, a, torch.complex64, "tensor")
         e0, g0 = adjoint.energy_and_grad(th, a, torch.complex128, "segmented")
+        plan = adjoint.tensor_core_plan(a)
+        assert 0 < plan.fused_blocks < len(plan.blocks)  # both backward paths in one sweep
     finally:
         for low in lows:
             lib.qsv_set_block_mode(st.handle, 6, low, -1)
