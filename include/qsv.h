@@ -324,8 +324,10 @@ int qsv_batch_segment_adjoint(void* psi, void* lam, int nsets, int n, int dtype,
  * blocks in the direct, prefix and pair access modes the correlation and both un-computes
  * are one pass over psi and lam; qsv_adjoint_plan_fused_blocks writes how many blocks of
  * the plan take it to *out (the others use three passes).
- * scratch: caller-owned device memory of qsv_adjoint_scratch_bytes (per-set images and
- * correlations); psi, lam and scratch 256-byte aligned; work queued on `stream`.
+ * scratch: caller-owned device memory of qsv_adjoint_scratch_bytes (per set one block
+ * image, and per block and set one 128 x 128 FP64 correlation, all walked to gradients in
+ * one launch at the end of the backward; nblocks <= 65535); psi, lam and scratch
+ * 256-byte aligned; work queued on `stream`.
  * qsv_adjoint_status synchronises and reports a bounded device wait that gave up
  * (QSV_ERR_TIMEOUT).  Errors: qsv_last_error(NULL). */
 typedef struct qsv_adjoint_plan qsv_adjoint_plan;

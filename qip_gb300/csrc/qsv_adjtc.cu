@@ -507,19 +507,22 @@ __global__ void __launch_bounds__(CORR_THREADS, 1) k_adj_corr_d(const __grid_con
 }
 
 // ---- the gradient walk -----------------------------------------------------------------
-// grid = nsets.  Q = X from corr[set] (which is then cleared for the next block); for the
-// block's gates from last to first: a rotation adds Im Tr(P Q) to its parameter's
-// gradient (P = Y for RY, Z for RZ, on the gate's local bit), then Q <- U^+ Q U.  FP64.
+// One launch for every block of the backward: grid = (nsets, nblocks), CTA (s, b) walks
+// block b for set s from corr[b][s] (each block has its own correlation slice, so the walks
+// are independent).  Q = X; for the block's gates from last to first: a rotation adds
+// Im Tr(P Q) to its parameter's gradient (P = Y for RY, Z for RZ, on the gate's local bit;
+// FP64 atomics, as gates of several blocks may share a parameter), then Q <- U^+ Q U.
 __global__ void __launch_bounds__(A_THREADS)
-    k_adj_walk(const AdjBlockDev* __restrict__ blk, const AdjGate* __restrict__ gates,
-               const double* __restrict__ thetas, int nparams, double* __restrict__ corr,
+    k_adj_walk(const AdjBlockDev* __restrict__ blocks, const AdjGate* __restrict__ gates,
+               const double* __restrict__ thetas, int nparams, const double* __restrict__ corr,
                double* __restrict__ grads, int grad_stride) {
   extern __shared__ __align__(16) uint8_t wsm[];
   double2(*Q)[AT] = reinterpret_cast<double2(*)[AT]>(wsm);
   __shared__ double red[32];
   const int tid = threadIdx.x;
   const int set = blockIdx.x;
-  double* D = corr + (size_t)set * AKD * AKD;
+  const AdjBlockDev* blk = blocks + blockIdx.y;
+  const double* D = corr + ((size_t)blockIdx.y * gridDim.x + set) * AKD * AKD;
   for (int i = tid; i < AT * AT; i += A_THREADS) {
     const int b = i / AT, c = i % AT;
     const double re = D[b * AKD + c] + D[(AT + b) * AKD + AT + c];
@@ -527,7 +530,6 @@ __global__ void __launch_bounds__(A_THREADS)
     Q[b][c] = make_double2(re, im);
   }
   __syncthreads();
-  for (int i = tid; i < AKD * AKD; i += A_THREADS) D[i] = 0.0;
   for (int g = blk->ngates - 1; g >= 0; --g) {
     const AdjGate G = gates[blk->first_gate + g];
     const int tb = 1 << G.t;
@@ -546,7 +548,7 @@ __global__ void __launch_bounds__(A_THREADS)
         if ((tid & 31) == 0) red[tid >> 5] = part;
       }
       __syncthreads();
-      if (tid == 0) grads[(size_t)set * grad_stride + G.param] += red[0] + red[1];
+      if (tid == 0) atomicAdd(&grads[(size_t)set * grad_stride + G.param], red[0] + red[1]);
       // U^+ Q U for the rotation u.
       double2 u[4];
       rot_matrix(G.kind, thetas[(size_t)set * nparams + G.param], u);
@@ -633,7 +635,8 @@ extern "C" int qsv_adjoint_plan_create(int n, int nblocks, const int* block_qubi
   if (!out) return set_error(nullptr, QSV_ERR_INVALID, "null plan output");
   *out = nullptr;
   if (n < AK + 7 || n > 34) return set_error(nullptr, QSV_ERR_UNSUPPORTED, "tensor-core adjoint needs 13 <= n <= 34");
-  if (nblocks < 1 || !block_qubits || !block_ngates || !gates) return set_error(nullptr, QSV_ERR_INVALID, "bad plan");
+  if (nblocks < 1 || nblocks > 65535 || !block_qubits || !block_ngates || !gates)
+    return set_error(nullptr, QSV_ERR_INVALID, "bad plan (1..65535 blocks)");
   auto* p = new (std::nothrow) qsv_adjoint_plan();
   if (!p) return set_error(nullptr, QSV_ERR_OOM, "host allocation failed");
   p->n = n;
@@ -733,7 +736,8 @@ extern "C" int qsv_adjoint_plan_destroy(qsv_adjoint_plan* p) {
 
 extern "C" size_t qsv_adjoint_scratch_bytes(const qsv_adjoint_plan* p, int nsets) {
   if (!p || nsets < 1) return 0;
-  return (size_t)nsets * (image_stride() + (size_t)AKD * AKD * sizeof(double));
+  // Per set one W image, and per block and set one 128 x 128 FP64 correlation.
+  return (size_t)nsets * (image_stride() + (size_t)p->nblocks * AKD * AKD * sizeof(double));
 }
 
 namespace {
@@ -789,13 +793,14 @@ extern "C" int qsv_adjoint_backward(qsv_adjoint_plan* p, void* psi, void* lam, i
     return set_error(nullptr, QSV_ERR_INVALID, "bad lambda or gradient buffer");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   uint8_t* images = static_cast<uint8_t*>(scratch);
-  double* corr = reinterpret_cast<double*>(images + (size_t)nsets * image_stride());
-  QSV_CUDA(nullptr, cudaMemsetAsync(corr, 0, (size_t)nsets * AKD * AKD * sizeof(double), st));
+  // Correlations: one [nsets][128][128] slice per block, all walked in one launch at the end.
+  double* corr_all = reinterpret_cast<double*>(images + (size_t)nsets * image_stride());
+  const size_t slice = (size_t)nsets * AKD * AKD;
+  QSV_CUDA(nullptr, cudaMemsetAsync(corr_all, 0, (size_t)p->nblocks * slice * sizeof(double), st));
   float2* states[2] = {static_cast<float2*>(psi), static_cast<float2*>(lam)};
   CorrArgs ca{};
   ca.psi = states[0];
   ca.lam = states[1];
-  ca.corr = corr;
   ca.tile_shift = p->n - 12;
   ca.ntiles = (uint64_t)nsets << ca.tile_shift;
   ca.n = p->n;
@@ -811,8 +816,10 @@ extern "C" int qsv_adjoint_backward(qsv_adjoint_plan* p, void* psi, void* lam, i
   const unsigned grid_direct = grid_of((const void*)k_adj_corr_d<0>, CORRD_SMEM);
   for (int b = p->nblocks - 1; b >= 0; --b) {
     ca.blk = p->d_blocks + b;
+    double* corr = corr_all + (size_t)b * slice;
+    ca.corr = corr;
     if (fused_geom_backward_ok(p->geom[(size_t)b])) {
-      // One pass: U^+ images, then un-compute and correlation together, then the walk.
+      // One pass: U^+ images, then un-compute and correlation together.
       k_adj_images<true><<<nsets, A_THREADS, 0, st>>>(p->d_blocks + b, p->d_gates, thetas, nparams, images,
                                                      image_stride());
       rc = check_stream_launch("adjoint images");
@@ -820,10 +827,6 @@ extern "C" int qsv_adjoint_backward(qsv_adjoint_plan* p, void* psi, void* lam, i
       rc = fused_geom_launch_backward(p->geom[(size_t)b], states[0], states[1], corr, nsets, p->n, images,
                                       image_stride(), p->d_flag, st, p->sm_count);
       if (rc) return set_error(nullptr, rc, "adjoint backward launch failed");
-      k_adj_walk<<<nsets, A_THREADS, AT * AT * sizeof(double2), st>>>(p->d_blocks + b, p->d_gates, thetas, nparams,
-                                                                      corr, grads, grad_stride);
-      rc = check_stream_launch("adjoint walk");
-      if (rc) return rc;
       continue;
     }
     switch (p->corr_kind[(size_t)b]) {
@@ -834,14 +837,13 @@ extern "C" int qsv_adjoint_backward(qsv_adjoint_plan* p, void* psi, void* lam, i
     }
     rc = check_stream_launch("adjoint correlation");
     if (rc) return rc;
-    k_adj_walk<<<nsets, A_THREADS, AT * AT * sizeof(double2), st>>>(p->d_blocks + b, p->d_gates, thetas, nparams,
-                                                                    corr, grads, grad_stride);
-    rc = check_stream_launch("adjoint walk");
-    if (rc) return rc;
     rc = apply_block(p, b, true, states, 2, nsets, thetas, nparams, images, st);
     if (rc) return rc;
   }
-  return QSV_OK;
+  // Every block's gradients from its correlation, in one launch.
+  k_adj_walk<<<dim3((unsigned)nsets, (unsigned)p->nblocks), A_THREADS, AT * AT * sizeof(double2), st>>>(
+      p->d_blocks, p->d_gates, thetas, nparams, corr_all, grads, grad_stride);
+  return check_stream_launch("adjoint walk");
 }
 
 extern "C" int qsv_adjoint_plan_fused_blocks(const qsv_adjoint_plan* p, int* out) {
