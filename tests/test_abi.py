@@ -71,3 +71,20 @@ def test_normal_build_is_not_the_bounds_checked_one():
 
     count, first = ctypes.c_ulonglong(), ctypes.c_ulonglong()
     assert _native.load().qsv_bounds_report(ctypes.byref(count), ctypes.byref(first)) == _native.QSV_ERR_UNSUPPORTED
+
+
+def test_adjoint_plan_queries_check_their_arguments_without_a_device():
+    """The adjoint plan's host-side queries reject a null plan or output before any
+    device call (the scratch size of a null plan is 0)."""
+    from qip_gb300 import _native
+
+    lib = _native.load()
+    out = ctypes.c_int(-1)
+    assert lib.qsv_adjoint_plan_fused_blocks(None, ctypes.byref(out)) == _native.QSV_ERR_INVALID
+    assert out.value == -1
+    assert lib.qsv_adjoint_scratch_bytes(None, 64) == 0
+    bad = ctypes.c_void_p()
+    # Too many blocks for one walk launch (grid y <= 65535) or none at all.
+    assert lib.qsv_adjoint_plan_create(24, 0, None, None, None, ctypes.byref(bad)) == _native.QSV_ERR_INVALID
+    assert lib.qsv_adjoint_plan_create(24, 65536, None, None, None, ctypes.byref(bad)) == _native.QSV_ERR_INVALID
+    assert not bad.value
