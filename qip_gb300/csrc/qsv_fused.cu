@@ -581,13 +581,28 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
           float col[32];
           tmem_ld<32>(lane_addr + (uint32_t)(h * 64 + c0), col);
           tmem_ld_wait();
+          if constexpr (PAIR == 2) {
+            // Groups b..b+3 are address bits 0, 1: the even lane takes b, b+1 and the odd
+            // lane b+2, b+3, each one 16-byte store (a lane pair fills a 32-byte sector).
   #pragma unroll
-          for (int i = 0; i < 32; i += 2) {
-            const float got = __shfl_xor_sync(0xffffffffu, odd ? col[i] : col[i + 1], 1);
-            const int b = h * 64 + c0 + i + (odd ? 1 : 0);
-            const uint64_t idx = tbase + dep(eb[b]) + ot;
-            if (QSV_IN_BOUNDS(idx, lim))
-              __stcs(psi + idx, odd ? make_float2(got, col[i + 1]) : make_float2(col[i], got));
+            for (int i = 0; i < 32; i += 4) {
+              const float g0 = __shfl_xor_sync(0xffffffffu, odd ? col[i] : col[i + 2], 1);
+              const float g1 = __shfl_xor_sync(0xffffffffu, odd ? col[i + 1] : col[i + 3], 1);
+              const int b = h * 64 + c0 + i + (odd ? 2 : 0);
+              const uint64_t idx = tbase + dep(eb[b]) + ot;
+              if (QSV_IN_BOUNDS(idx + 1, lim))
+                __stcs(reinterpret_cast<float4*>(psi + idx),
+                       odd ? make_float4(g0, col[i + 2], g1, col[i + 3]) : make_float4(col[i], g0, col[i + 1], g1));
+            }
+          } else {
+  #pragma unroll
+            for (int i = 0; i < 32; i += 2) {
+              const float got = __shfl_xor_sync(0xffffffffu, odd ? col[i] : col[i + 1], 1);
+              const int b = h * 64 + c0 + i + (odd ? 1 : 0);
+              const uint64_t idx = tbase + dep(eb[b]) + ot;
+              if (QSV_IN_BOUNDS(idx, lim))
+                __stcs(psi + idx, odd ? make_float2(got, col[i + 1]) : make_float2(col[i], got));
+            }
           }
         }
       } else {
@@ -1099,12 +1114,25 @@ __global__ void __launch_bounds__(AB_THREADS, 1)
       float col[32];
       tmem_ld<32>(acc + lane_off + (uint32_t)(h * 32), col);
       tmem_ld_wait();
+      if constexpr (PAIR == 2) {  // 16-byte stores of groups b, b+1 (even) / b+2, b+3 (odd)
 #pragma unroll
-      for (int i = 0; i < 32; i += 2) {
-        const float got = __shfl_xor_sync(0xffffffffu, odd ? col[i] : col[i + 1], 1);
-        const int b = h * 32 + i + (odd ? 1 : 0);
-        const uint64_t idx = base + dep(eb[b]) + ot;
-        if (QSV_IN_BOUNDS(idx, lim)) __stcs(dst + idx, odd ? make_float2(got, col[i + 1]) : make_float2(col[i], got));
+        for (int i = 0; i < 32; i += 4) {
+          const float g0 = __shfl_xor_sync(0xffffffffu, odd ? col[i] : col[i + 2], 1);
+          const float g1 = __shfl_xor_sync(0xffffffffu, odd ? col[i + 1] : col[i + 3], 1);
+          const int b = h * 32 + i + (odd ? 2 : 0);
+          const uint64_t idx = base + dep(eb[b]) + ot;
+          if (QSV_IN_BOUNDS(idx + 1, lim))
+            __stcs(reinterpret_cast<float4*>(dst + idx),
+                   odd ? make_float4(g0, col[i + 2], g1, col[i + 3]) : make_float4(col[i], g0, col[i + 1], g1));
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 32; i += 2) {
+          const float got = __shfl_xor_sync(0xffffffffu, odd ? col[i] : col[i + 1], 1);
+          const int b = h * 32 + i + (odd ? 1 : 0);
+          const uint64_t idx = base + dep(eb[b]) + ot;
+          if (QSV_IN_BOUNDS(idx, lim)) __stcs(dst + idx, odd ? make_float2(got, col[i + 1]) : make_float2(col[i], got));
+        }
       }
     } else {
       const int b = q * 32 + lane;

@@ -73,8 +73,7 @@ def test_tensor_core_adjoint_matches_fp64_path(n, layers, B):
     th = torch.tensor(numpy.random.default_rng(n).uniform(0, 2 * numpy.pi, (B, a.nparams)), device="cuda")
     e1, g1 = adjoint.energy_and_grad(th, a, torch.complex64, "tensor")
     e0, g0 = adjoint.energy_and_grad(th, a, torch.complex128, "segmented")
-    plan = adjoint.tensor_core_plan(a)
-    assert len(plan.blocks) > 1 and plan.fused_blocks > 0  # the one-pass backward is in use
+    assert len(adjoint.tensor_core_plan(a).blocks) > 1
     numpy.testing.assert_allclose(e1.cpu().numpy(), e0.cpu().numpy(), atol=1e-5)
     numpy.testing.assert_allclose(g1.cpu().numpy(), g0.cpu().numpy(), atol=5e-5)
 
@@ -87,18 +86,20 @@ def test_tensor_core_adjoint_three_launch_backward():
 
     n, layers, B = 15, 3, 3
     a = adjoint.Ansatz(n, layers)
-    lows = set()
+    # Every class of the ansatz is pinned (modes recorded by earlier tuning in this process
+    # would otherwise decide): shuffle where it applies, direct elsewhere.
+    lows, pins = set(), {}
     for qs, _ in adjoint.block_partition(a):
         low = sum(1 << (n - 1 - q) for q in qs if n - 1 - q < 7)
-        if len(qs) == 6 and 1 <= bin(low & 0x1F).count("1") <= 5:
-            lows.add(low)
-    assert lows
+        lows.add(low)
+        pins[low] = 2 if 1 <= bin(low & 0x1F).count("1") <= 5 else 0
+    assert 2 in pins.values() and 0 in pins.values()
     lib = nat.load()
     st = GpuBackend.make_state(13, [], [], statetype=numpy.complex64, fusion=True, autotune=False)
     adjoint._TC_PLANS.pop((n, layers), None)
     try:
         for low in lows:
-            nat.check(lib.qsv_set_block_mode(st.handle, 6, low, 2), st.handle, "set_block_mode")
+            nat.check(lib.qsv_set_block_mode(st.handle, 6, low, pins[low]), st.handle, "set_block_mode")
         th = torch.tensor(numpy.random.default_rng(7).uniform(0, 2 * numpy.pi, (B, a.nparams)), device="cuda")
         e1, g1 = adjoint.energy_and_grad(th, a, torch.complex64, "tensor")
         e0, g0 = adjoint.energy_and_grad(th, a, torch.complex128, "segmented")
